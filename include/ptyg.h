@@ -1,0 +1,181 @@
+/*
+ * ptyg.h -- C ABI of libptyg.so, the GB300 (sm_103a) kernels behind the
+ * ptylab_gb300 drop-in for PtyLab's per-position reconstruction loop.
+ *
+ * Plain C types only: every array argument is a device pointer (CUDA global
+ * memory on the current device) unless its comment says "host".  complex64
+ * data is interleaved (re, im) float pairs, C-contiguous, in PtyLab's 6-D
+ * layout with nlambda = 1:
+ *   object      (nosm, nslice, No, No)      PtyLab/Reconstruction/Reconstruction.py:362-374
+ *   probe       (npsm, nslice, Np, Np)      PtyLab/Reconstruction/Reconstruction.py:395-413
+ *   ptychogram  float32 (numFrames, Np, Np) PtyLab/ExperimentalData/ExperimentalData.py:234-250
+ *   positions   int32 (numFrames, 2) = (row, col) of the patch corner
+ *               PtyLab/Reconstruction/Reconstruction.py:676-710
+ * Streams are passed as `void*` (a cudaStream_t; NULL = legacy default stream).
+ *
+ * Every function returns PTYG_OK (0) or a negative status; the message of the
+ * last failure on the calling thread is available from ptyg_last_error().
+ * No C++ exception crosses this boundary.
+ */
+#ifndef PTYG_H
+#define PTYG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PTYG_API __attribute__((visibility("default")))
+#else
+#define PTYG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTYG_VERSION 1000 /* 0.1.0 */
+
+enum ptyg_status {
+  PTYG_OK = 0,
+  PTYG_ERR_INVALID = -1,     /* bad argument (maps to ValueError)            */
+  PTYG_ERR_UNSUPPORTED = -2, /* valid in PtyLab, not on this path (NotImplementedError) */
+  PTYG_ERR_OOM = -3,         /* device allocation failed (MemoryError)       */
+  PTYG_ERR_CUDA = -4,        /* CUDA runtime error (RuntimeError)            */
+  PTYG_ERR_TIMEOUT = -5,     /* a bounded device wait gave up (TimeoutError) */
+  PTYG_ERR_DEVICE = -6       /* no usable sm_103a device (ImportError)       */
+};
+
+enum ptyg_engine { PTYG_EPIE = 0, PTYG_MPIE = 1, PTYG_QNEWTON = 2, PTYG_E3PIE = 3 };
+enum ptyg_propagator { PTYG_FRAUNHOFER = 0, PTYG_FRESNEL = 1, PTYG_ASP = 2 };
+enum ptyg_direction { PTYG_FORWARD = 0, PTYG_INVERSE = 1 };
+
+/* Library version (PTYG_VERSION of the build). */
+PTYG_API int ptyg_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+PTYG_API const char* ptyg_last_error(void);
+
+/* Select `device`, check it is a compute-capability 10.3 GPU and build the
+ * per-device twiddle tables.  Replaces the cupy probe of
+ * PtyLab/Params/Params.py:10-28 (gpuSwitch availability). */
+PTYG_API int ptyg_device_init(int device);
+
+/* ------------------------------------------------------------------------
+ * Propagators: the drop-in for Operators.object2detector / detector2object
+ * (PtyLab/Operators/Operators.py:561-584) on `batch` fields of Np x Np.
+ *   FRAUNHOFER  fft2c / ifft2c                    Operators.py:27-74
+ *   FRESNEL     fft2c(x*Q) / ifft2c(X)*conj(Q)     Operators.py:77-152
+ *   ASP         ifft2(fft2(x)*H) (conj H inverse)  Operators.py:155-230
+ * `table`: FRESNEL -> Q (Np*Np complex64, natural order); ASP -> the
+ * ifftshifted transfer function (Np*Np complex64); FRAUNHOFER -> NULL.
+ * `fftshift` != 0 selects uncentred transforms (params.fftshiftSwitch).
+ * `scratch`: batch*Np*Np complex64 of device memory, or NULL to let the call
+ * allocate (stream-ordered) and free it.  in == out is allowed.
+ * Np must be 32, 64, 128 or 256. */
+PTYG_API int ptyg_propagate(int propagator, int direction, int fftshift, int Np, int batch, const void* in, void* out,
+                   const void* table, void* scratch, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Engine plans: the drop-in for the position loop of ePIE.reconstruct_stepwise
+ * (PtyLab/Engines/ePIE.py:78-112), mPIE.reconstruct (mPIE.py:276-333),
+ * qNewton.reconstruct (qNewton.py:67-90) and e3PIE.reconstruct
+ * (e3PIE.py:229-313), with BaseEngine.intensityProjection
+ * (BaseEngine.py:870-1012) and getRMSD (BaseEngine.py:843-868).
+ */
+typedef struct ptyg_geometry {
+  int32_t Np;          /* probe/detector size: 32, 64, 128, 256 */
+  int32_t No;          /* object size, >= Np */
+  int32_t nosm;        /* object modes */
+  int32_t npsm;        /* probe modes */
+  int32_t nslice;      /* slices (e3PIE), else 1 */
+  int32_t num_frames;  /* diffraction patterns per scan */
+  int32_t num_scans;   /* independent scans reconstructed side by side (>= 1) */
+  int32_t engine;      /* enum ptyg_engine */
+  int32_t propagator;  /* enum ptyg_propagator */
+  int32_t fftshift;    /* params.fftshiftSwitch: uncentred transforms, pre-shifted data */
+  int32_t fpm;         /* operationMode == "FPM" (mPIE object step, mPIE.py:237-243) */
+  int32_t cluster;     /* CTAs per scan (0 = choose) */
+} ptyg_geometry;
+
+/* Engine scalars (ePIE.py:35-42, mPIE.py:233-245, qNewton.py:43-52,
+ * e3PIE.py:186-195); probe_weight is mPIE's per-update weight (1). */
+typedef struct ptyg_update_params {
+  float beta_object, beta_probe;
+  float alpha_object, alpha_probe;
+  float reg_object, reg_probe;
+  float friction, feedback;
+  float probe_weight;
+  float slice_beta; /* e3PIE probe step for slices >= 1 (0.9 in e3PIE.py:280) */
+} ptyg_update_params;
+
+/* Caller-owned device buffers of one scan.  Momentum/buffer pointers are
+ * needed by mPIE only; momentum_flags by mPIE only (one byte per order slot,
+ * nonzero -> momentum step after that position, mPIE.py:330-332). */
+typedef struct ptyg_scan_buffers {
+  void* object;
+  void* probe;
+  const int32_t* positions;
+  const int32_t* order;
+  const uint8_t* momentum_flags;
+  void* object_buffer;
+  void* object_momentum;
+  void* probe_buffer;
+  void* probe_momentum;
+} ptyg_scan_buffers;
+
+typedef struct ptyg_plan ptyg_plan;
+
+/* Validate the geometry and allocate the plan's scratch (transposition
+ * buffers, reduction slots, error partials, the layout-converted ptychogram). */
+PTYG_API int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan);
+PTYG_API int ptyg_plan_destroy(ptyg_plan* plan);
+
+/* Host complex64 tables, Np*Np each, centred (DC at Np/2), built in double
+ * and rounded as PtyLab builds them; NULL where the configuration needs none:
+ *   fresnel_q  __make_quad_phase      (Operators/_propagation_kernels.py:16-36)
+ *   asp_h      __aspw_transfer_function at zo (Operators.py:631-684, 861-893)
+ *   slice_h    aspw at dz, wavelength/refrIndex (e3PIE.py:62-69) */
+PTYG_API int ptyg_plan_set_tables(ptyg_plan* plan, const void* fresnel_q, const void* asp_h, const void* slice_h);
+
+/* Bind scan `scan`'s buffers and load its measured intensities (device
+ * float32, natural layout, already fftshifted by the caller when fftshift). */
+PTYG_API int ptyg_plan_bind_scan(ptyg_plan* plan, int scan, const ptyg_scan_buffers* buffers, const float* ptychogram,
+                        void* stream);
+
+/* Process order slots [start, start+count) of every bound scan: for each
+ * slot, position order[slot] goes through gather -> propagate -> intensity
+ * projection -> back-propagate -> object/probe update (-> momentum step).
+ * flags bit 0: also record |I_meas - I_est| per pixel (detectorError). */
+PTYG_API int ptyg_plan_run(ptyg_plan* plan, const ptyg_update_params* params, int start, int count, int flags, void* stream);
+
+/* Per-frame sum_xy |I_meas - I_est| of the frames processed since the plan
+ * was bound (FP64), into `host_out` (num_frames doubles); synchronises. */
+PTYG_API int ptyg_plan_frame_errors(ptyg_plan* plan, int scan, double* host_out, void* stream);
+
+/* The recorded |I_meas - I_est| maps (flags bit 0) in natural layout:
+ * `out` is device float32 (num_frames, Np, Np). */
+PTYG_API int ptyg_plan_detector_error(ptyg_plan* plan, int scan, float* out, void* stream);
+
+/* Device status word of scan `scan` (0 = ok; 2 = a position fell outside
+ * the object and was skipped). */
+PTYG_API int ptyg_plan_status(ptyg_plan* plan, int scan, int* host_status, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Small per-iteration helpers of BaseEngine.applyConstraints
+ * (BaseEngine.py:1440-1612) and orthogonalizeModes (utils.py:130-211).
+ */
+/* x[i] *= w[i % n_window] for complex64 x (n elements), float32 window. */
+PTYG_API int ptyg_mul_window(void* x, const float* window, int64_t n, int64_t n_window, void* stream);
+
+/* Gram matrix G[a][b] = sum_i conj(p[a][i]) * p[b][i] of `modes` complex64
+ * vectors of length n, accumulated in FP64 into `gram` (device complex128). */
+PTYG_API int ptyg_gram(const void* p, int modes, int64_t n, void* gram, void* stream);
+
+/* out[a][i] = sum_b V[a][b] * p[b][i]; V is device complex64 modes x modes. */
+PTYG_API int ptyg_mix_modes(const void* V, const void* p, void* out, int modes, int64_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PTYG_H */

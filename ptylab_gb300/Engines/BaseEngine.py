@@ -1,0 +1,452 @@
+"""Host control of the GB300 engines, mirroring PtyLab's ``BaseEngine``
+(PtyLab/Engines/BaseEngine.py:69-1858) for the per-position path.
+
+What stays on the host, as in the reference: switch validation, the
+fftshift of the data, the position order (same NumPy calls, same global RNG),
+the per-iteration error metric and the in-scope constraints.  What moves to
+the GPU: the whole walk over the scan positions of an iteration, which is one
+``ptyg_plan_run`` launch (libptyg.so, sm_103a), and the constraint kernels.
+
+State lives in torch CUDA tensors while ``reconstruct()`` runs
+(``reconstruction.object`` / ``.probe`` and, for mPIE, the buffers and
+momenta are replaced by device tensors, as the reference replaces them by CuPy
+arrays) and is written back as NumPy complex64 arrays at the end
+(ePIE.py:123-126).  There is no CPU code path: without libptyg.so and an
+sm_103a device every engine raises ImportError.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import logging
+
+import numpy as np
+
+from .. import _native, _tables
+from ..Reconstruction import circ
+
+# Switches whose branches are not on this path; PtyLab default for all is off.
+_UNSUPPORTED = (
+    "backgroundModeSwitch",
+    "CPSCswitch",
+    "FourierMaskSwitch",
+    "adaptiveDenoisingSwitch",
+    "positionCorrectionSwitch",
+    "OPRP",
+    "objectTVregSwitch",
+    "modulusEnforcedProbeSwitch",
+    "l2reg",
+    "probeSpectralPowerCorrectionSwitch",
+    "probeSmoothenessSwitch",
+    "objectSmoothenessSwitch",
+    "absObjectSwitch",
+    "absProbeSwitch",
+    "objectContrastSwitch",
+    "couplingSwitch",
+    "binaryProbeSwitch",
+    "PSDestimationSwitch",
+    "TV_autofocus",
+    "map_position_to_z_change",
+    "intensityMask",
+)
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class BaseEngine(object):
+    engine_name = "BaseEngine"
+
+    def __init__(self, reconstruction, experimentalData, params, monitor):
+        self.betaObject = 0.25
+        self.reconstruction = reconstruction
+        self.experimentalData = experimentalData
+        self.params = params
+        self.monitor = monitor
+        try:
+            self.monitor.reconstruction = reconstruction
+        except AttributeError:
+            pass
+        self.logger = logging.getLogger(self.engine_name)
+        self._plan = None
+        self._dev = {}
+
+    # --------------------------------------------------------- validation
+    def _check_supported(self):
+        p, rec = self.params, self.reconstruction
+        if p.intensityConstraint != "standard":
+            raise NotImplementedError(
+                f"intensityConstraint {p.intensityConstraint!r}: only 'standard' is on this path (BaseEngine.py:954-961)"
+            )
+        for name in _UNSUPPORTED:
+            if getattr(p, name, False):
+                raise NotImplementedError(f"params.{name} is not supported by the GB300 engines")
+        if getattr(p, "comStabilizationSwitch", None) not in (None, False):
+            raise NotImplementedError("params.comStabilizationSwitch is not supported by the GB300 engines")
+        if getattr(rec, "nlambda", 1) != 1:
+            raise NotImplementedError("nlambda > 1 (polychromatic propagators) is not on this path")
+        if p.propagatorType.lower() not in ("fraunhofer", "fresnel", "asp"):
+            raise NotImplementedError(f"propagatorType {p.propagatorType!r} is not on this path")
+
+    def _checkMISC(self):
+        """BaseEngine.py:376-403."""
+        if self.params.probePowerCorrectionSwitch and self.params.modulusEnforcedProbeSwitch:
+            raise ValueError(
+                "probePowerCorrectionSwitch and modulusEnforcedProbeSwitch can not simultaneously be switched on!"
+            )
+        if self.params.propagatorType == "ASP" and self.params.fftshiftSwitch:
+            raise ValueError("ASP propagatorType works only with fftshiftSwitch = False")
+
+    def _checkFFT(self):
+        """Shift the data once so the uncentred transform applies (BaseEngine.py:405-450)."""
+        d = self.experimentalData
+        if self.params.fftshiftSwitch:
+            if self.params.fftshiftFlag == 0:
+                d.ptychogram = np.fft.ifftshift(d.ptychogram, axes=(-1, -2))
+                self.params.fftshiftFlag = 1
+        else:
+            if self.params.fftshiftFlag == 1:
+                d.ptychogram = np.fft.fftshift(d.ptychogram, axes=(-1, -2))
+                self.params.fftshiftFlag = 0
+
+    def _initialProbePowerCorrection(self):
+        if self.params.probePowerCorrectionSwitch:
+            rec = self.reconstruction
+            rec.probe = (
+                rec.probe / np.sqrt(np.sum(rec.probe * rec.probe.conj())) * self.experimentalData.maxProbePower
+            )
+
+    def _probeWindow(self):
+        """BaseEngine.py:237-266."""
+        rec = self.reconstruction
+        self.probeWindow = None
+        if not self.params.saveMemory or self.params.absorbingProbeBoundary:
+            self.probeWindow = np.exp(
+                -(((rec.Xp**2 + rec.Yp**2) / (2 * (3 / 4 * rec.Np * rec.dxp / 2.355) ** 2)) ** 10)
+            )
+        if self.params.probeBoundary:
+            d = self.experimentalData.entrancePupilDiameter
+            self.probeWindow = circ(rec.Xp, rec.Yp, d + d * 0.2)
+
+    def _initializeErrors(self):
+        """BaseEngine.py:199-225; detectorError is filled at the end of the run."""
+        rec = self.reconstruction
+        if self.params.saveMemory:
+            rec.detectorError = 0
+        if not hasattr(rec, "errorAtPos"):
+            rec.errorAtPos = np.zeros((self.experimentalData.numFrames, 1), dtype=np.float32)
+        if not hasattr(rec, "error"):
+            rec.error = []
+
+    def _prepareReconstruction(self):
+        self._check_supported()
+        self._checkMISC()
+        self._checkFFT()
+        self._initialProbePowerCorrection()
+        self._probeWindow()
+        self._initializeErrors()
+        self._checkGPU()
+
+    # --------------------------------------------------------- device state
+    def _engine_code(self):
+        return _native.ENGINES[self.engine_name]
+
+    def _state_fields(self):
+        return ["object", "probe"]
+
+    def _to_device(self, x, dtype):
+        torch = _torch()
+        dev = self._dev["device"]
+        if isinstance(x, torch.Tensor):
+            return x.to(device=dev, dtype=dtype).contiguous()
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(x))).to(device=dev, dtype=dtype)
+
+    def _checkGPU(self):
+        """Move the state to the GPU and build the launch plan (BaseEngine.py:613-635)."""
+        torch = _torch()
+        if not getattr(self.params, "gpuSwitch", True):
+            self.logger.warning("params.gpuSwitch is False; the GB300 engines always run on the GPU")
+        if not torch.cuda.is_available():
+            raise ImportError("no CUDA device: the GB300 engines need an sm_103a GPU")
+        device = torch.device("cuda", torch.cuda.current_device())
+        lib = _native.require(device.index)
+        rec, d, p = self.reconstruction, self.experimentalData, self.params
+        self._dev = {"device": device, "lib": lib}
+        for name in self._state_fields():
+            setattr(rec, name, self._to_device(getattr(rec, name), torch.complex64))
+        Np, No = int(rec.Np), int(rec.No)
+        nosm, npsm, nslice = int(rec.nosm), int(rec.npsm), int(rec.nslice)
+        if tuple(rec.object.shape) != (1, nosm, 1, nslice, No, No):
+            raise ValueError(f"object shape {tuple(rec.object.shape)} != {(1, nosm, 1, nslice, No, No)}")
+        if tuple(rec.probe.shape) != (1, 1, npsm, nslice, Np, Np):
+            raise ValueError(f"probe shape {tuple(rec.probe.shape)} != {(1, 1, npsm, nslice, Np, Np)}")
+        nf = int(d.numFrames)
+        positions = np.asarray(rec.positions).astype(np.int64)
+        if positions.shape != (nf, 2):
+            raise ValueError(f"positions shape {positions.shape} != {(nf, 2)}")
+        if positions.min() < 0 or positions.max() > No - Np:
+            raise ValueError(f"scan positions fall outside the {No}x{No} object (patch {Np})")
+        self._positions_host = positions
+        self._dev["positions"] = torch.from_numpy(positions.astype(np.int32)).to(device)
+        self._dev["data"] = self._to_device(d.ptychogram, torch.float32)
+        self._dev["order"] = torch.zeros(nf, dtype=torch.int32, device=device)
+        self._dev["flags"] = torch.zeros(nf, dtype=torch.uint8, device=device)
+        self._order_host = torch.zeros(nf, dtype=torch.int32).pin_memory()
+        self._flags_host = torch.zeros(nf, dtype=torch.uint8).pin_memory()
+        geom = _native.Geometry(
+            Np=Np, No=No, nosm=nosm, npsm=npsm, nslice=nslice, num_frames=nf, num_scans=1,
+            engine=self._engine_code(), propagator=_native.PROPAGATORS[p.propagatorType.lower()],
+            fftshift=int(bool(p.fftshiftSwitch)), fpm=int(d.operationMode == "FPM"),
+            cluster=int(getattr(self, "cluster", 0) or 0),
+        )
+        self._release_plan()
+        plan = C.c_void_p()
+        _native.check(lib.ptyg_plan_create(C.byref(geom), C.byref(plan)), "ptyg_plan_create")
+        self._plan = plan
+        self._set_tables()
+        self._bind()
+        self.params.gpuFlag = 1
+
+    def _set_tables(self):
+        rec, p = self.reconstruction, self.params
+        lib = self._dev["lib"]
+        Np = int(rec.Np)
+        q = h = sh = None
+        kind = p.propagatorType.lower()
+        if kind == "fresnel":
+            q = np.ascontiguousarray(
+                _tables.fresnel_chirp(float(rec.zo), float(rec.wavelength), Np, float(rec.dxp)).astype(np.complex64)
+            )
+        elif kind == "asp":
+            h = np.ascontiguousarray(_tables.asp_detector_tf(float(rec.zo), float(rec.wavelength), Np, Np * float(rec.dxp)))
+        sh = self._slice_table()
+        self._tables_keepalive = (q, h, sh)
+        ptr = lambda a: a.ctypes.data if a is not None else None  # noqa: E731
+        _native.check(lib.ptyg_plan_set_tables(self._plan, ptr(q), ptr(h), ptr(sh)), "ptyg_plan_set_tables")
+
+    def _slice_table(self):
+        return None
+
+    def _scan_buffers(self):
+        rec = self.reconstruction
+        b = _native.ScanBuffers()
+        b.object = rec.object.data_ptr()
+        b.probe = rec.probe.data_ptr()
+        b.positions = self._dev["positions"].data_ptr()
+        b.order = self._dev["order"].data_ptr()
+        b.momentum_flags = self._dev["flags"].data_ptr()
+        return b
+
+    def _bind(self):
+        torch = _torch()
+        lib = self._dev["lib"]
+        self._buffers = self._scan_buffers()
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        _native.check(
+            lib.ptyg_plan_bind_scan(self._plan, 0, C.byref(self._buffers), self._dev["data"].data_ptr(), stream),
+            "ptyg_plan_bind_scan",
+        )
+
+    def _release_plan(self):
+        if self._plan is not None and self._plan.value:
+            _native.load_library().ptyg_plan_destroy(self._plan)
+        self._plan = None
+
+    def __del__(self):
+        try:
+            self._release_plan()
+        except Exception:
+            pass
+
+    def _update_params(self):
+        u = _native.UpdateParams()
+        u.beta_object = float(self.betaObject)
+        u.beta_probe = float(getattr(self, "betaProbe", 0.25))
+        u.alpha_object = float(getattr(self, "alphaObject", 0.1))
+        u.alpha_probe = float(getattr(self, "alphaProbe", 0.1))
+        u.reg_object = float(getattr(self, "regObject", 1.0))
+        u.reg_probe = float(getattr(self, "regProbe", 1.0))
+        u.friction = float(getattr(self, "frictionM", 0.7))
+        u.feedback = float(getattr(self, "feedbackM", 0.3))
+        u.probe_weight = 1.0
+        u.slice_beta = 0.9
+        return u
+
+    def _upload_order(self, momentum=None):
+        torch = _torch()
+        self._order_host.copy_(torch.from_numpy(np.asarray(self.positionIndices, dtype=np.int32)))
+        self._dev["order"].copy_(self._order_host, non_blocking=True)
+        if momentum is not None:
+            self._flags_host.copy_(torch.from_numpy(np.asarray(momentum, dtype=np.uint8)))
+            self._dev["flags"].copy_(self._flags_host, non_blocking=True)
+
+    def _run_positions(self, start, count, record_detector_error=False):
+        torch = _torch()
+        lib = self._dev["lib"]
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        u = self._update_params()
+        _native.check(
+            lib.ptyg_plan_run(self._plan, C.byref(u), int(start), int(count), int(bool(record_detector_error)), stream),
+            "ptyg_plan_run",
+        )
+
+    # ------------------------------------------------------ host control
+    def setPositionOrder(self):
+        """BaseEngine.py:637-665 (same NumPy calls, same global RNG)."""
+        nf = self.experimentalData.numFrames
+        order = self.params.positionOrder
+        if order == "sequential":
+            self.positionIndices = np.arange(nf)
+        elif order == "random":
+            self.positionIndices = np.arange(nf)
+            if len(self.reconstruction.error) >= 2:
+                np.random.shuffle(self.positionIndices)
+        elif order == "NA":
+            pos = self._positions_host
+            rows = pos[:, 0] - np.mean(pos[:, 0])
+            cols = pos[:, 1] - np.mean(pos[:, 1])
+            self.positionIndices = np.argsort(np.sqrt(rows**2 + cols**2))
+        else:
+            raise ValueError("position order not properly set")
+
+    def getErrorMetrics(self):
+        """BaseEngine.py:819-841, from the per-frame FP64 sums of |I_meas - I_est|."""
+        torch = _torch()
+        rec = self.reconstruction
+        nf = self.experimentalData.numFrames
+        err = np.empty(nf, dtype=np.float64)
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        _native.check(
+            self._dev["lib"].ptyg_plan_frame_errors(self._plan, 0, err.ctypes.data, stream), "ptyg_plan_frame_errors"
+        )
+        energy = np.asarray(self.experimentalData.energyAtPos)
+        if self.params.saveMemory:
+            # getRMSD stores one sum per position into errorAtPos (BaseEngine.py:857-866)
+            eap = np.array(rec.errorAtPos, copy=True)
+            eap[...] = err.reshape((nf,) + (1,) * (eap.ndim - 1)).astype(eap.dtype)
+            rec.errorAtPos = eap / (energy + 1e-20)
+        else:
+            rec.errorAtPos = err / (energy + 1e-20)
+        rec.error = np.append(rec.error, np.sum(rec.errorAtPos))
+
+    def applyConstraints(self, loop):
+        """In-scope subset of BaseEngine.applyConstraints (BaseEngine.py:1440-1500), in place on the device."""
+        torch = _torch()
+        p, rec = self.params, self.reconstruction
+        lib = self._dev["lib"]
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        if p.orthogonalizationSwitch and np.mod(loop, p.orthogonalizationFrequency) == 0:
+            self.orthogonalization()
+        if p.probePowerCorrectionSwitch:
+            norm = torch.sqrt(torch.sum(rec.probe * rec.probe.conj()))
+            rec.probe.mul_(float(self.experimentalData.maxProbePower) / norm)
+        if p.probeBoundary or p.absorbingProbeBoundary:
+            w = self._window_device()
+            if p.probeBoundary:
+                _native.check(
+                    lib.ptyg_mul_window(rec.probe.data_ptr(), w.data_ptr(), rec.probe.numel(), w.numel(), stream),
+                    "ptyg_mul_window",
+                )
+            if p.absorbingProbeBoundary:
+                a = float(p.absorbingProbeBoundaryAleph)
+                rec.probe.mul_((1 - a) + a * w.to(torch.complex64))
+
+    def _window_device(self):
+        torch = _torch()
+        if "window" not in self._dev:
+            w = np.asarray(self.probeWindow, dtype=np.float32)
+            self._dev["window"] = torch.from_numpy(np.ascontiguousarray(w)).to(self._dev["device"])
+        return self._dev["window"]
+
+    def _orthogonalize(self, stack, companions=()):
+        """Gram-matrix orthogonalisation of (modes, N, N) in place (utils.py:130-175):
+        G on the device in FP64, eigh on the host, modes <- V^T stack."""
+        torch = _torch()
+        lib = self._dev["lib"]
+        dev = self._dev["device"]
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        m = int(stack.shape[0])
+        n = int(stack[0].numel())
+        G = torch.empty((m, m), dtype=torch.complex128, device=dev)
+        src = stack.contiguous()
+        _native.check(lib.ptyg_gram(src.data_ptr(), m, n, G.data_ptr(), stream), "ptyg_gram")
+        w, V = np.linalg.eigh(G.cpu().numpy())
+        order = np.argsort(w)[::-1]
+        s = np.sqrt(np.clip(w[order].real, 0.0, None))
+        evals = s**2 / np.sum(s**2)
+        Vt = np.ascontiguousarray(V[:, order].T).astype(np.complex64)
+        Vd = torch.from_numpy(Vt).to(dev)
+        for arr in (stack,) + tuple(companions):
+            a = arr.contiguous()
+            out = torch.empty_like(a)
+            _native.check(lib.ptyg_mix_modes(Vd.data_ptr(), a.data_ptr(), out.data_ptr(), m, n, stream), "ptyg_mix_modes")
+            arr.copy_(out)
+        return evals, Vt
+
+    def orthogonalization(self):
+        """BaseEngine.py:1614-1722 (probe modes first, else object modes)."""
+        rec = self.reconstruction
+        mom = bool(getattr(self.params, "momentumAcceleration", False))
+        if rec.npsm > 1:
+            for s in range(rec.nslice):
+                comp = (rec.probeBuffer[0, 0, :, s], rec.probeMomentum[0, 0, :, s]) if mom else ()
+                evals, V = self._orthogonalize(rec.probe[0, 0, :, s], comp)
+                self.normalizedEigenvaluesProbe, self.MSPVprobe = evals, V
+                rec.purityProbe = float(np.sqrt(np.sum(evals**2)))
+                if hasattr(rec, "purityProbeHist"):
+                    rec.purityProbeHist.append(rec.purityProbe)
+        elif rec.nosm > 1:
+            for s in range(rec.nslice):
+                comp = (rec.objectBuffer[0, :, 0, s], rec.objectMomentum[0, :, 0, s]) if mom else ()
+                evals, V = self._orthogonalize(rec.object[0, :, 0, s], comp)
+                self.normalizedEigenvaluesObject, self.MSPVobject = evals, V
+                rec.purityObject = float(np.sqrt(np.sum(evals**2)))
+
+    def _detector_error_host(self):
+        torch = _torch()
+        d = self.experimentalData
+        Np = int(self.reconstruction.Np)
+        out = torch.empty((int(d.numFrames), Np, Np), dtype=torch.float32, device=self._dev["device"])
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        _native.check(
+            self._dev["lib"].ptyg_plan_detector_error(self._plan, 0, out.data_ptr(), stream), "ptyg_plan_detector_error"
+        )
+        return out.cpu().numpy().astype(np.float64)
+
+    def _check_status(self):
+        st = C.c_int(0)
+        torch = _torch()
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        _native.check(self._dev["lib"].ptyg_plan_status(self._plan, 0, C.byref(st), stream), "ptyg_plan_status")
+        if st.value != 0:
+            raise RuntimeError(f"device status {st.value}: a scan position fell outside the object")
+
+    def _move_data_to_cpu(self, detector_error=True):
+        """Write the device state back as NumPy arrays (BaseEngine.py:543-611)."""
+        torch = _torch()
+        rec = self.reconstruction
+        torch.cuda.current_stream(self._dev["device"]).synchronize()
+        self._check_status()
+        if detector_error and not self.params.saveMemory:
+            rec.detectorError = self._detector_error_host()
+        for name in self._state_fields():
+            v = getattr(rec, name)
+            if isinstance(v, torch.Tensor):
+                setattr(rec, name, v.cpu().numpy())
+        self._release_plan()
+        self.params.gpuFlag = 0
+
+    def changeExperimentalData(self, experimentalData):
+        if experimentalData is not None:
+            self.experimentalData = experimentalData
+
+    def changeOptimizable(self, optimizable):
+        if optimizable is not None:
+            self.reconstruction = optimizable
+
+    def showReconstruction(self, loop):
+        """GUI monitors are outside this package; the DummyMonitor hooks are no-ops."""
+        return None

@@ -1,0 +1,9 @@
+"""GB300 engines with PtyLab's constructor and attribute surface
+(``Engines.ePIE/mPIE/qNewton/e3PIE(reconstruction, experimentalData, params, monitor)``)."""
+
+from .BaseEngine import BaseEngine
+from .ePIE import ePIE
+from .mPIE import mPIE
+from .qNewton import qNewton
+
+__all__ = ["BaseEngine", "ePIE", "mPIE", "qNewton"]

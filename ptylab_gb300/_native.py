@@ -1,0 +1,171 @@
+"""ctypes binding of libptyg.so (the C ABI in include/ptyg.h).
+
+Only plain pointers and sizes cross the boundary.  Statuses map to the
+exceptions PtyLab raises on the same conditions: invalid switches ->
+ValueError (PtyLab/Engines/BaseEngine.py:376-403), unsupported branches ->
+NotImplementedError, no usable GPU -> ImportError (BaseEngine.py:617-621).
+There is no fallback: if the library is missing or no sm_103a device is
+present, every entry point raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libptyg.so"
+
+PTYG_OK = 0
+PTYG_ERR_INVALID = -1
+PTYG_ERR_UNSUPPORTED = -2
+PTYG_ERR_OOM = -3
+PTYG_ERR_CUDA = -4
+PTYG_ERR_TIMEOUT = -5
+PTYG_ERR_DEVICE = -6
+
+ENGINES = {"ePIE": 0, "mPIE": 1, "qNewton": 2, "e3PIE": 3}
+PROPAGATORS = {"fraunhofer": 0, "fresnel": 1, "asp": 2}
+
+_EXC = {
+    PTYG_ERR_INVALID: ValueError,
+    PTYG_ERR_UNSUPPORTED: NotImplementedError,
+    PTYG_ERR_OOM: MemoryError,
+    PTYG_ERR_CUDA: RuntimeError,
+    PTYG_ERR_TIMEOUT: TimeoutError,
+    PTYG_ERR_DEVICE: ImportError,
+}
+
+
+class Geometry(C.Structure):
+    _fields_ = [
+        ("Np", C.c_int32),
+        ("No", C.c_int32),
+        ("nosm", C.c_int32),
+        ("npsm", C.c_int32),
+        ("nslice", C.c_int32),
+        ("num_frames", C.c_int32),
+        ("num_scans", C.c_int32),
+        ("engine", C.c_int32),
+        ("propagator", C.c_int32),
+        ("fftshift", C.c_int32),
+        ("fpm", C.c_int32),
+        ("cluster", C.c_int32),
+    ]
+
+
+class UpdateParams(C.Structure):
+    _fields_ = [
+        ("beta_object", C.c_float),
+        ("beta_probe", C.c_float),
+        ("alpha_object", C.c_float),
+        ("alpha_probe", C.c_float),
+        ("reg_object", C.c_float),
+        ("reg_probe", C.c_float),
+        ("friction", C.c_float),
+        ("feedback", C.c_float),
+        ("probe_weight", C.c_float),
+        ("slice_beta", C.c_float),
+    ]
+
+
+class ScanBuffers(C.Structure):
+    _fields_ = [
+        ("object", C.c_void_p),
+        ("probe", C.c_void_p),
+        ("positions", C.c_void_p),
+        ("order", C.c_void_p),
+        ("momentum_flags", C.c_void_p),
+        ("object_buffer", C.c_void_p),
+        ("object_momentum", C.c_void_p),
+        ("probe_buffer", C.c_void_p),
+        ("probe_momentum", C.c_void_p),
+    ]
+
+
+# name -> (restype, argtypes); every function returns an int status
+_SIGNATURES = {
+    "ptyg_version": [],
+    "ptyg_last_error": None,
+    "ptyg_device_init": [C.c_int],
+    "ptyg_propagate": [
+        C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+    ],
+    "ptyg_plan_create": [C.POINTER(Geometry), C.POINTER(C.c_void_p)],
+    "ptyg_plan_destroy": [C.c_void_p],
+    "ptyg_plan_set_tables": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "ptyg_plan_bind_scan": [C.c_void_p, C.c_int, C.POINTER(ScanBuffers), C.c_void_p, C.c_void_p],
+    "ptyg_plan_run": [C.c_void_p, C.POINTER(UpdateParams), C.c_int, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_plan_frame_errors": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_plan_detector_error": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_plan_status": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p],
+    "ptyg_mul_window": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p],
+    "ptyg_gram": [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p],
+    "ptyg_mix_modes": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.c_void_p],
+}
+
+_lock = threading.Lock()
+_lib = None
+_device_ready = set()
+
+
+def load_library(path: Path | str | None = None):
+    """Load libptyg.so and declare its prototypes (no device needed)."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path is not None else LIB_PATH
+        if not p.exists():
+            raise ImportError(
+                f"{p} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+                "or `python -m ptylab_gb300._build`"
+            )
+        lib = C.CDLL(str(p))
+        for name, args in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            if name == "ptyg_last_error":
+                fn.restype = C.c_char_p
+                fn.argtypes = []
+            else:
+                fn.restype = C.c_int
+                fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status == PTYG_OK:
+        return
+    lib = load_library()
+    msg = lib.ptyg_last_error().decode(errors="replace")
+    exc = _EXC.get(status, RuntimeError)
+    raise exc(f"{what}: {msg}" if what else msg)
+
+
+def require(device: int = 0):
+    """Return the library once `device` is initialised; raise ImportError if unusable."""
+    lib = load_library()
+    if device not in _device_ready:
+        check(lib.ptyg_device_init(int(device)), "ptyg_device_init")
+        _device_ready.add(device)
+    return lib
+
+
+def available(device: int = 0) -> bool:
+    """True when the library loads and `device` is an sm_103a GPU (gpuSwitch check)."""
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return False
+        require(device)
+        return True
+    except Exception:
+        return False
+
+
+def exported_symbols() -> list[str]:
+    return sorted(_SIGNATURES)

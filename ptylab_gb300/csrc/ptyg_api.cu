@@ -1,0 +1,541 @@
+// C ABI of libptyg.so (declared in include/ptyg.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/ptyg.h"
+#include "ptyg_engine.cuh"
+#include "ptyg_ops.cuh"
+
+using ptyg::EngineArgs;
+using ptyg::ScanDev;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation) return fail(PTYG_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorNotSupported) return fail(PTYG_ERR_UNSUPPORTED, "%s: configuration not supported", what);
+  return fail(PTYG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define PTYG_CUDA(call, what)                    \
+  do {                                           \
+    cudaError_t e_ = (call);                     \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+static bool valid_np(int Np) { return Np == 32 || Np == 64 || Np == 128 || Np == 256; }
+
+// ------------------------------------------------------- per-device tables
+// W_N^m = exp(-2*pi*i*m/N), m = 0..N-1, built in double and rounded.
+namespace {
+struct DeviceTables {
+  float2* tw[4] = {nullptr, nullptr, nullptr, nullptr};  // N = 32, 64, 128, 256
+};
+std::mutex g_tables_mu;
+std::vector<DeviceTables> g_tables;
+
+int table_slot(int Np) { return Np == 32 ? 0 : Np == 64 ? 1 : Np == 128 ? 2 : 3; }
+
+int ensure_tables(int device) {
+  std::lock_guard<std::mutex> lk(g_tables_mu);
+  if ((int)g_tables.size() <= device) g_tables.resize(device + 1);
+  DeviceTables& t = g_tables[device];
+  if (t.tw[0]) return PTYG_OK;
+  const double pi = 3.14159265358979323846;
+  for (int s = 0; s < 4; ++s) {
+    const int N = 32 << s;
+    std::vector<float2> h(N);
+    for (int m = 0; m < N; ++m) {
+      const double ang = -2.0 * pi * (double)m / (double)N;
+      h[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+    }
+    float2* d = nullptr;
+    PTYG_CUDA(cudaMalloc(&d, N * sizeof(float2)), "twiddle table");
+    PTYG_CUDA(cudaMemcpy(d, h.data(), N * sizeof(float2), cudaMemcpyHostToDevice), "twiddle table");
+    t.tw[s] = d;
+  }
+  return PTYG_OK;
+}
+
+int current_device(int* dev) {
+  cudaError_t e = cudaGetDevice(dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  return PTYG_OK;
+}
+
+const float2* twiddles(int device, int Np) { return g_tables[device].tw[table_slot(Np)]; }
+}  // namespace
+
+extern "C" int ptyg_version(void) { return PTYG_VERSION; }
+
+extern "C" const char* ptyg_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int ptyg_device_init(int device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(PTYG_ERR_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  if (device < 0 || device >= n) return fail(PTYG_ERR_INVALID, "device %d out of range (%d devices)", device, n);
+  PTYG_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  cudaDeviceProp prop;
+  PTYG_CUDA(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(PTYG_ERR_DEVICE, "device %d is sm_%d%d; libptyg is built for sm_103a only", device, prop.major,
+                prop.minor);
+  return ensure_tables(device);
+}
+
+static int ready_device(int* dev) {
+  int r = current_device(dev);
+  if (r) return r;
+  if ((int)g_tables.size() <= *dev || !g_tables[*dev].tw[0]) {
+    r = ptyg_device_init(*dev);
+    if (r) return r;
+  }
+  return PTYG_OK;
+}
+
+// ------------------------------------------------------------ propagators
+extern "C" int ptyg_propagate(int propagator, int direction, int fftshift, int Np, int batch, const void* in,
+                              void* out, const void* table, void* scratch, void* stream) {
+  if (!valid_np(Np)) return fail(PTYG_ERR_UNSUPPORTED, "Np=%d: supported sizes are 32, 64, 128, 256", Np);
+  if (batch < 0) return fail(PTYG_ERR_INVALID, "batch=%d", batch);
+  if (batch == 0) return PTYG_OK;
+  if (!in || !out) return fail(PTYG_ERR_INVALID, "null field pointer");
+  if (direction != PTYG_FORWARD && direction != PTYG_INVERSE) return fail(PTYG_ERR_INVALID, "direction=%d", direction);
+  if ((propagator == PTYG_FRESNEL || propagator == PTYG_ASP) && !table)
+    return fail(PTYG_ERR_INVALID, "propagator %d needs its table", propagator);
+  if (propagator == PTYG_ASP && fftshift)
+    return fail(PTYG_ERR_INVALID, "ASP propagator only works with fftshiftSwitch == False");
+  if (propagator < PTYG_FRAUNHOFER || propagator > PTYG_ASP)
+    return fail(PTYG_ERR_UNSUPPORTED, "propagator %d is not on this path", propagator);
+  int dev;
+  int r = ready_device(&dev);
+  if (r) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  const float2* tw = twiddles(dev, Np);
+  const float2* src = (const float2*)in;
+  float2* dst = (float2*)out;
+  float2* tmp = (float2*)scratch;
+  bool own = false;
+  if (!tmp) {
+    PTYG_CUDA(cudaMallocAsync((void**)&tmp, (size_t)batch * Np * Np * sizeof(float2), st), "propagate scratch");
+    own = true;
+  }
+  const bool inv = direction == PTYG_INVERSE;
+  const bool centred = !fftshift;
+  const float2* tab = (const float2*)table;
+  cudaError_t e = cudaSuccess;
+  if (propagator == PTYG_FRAUNHOFER || propagator == PTYG_FRESNEL) {
+    ptyg::RowOp ro = {};
+    ro.inverse = inv;
+    ro.preSign = centred;
+    ro.scale = 1.f;
+    if (propagator == PTYG_FRESNEL && !inv) ro.pre = tab;
+    ptyg::ColOp co = {};
+    co.inverse1 = inv;
+    co.postSign = centred;
+    co.scale = 1.f / (float)Np;
+    if (propagator == PTYG_FRESNEL && inv) {
+      co.post = tab;
+      co.conjPost = 1;
+    }
+    e = ptyg::prop_rows(Np, src, tmp, batch, ro, tw, st);
+    if (e == cudaSuccess) e = ptyg::prop_cols(Np, tmp, dst, batch, co, tw, st);
+  } else {
+    ptyg::RowOp r1 = {};
+    r1.scale = 1.f;
+    ptyg::ColOp co = {};
+    co.inverse1 = 0;
+    co.filter = tab;
+    co.conjFilter = inv;
+    co.filterScale = 1.f / (float)(Np * Np);
+    co.inverse2 = 1;
+    co.scale = 1.f;
+    ptyg::RowOp r2 = {};
+    r2.inverse = 1;
+    r2.scale = 1.f;
+    e = ptyg::prop_rows(Np, src, tmp, batch, r1, tw, st);
+    if (e == cudaSuccess) e = ptyg::prop_cols(Np, tmp, tmp, batch, co, tw, st);
+    if (e == cudaSuccess) e = ptyg::prop_rows(Np, tmp, dst, batch, r2, tw, st);
+  }
+  if (own) {
+    cudaError_t e2 = cudaFreeAsync(tmp, st);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "ptyg_propagate");
+  return PTYG_OK;
+}
+
+// ------------------------------------------------------------------ plans
+struct ScanOwned {
+  float* data = nullptr;      // converted ptychogram
+  float2* work = nullptr;
+  float2* esw = nullptr;
+  double* errPart = nullptr;
+  double* err = nullptr;
+  float* detErr = nullptr;
+  unsigned* red = nullptr;
+  int* status = nullptr;
+  bool bound = false;
+  ptyg_scan_buffers buf = {};
+};
+
+struct ptyg_plan {
+  ptyg_geometry g = {};
+  int device = 0;
+  int C = 1;
+  int threads = 256;
+  size_t smem = 0;
+  float2* fresnelQ = nullptr;
+  float2* aspH = nullptr;
+  float2* sliceH = nullptr;
+  std::vector<ScanOwned> scans;
+  ScanDev* dScans = nullptr;
+  std::vector<ScanDev> hScans;
+};
+
+static void plan_free(ptyg_plan* p) {
+  if (!p) return;
+  cudaFree(p->fresnelQ);
+  cudaFree(p->aspH);
+  cudaFree(p->sliceH);
+  for (auto& s : p->scans) {
+    cudaFree(s.data);
+    cudaFree(s.work);
+    cudaFree(s.esw);
+    cudaFree(s.errPart);
+    cudaFree(s.err);
+    cudaFree(s.detErr);
+    cudaFree(s.red);
+    cudaFree(s.status);
+  }
+  cudaFree(p->dScans);
+  delete p;
+}
+
+static int choose_cluster(const ptyg_geometry& g, int* C, int* threads) {
+  int c = g.cluster;
+  if (c <= 0) c = g.Np / 8;  // 8 rows per CTA
+  if (c > 16) c = 16;
+  if (c < 1) c = 1;
+  if (g.Np % c != 0 || (c & (c - 1)) != 0) return fail(PTYG_ERR_INVALID, "cluster=%d must be a power of two dividing Np", c);
+  const int L = g.Np / c;
+  int w = L < 8 ? L : 8;
+  if (w < 4) w = 4;
+  *C = c;
+  *threads = 32 * w;
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan) {
+  if (!geometry || !plan) return fail(PTYG_ERR_INVALID, "null argument");
+  *plan = nullptr;
+  const ptyg_geometry& g = *geometry;
+  if (!valid_np(g.Np)) return fail(PTYG_ERR_UNSUPPORTED, "Np=%d: supported sizes are 32, 64, 128, 256", g.Np);
+  if (g.No < g.Np) return fail(PTYG_ERR_INVALID, "No=%d smaller than Np=%d", g.No, g.Np);
+  if (g.nosm < 1 || g.npsm < 1 || g.nslice < 1 || g.num_frames < 1 || g.num_scans < 1)
+    return fail(PTYG_ERR_INVALID, "mode/slice/frame/scan counts must be >= 1");
+  if (g.engine < PTYG_EPIE || g.engine > PTYG_E3PIE) return fail(PTYG_ERR_INVALID, "engine=%d", g.engine);
+  if (g.propagator < PTYG_FRAUNHOFER || g.propagator > PTYG_ASP)
+    return fail(PTYG_ERR_UNSUPPORTED, "propagator %d is not on this path", g.propagator);
+  if (g.propagator == PTYG_ASP && g.fftshift)
+    return fail(PTYG_ERR_INVALID, "ASP propagatorType works only with fftshiftSwitch = False");
+  if (g.engine == PTYG_E3PIE)
+    return fail(PTYG_ERR_UNSUPPORTED, "e3PIE is not available in this build");
+  if (g.nslice != 1) return fail(PTYG_ERR_UNSUPPORTED, "nslice=%d needs the e3PIE engine", g.nslice);
+  if (!ptyg::engine_modes_supported(g.Np, g.nosm, g.npsm))
+    return fail(PTYG_ERR_UNSUPPORTED, "nosm=%d npsm=%d at Np=%d is not instantiated", g.nosm, g.npsm, g.Np);
+  int dev;
+  int r = ready_device(&dev);
+  if (r) return r;
+  ptyg_plan* p = new (std::nothrow) ptyg_plan();
+  if (!p) return fail(PTYG_ERR_OOM, "host allocation");
+  p->g = g;
+  p->device = dev;
+  r = choose_cluster(g, &p->C, &p->threads);
+  if (r) {
+    plan_free(p);
+    return r;
+  }
+  int maxSmem = 0;
+  cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // largest cluster (<= the requested one) that fits in shared memory and can be co-scheduled
+  for (;;) {
+    p->smem = ptyg::engine_smem_bytes(g.Np, p->C, g.nosm, g.npsm, g.engine);
+    int nclusters = 0;
+    cudaError_t e = cudaSuccess;
+    if ((int)p->smem <= maxSmem) {
+      e = ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, p->C, p->threads, p->smem, &nclusters);
+      if (e != cudaSuccess) cudaGetLastError();
+    }
+    if (e == cudaSuccess && nclusters > 0) break;
+    if (p->C == 1) {
+      plan_free(p);
+      return fail(PTYG_ERR_UNSUPPORTED, "no launchable cluster shape (needs %zu B shared memory per CTA, max %d)",
+                  p->smem, maxSmem);
+    }
+    p->C /= 2;
+    const int L = g.Np / p->C;
+    const int w = L < 8 ? (L < 4 ? 4 : L) : 8;
+    p->threads = 32 * w;
+  }
+  const size_t np2 = (size_t)g.Np * g.Np;
+  const int K = g.nosm * g.npsm;
+  p->scans.resize(g.num_scans);
+  p->hScans.resize(g.num_scans);
+  for (int s = 0; s < g.num_scans; ++s) {
+    ScanOwned& o = p->scans[s];
+    cudaError_t e = cudaMalloc(&o.data, (size_t)g.num_frames * np2 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&o.work, (size_t)K * np2 * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&o.errPart, (size_t)g.num_frames * p->C * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(o.errPart, 0, (size_t)g.num_frames * p->C * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&o.err, (size_t)g.num_frames * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&o.red, 2 * ptyg::RED_BANK * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&o.status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(o.status, 0, sizeof(int));
+    if (e != cudaSuccess) {
+      plan_free(p);
+      return cuda_fail(e, "plan allocation");
+    }
+  }
+  cudaError_t e = cudaMalloc(&p->dScans, g.num_scans * sizeof(ScanDev));
+  if (e != cudaSuccess) {
+    plan_free(p);
+    return cuda_fail(e, "plan allocation");
+  }
+  *plan = p;
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_destroy(ptyg_plan* plan) {
+  plan_free(plan);
+  return PTYG_OK;
+}
+
+// Fourier-layout permutation of a centred table: out[sx][sy] = ifftshift(H)[ky][kx].
+static std::vector<float2> to_fourier_layout_host(const float2* centred, int Np) {
+  const int E = Np / 32;
+  auto bitrev5 = [](int l) {
+    int r = 0;
+    for (int b = 0; b < 5; ++b) r |= ((l >> b) & 1) << (4 - b);
+    return r;
+  };
+  auto k_of = [&](int s) { return (s >> 5) + E * bitrev5(s & 31); };
+  std::vector<float2> out((size_t)Np * Np);
+  for (int sx = 0; sx < Np; ++sx)
+    for (int sy = 0; sy < Np; ++sy) {
+      const int ky = k_of(sy), kx = k_of(sx);
+      // ifftshift: element k of the shifted array is element (k + Np/2) % Np of the centred one
+      const int cy = (ky + Np / 2) % Np, cx = (kx + Np / 2) % Np;
+      out[(size_t)sx * Np + sy] = centred[(size_t)cy * Np + cx];
+    }
+  return out;
+}
+
+static int upload(float2** dst, const void* host, size_t n) {
+  if (!*dst) PTYG_CUDA(cudaMalloc(dst, n * sizeof(float2)), "table allocation");
+  PTYG_CUDA(cudaMemcpy(*dst, host, n * sizeof(float2), cudaMemcpyHostToDevice), "table upload");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_set_tables(ptyg_plan* p, const void* fresnel_q, const void* asp_h, const void* slice_h) {
+  if (!p) return fail(PTYG_ERR_INVALID, "null plan");
+  const int Np = p->g.Np;
+  const size_t n = (size_t)Np * Np;
+  int r;
+  if (fresnel_q && (r = upload(&p->fresnelQ, fresnel_q, n))) return r;
+  if (asp_h) {
+    auto t = to_fourier_layout_host((const float2*)asp_h, Np);
+    if ((r = upload(&p->aspH, t.data(), n))) return r;
+  }
+  if (slice_h) {
+    auto t = to_fourier_layout_host((const float2*)slice_h, Np);
+    if ((r = upload(&p->sliceH, t.data(), n))) return r;
+  }
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffers* b, const float* ptychogram,
+                                   void* stream) {
+  if (!p || !b) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  if (!b->object || !b->probe || !b->positions || !b->order || !ptychogram)
+    return fail(PTYG_ERR_INVALID, "object, probe, positions, order and ptychogram are required");
+  if (p->g.engine == PTYG_MPIE &&
+      (!b->object_buffer || !b->object_momentum || !b->probe_buffer || !b->probe_momentum))
+    return fail(PTYG_ERR_INVALID, "mPIE needs object/probe buffers and momenta");
+  cudaStream_t st = (cudaStream_t)stream;
+  ScanOwned& o = p->scans[scan];
+  o.buf = *b;
+  const int Np = p->g.Np;
+  const size_t n = (size_t)p->g.num_frames * Np * Np;
+  if (p->g.propagator == PTYG_ASP) {
+    PTYG_CUDA(cudaMemcpyAsync(o.data, ptychogram, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "data copy");
+  } else {
+    PTYG_CUDA(ptyg::to_fourier_layout(ptychogram, o.data, p->g.num_frames, Np, st), "data layout");
+  }
+  PTYG_CUDA(cudaMemsetAsync(o.errPart, 0, (size_t)p->g.num_frames * p->C * sizeof(double), st), "reset");
+  PTYG_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int), st), "reset");
+  ScanDev& d = p->hScans[scan];
+  d = ScanDev{};
+  d.object = (float2*)b->object;
+  d.probe = (float2*)b->probe;
+  d.data = o.data;
+  d.positions = b->positions;
+  d.order = b->order;
+  d.momentum = b->momentum_flags;
+  d.objectBuffer = (float2*)b->object_buffer;
+  d.objectMomentum = (float2*)b->object_momentum;
+  d.probeBuffer = (float2*)b->probe_buffer;
+  d.probeMomentum = (float2*)b->probe_momentum;
+  d.work = o.work;
+  d.eswStore = o.esw;
+  d.errPart = o.errPart;
+  d.detErr = o.detErr;
+  d.red = o.red;
+  d.status = o.status;
+  o.bound = true;
+  PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &d, sizeof(ScanDev), cudaMemcpyHostToDevice, st), "scan upload");
+  // the host copy must outlive the async copy: hScans is owned by the plan
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int start, int count, int flags,
+                             void* stream) {
+  if (!p || !u) return fail(PTYG_ERR_INVALID, "null argument");
+  if (start < 0 || count < 0) return fail(PTYG_ERR_INVALID, "start=%d count=%d", start, count);
+  for (int s = 0; s < p->g.num_scans; ++s)
+    if (!p->scans[s].bound) return fail(PTYG_ERR_INVALID, "scan %d is not bound", s);
+  if (count == 0) return PTYG_OK;
+  const ptyg_geometry& g = p->g;
+  if ((long long)start + count > g.num_frames)
+    return fail(PTYG_ERR_INVALID, "order slots [%d, %d) exceed num_frames=%d", start, start + count, g.num_frames);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g.propagator == PTYG_FRESNEL && !p->fresnelQ) return fail(PTYG_ERR_INVALID, "Fresnel table not set");
+  if (g.propagator == PTYG_ASP && !p->aspH) return fail(PTYG_ERR_INVALID, "ASP transfer function not set");
+  const bool det = (flags & 1) != 0;
+  if (det) {
+    for (int s = 0; s < g.num_scans; ++s) {
+      ScanOwned& o = p->scans[s];
+      if (!o.detErr) {
+        PTYG_CUDA(cudaMalloc(&o.detErr, (size_t)g.num_frames * g.Np * g.Np * sizeof(float)), "detector error");
+        PTYG_CUDA(cudaMemsetAsync(o.detErr, 0, (size_t)g.num_frames * g.Np * g.Np * sizeof(float), st), "reset");
+        p->hScans[s].detErr = o.detErr;
+        PTYG_CUDA(cudaMemcpyAsync(p->dScans + s, &p->hScans[s], sizeof(ScanDev), cudaMemcpyHostToDevice, st),
+                  "scan upload");
+      }
+    }
+  }
+  EngineArgs a = {};
+  a.scans = p->dScans;
+  a.twiddle = twiddles(p->device, g.Np);
+  a.fresnelQ = p->fresnelQ;
+  a.aspH = p->aspH;
+  a.sliceH = p->sliceH;
+  a.Np = g.Np;
+  a.No = g.No;
+  a.nosm = g.nosm;
+  a.npsm = g.npsm;
+  a.nslice = g.nslice;
+  a.numFrames = g.num_frames;
+  a.engine = g.engine;
+  a.prop = g.propagator;
+  a.centred = !g.fftshift;
+  a.fpm = g.fpm;
+  a.start = start;
+  a.count = count;
+  a.writeDetErr = det;
+  a.cluster = p->C;
+  a.betaO = u->beta_object;
+  a.betaP = u->beta_probe;
+  a.alphaO = u->alpha_object;
+  a.alphaP = u->alpha_probe;
+  a.regO = u->reg_object;
+  a.regP = u->reg_probe;
+  a.frictionM = u->friction;
+  a.feedbackM = u->feedback;
+  a.weightP = u->probe_weight;
+  a.bethSlice = u->slice_beta;
+  cudaError_t e = ptyg::launch_engine(a, g.num_scans, p->threads, p->smem, st);
+  if (e != cudaSuccess) return cuda_fail(e, "engine launch");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_frame_errors(ptyg_plan* p, int scan, double* host_out, void* stream) {
+  if (!p || !host_out) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  cudaStream_t st = (cudaStream_t)stream;
+  ScanOwned& o = p->scans[scan];
+  PTYG_CUDA(ptyg::sum_parts(o.errPart, o.err, p->g.num_frames, p->C, st), "error sum");
+  PTYG_CUDA(cudaMemcpyAsync(host_out, o.err, p->g.num_frames * sizeof(double), cudaMemcpyDeviceToHost, st),
+            "error readback");
+  PTYG_CUDA(cudaStreamSynchronize(st), "error readback");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_detector_error(ptyg_plan* p, int scan, float* out, void* stream) {
+  if (!p || !out) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  ScanOwned& o = p->scans[scan];
+  if (!o.detErr) return fail(PTYG_ERR_INVALID, "no detector error recorded (run with flags bit 0)");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n = (size_t)p->g.num_frames * p->g.Np * p->g.Np;
+  if (p->g.propagator == PTYG_ASP) {
+    PTYG_CUDA(cudaMemcpyAsync(out, o.detErr, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+  } else {
+    PTYG_CUDA(ptyg::from_fourier_layout(o.detErr, out, p->g.num_frames, p->g.Np, st), "layout");
+  }
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_status(ptyg_plan* p, int scan, int* host_status, void* stream) {
+  if (!p || !host_status) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  cudaStream_t st = (cudaStream_t)stream;
+  PTYG_CUDA(cudaMemcpyAsync(host_status, p->scans[scan].status, sizeof(int), cudaMemcpyDeviceToHost, st), "status");
+  PTYG_CUDA(cudaStreamSynchronize(st), "status");
+  return PTYG_OK;
+}
+
+// ---------------------------------------------------------------- helpers
+extern "C" int ptyg_mul_window(void* x, const float* window, int64_t n, int64_t n_window, void* stream) {
+  if (!x || !window || n < 0 || n_window <= 0) return fail(PTYG_ERR_INVALID, "bad arguments");
+  if (n == 0) return PTYG_OK;
+  PTYG_CUDA(ptyg::mul_window((float2*)x, window, n, n_window, (cudaStream_t)stream), "mul_window");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_gram(const void* p, int modes, int64_t n, void* gram, void* stream) {
+  if (!p || !gram || modes < 1 || n < 1) return fail(PTYG_ERR_INVALID, "bad arguments");
+  PTYG_CUDA(ptyg::gram((const float2*)p, modes, n, (double2*)gram, (cudaStream_t)stream), "gram");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_mix_modes(const void* V, const void* p, void* out, int modes, int64_t n, void* stream) {
+  if (!V || !p || !out || modes < 1 || n < 1) return fail(PTYG_ERR_INVALID, "bad arguments");
+  if (modes > 16) return fail(PTYG_ERR_UNSUPPORTED, "modes=%d > 16", modes);
+  if (p == out) return fail(PTYG_ERR_INVALID, "ptyg_mix_modes cannot work in place");
+  PTYG_CUDA(ptyg::mix_modes((const float2*)V, (const float2*)p, (float2*)out, modes, n, (cudaStream_t)stream),
+            "mix_modes");
+  return PTYG_OK;
+}

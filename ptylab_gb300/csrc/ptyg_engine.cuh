@@ -1,0 +1,59 @@
+// Device-side argument blocks of the persistent position-loop kernel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ptyg {
+
+enum Engine { ENG_EPIE = 0, ENG_MPIE = 1, ENG_QNEWTON = 2, ENG_E3PIE = 3 };
+enum Propagator { PROP_FRAUNHOFER = 0, PROP_FRESNEL = 1, PROP_ASP = 2 };
+
+// Reduction slots (unsigned bit patterns of non-negative floats, max-reduced
+// with atomicMax), two banks alternating by position parity.
+enum RedSlot {
+  RED_PMAX2 = 0,   // max_xy sum_p |P_p|^2
+  RED_OMAX2 = 1,   // max_xy sum_o |O_o|^2 over the patch
+  RED_PMAX1 = 2,   // max_xy sum_p |P_p|        (qNewton)
+  RED_OMAXW = 3,   // max over the whole object of sum_o |O_o| (qNewton)
+  RED_SLICE_P = 4, // e3PIE: max_xy sum_p |P_s|^2, slices 0..5
+  RED_SLICE_O = 10,// e3PIE: max_xy sum_o |O_s|^2, slices 0..5
+  RED_BANK = 16
+};
+
+// Per-scan device state.  Object/probe/buffers/positions/order belong to the
+// caller; work/esw/err/detErr/red/status belong to the plan.
+struct ScanDev {
+  float2* object;          // (nosm, nslice, No, No)
+  float2* probe;           // (npsm, nslice, Np, Np)
+  const float* data;       // Fraunhofer/Fresnel: [frame][sx][sy] Fourier layout; ASP: [frame][y][x]
+  const int* positions;    // [frame][2] = (row, col) of the patch corner
+  const int* order;        // scan order; a launch reads order[start .. start+count)
+  const uint8_t* momentum; // mPIE: momentum flag per order slot
+  float2* objectBuffer;
+  float2* objectMomentum;
+  float2* probeBuffer;
+  float2* probeMomentum;
+  float2* work;            // transposition buffer, K * Np * Np
+  float2* eswStore;        // e3PIE: forward exit waves, nslice * npsm * Np * Np
+  double* errPart;         // [frame][cluster] partial sums of |I_meas - I_est|
+  float* detErr;           // optional [frame][Np*Np] |I_meas - I_est| (data layout)
+  unsigned* red;           // 2 * RED_BANK reduction slots
+  int* status;             // 0 = ok, else first error code seen
+};
+
+struct EngineArgs {
+  const ScanDev* scans;
+  const float2* twiddle;   // W_Np^m, m = 0..Np-1
+  const float2* fresnelQ;  // Fresnel chirp, natural [y][x]
+  const float2* aspH;      // ASP detector TF (ifftshifted), Fourier layout [sx][sy]
+  const float2* sliceH;    // e3PIE slice TF (ifftshifted), Fourier layout [sx][sy]
+  int Np, No, nosm, npsm, nslice, numFrames;
+  int engine, prop, centred, fpm;
+  int start, count;
+  int writeDetErr;
+  int cluster;
+  float betaO, betaP, alphaO, alphaP, regO, regP, frictionM, feedbackM, weightP, bethSlice;
+};
+
+}  // namespace ptyg

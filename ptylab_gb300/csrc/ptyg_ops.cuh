@@ -1,0 +1,54 @@
+// Host-callable launchers of ptyg_ops.cu and ptyg_engine.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ptyg_engine.cuh"
+
+namespace ptyg {
+
+// Row pass of a standalone propagation: per row, x * pre (or conj) * [sign]
+// -> 1D transform -> * scale * [sign] * post (or conj).  The 2D centring
+// modulation is one pre-sign in the first pass and one post-sign in the last.
+struct RowOp {
+  int inverse;
+  int preSign;   // multiply the input by (-1)^(y+x)
+  int postSign;  // multiply the output by (-1)^(y+x)
+  const float2* pre;
+  int conjPre;
+  const float2* post;
+  int conjPost;
+  float scale;
+};
+
+// Column pass: transform (inverse1), optionally * filter*filterScale (or conj)
+// and transform again (inverse2); then * scale * [sign] * post.
+struct ColOp {
+  int inverse1;
+  const float2* filter;
+  int conjFilter;
+  float filterScale;
+  int inverse2;
+  int postSign;  // multiply the output by (-1)^(y+x)
+  const float2* post;
+  int conjPost;
+  float scale;
+};
+
+cudaError_t prop_rows(int Np, const float2* in, float2* out, int batch, const RowOp& op, const float2* tw,
+                      cudaStream_t st);
+cudaError_t prop_cols(int Np, const float2* in, float2* out, int batch, const ColOp& op, const float2* tw,
+                      cudaStream_t st);
+cudaError_t to_fourier_layout(const float* in, float* out, int frames, int Np, cudaStream_t st);
+cudaError_t from_fourier_layout(const float* in, float* out, int frames, int Np, cudaStream_t st);
+cudaError_t sum_parts(const double* part, double* err, int frames, int C, cudaStream_t st);
+cudaError_t mul_window(float2* x, const float* w, long long n, long long nw, cudaStream_t st);
+cudaError_t gram(const float2* p, int modes, long long n, double2* G, cudaStream_t st);
+cudaError_t mix_modes(const float2* V, const float2* p, float2* out, int modes, long long n, cudaStream_t st);
+
+size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine);
+cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
+bool engine_modes_supported(int Np, int nosm, int npsm);
+cudaError_t engine_max_clusters(int Np, int nosm, int npsm, int cluster, int threads, size_t smem, int* out);
+
+}  // namespace ptyg

@@ -1,0 +1,101 @@
+"""Host-side logic of the drop-in against the reference fixtures and the oracle (no GPU)."""
+
+import numpy as np
+import pytest
+
+from conftest import fixture_names, load_fixture
+from oracle import ptyoracle as O
+from ptylab_gb300 import ExperimentalData, Params, Reconstruction, _tables
+
+
+def containers(fx):
+    """Build the package's ExperimentalData/Params/Reconstruction from a fixture."""
+    m = {k[5:]: fx[k] for k in fx if k.startswith("meta_")}
+    i = {k[3:]: fx[k] for k in fx if k.startswith("in_")}
+    mode = str(m["operationMode"])
+    d = ExperimentalData(None, mode)
+    d.ptychogram = i["ptychogram"]
+    d.encoder = i["encoder"]
+    d.dxd = float(m["dxd"])
+    d.wavelength = float(i["wavelength"])
+    if mode == "CPM":
+        d.zo = float(i["zo"])
+        d.entrancePupilDiameter = float(i["entrancePupilDiameter"])
+    else:
+        d.zled = float(m["zled"])
+        d.magnification = float(m["magnification"])
+        d.NA = float(m["NA"])
+    d._setData()
+    p = Params()
+    p.propagatorType = str(m["propagator"])
+    p.positionOrder = str(m["order"])
+    p.fftshiftSwitch = bool(m["fftshift"])
+    p.probeBoundary = bool(m["probeBoundary"])
+    p.orthogonalizationSwitch = bool(m["orthogonalizationSwitch"])
+    p.orthogonalizationFrequency = int(m["orthogonalizationFrequency"])
+    rec = Reconstruction(d, p, No=int(i["No"]) if mode == "FPM" else None)
+    nl, nos, nps, nsl = (int(v) for v in m["modes"])
+    rec.nlambda, rec.nosm, rec.npsm, rec.nslice = nl, nos, nps, nsl
+    if nsl > 1:
+        rec.dz = float(i["dz"])
+        rec.refrIndex = 1.0
+    return m, i, d, p, rec
+
+
+@pytest.mark.parametrize("name", fixture_names("reg_") + fixture_names("scan_"))
+def test_geometry_positions_and_seeded_guesses(name):
+    """Reconstruction.positions, No, dxp and the seeded initial guesses match the reference."""
+    fx = load_fixture(name)
+    m, i, d, p, rec = containers(fx)
+    assert rec.No == int(i["No"])
+    assert rec.dxp == pytest.approx(float(i["dxp"]), rel=1e-15)
+    np.testing.assert_array_equal(rec.positions, i["positions"])
+    np.testing.assert_array_equal(d.energyAtPos, i["energyAtPos"])
+    np.random.seed(int(m["seed"]))
+    rec.initializeObjectProbe()
+    np.testing.assert_array_equal(rec.object, i["init_object"])
+    np.testing.assert_array_equal(rec.probe, i["init_probe"])
+    assert d.entrancePupilDiameter == pytest.approx(float(i["entrancePupilDiameter"]), rel=1e-15)
+
+
+def test_random_order_and_momentum_draws_follow_the_global_rng():
+    """A shuffle then rand(n) consumes the legacy RNG like a shuffle then n x rand(1)
+    (BaseEngine.py:646-653, mPIE.py:170)."""
+    np.random.seed(3)
+    idx = np.arange(40)
+    np.random.shuffle(idx)
+    batch = np.random.rand(40)
+    np.random.seed(3)
+    idx2 = np.arange(40)
+    np.random.shuffle(idx2)
+    single = np.array([np.random.rand(1)[0] for _ in range(40)])
+    np.testing.assert_array_equal(idx, idx2)
+    np.testing.assert_array_equal(batch, single)
+
+
+@pytest.mark.parametrize("n", [32, 64, 128, 256])
+def test_tables_match_the_oracle(n):
+    dxp, lam, z = 1.3e-5, 632.8e-9, 0.05
+    np.testing.assert_array_equal(_tables.fresnel_chirp(z, lam, n, dxp), O.quad_phase(z, lam, n, dxp))
+    np.testing.assert_array_equal(
+        _tables.angular_spectrum_tf(z, lam, n, n * dxp), O.aspw_transfer_function(z, lam, n, n * dxp)
+    )
+    np.testing.assert_array_equal(
+        _tables.asp_detector_tf(z, lam, n, n * dxp)[None, None, None, None],
+        O.asp_transfer_function(1, 1, n, z, lam, n * dxp),
+    )
+
+
+def _bitrev5(l):
+    return int(f"{l:05b}"[::-1], 2)
+
+
+@pytest.mark.parametrize("n", [32, 64, 128, 256])
+def test_fourier_layout_is_a_permutation(n):
+    """slot s = 32 r + l holds frequency k = r + E*bitrev5(l) (kernel layout); a bijection."""
+    E = n // 32
+    k = np.array([(s >> 5) + E * _bitrev5(s & 31) for s in range(n)])
+    assert sorted(k.tolist()) == list(range(n))
+    # the inverse used by from_fourier_layout: s = 32*(k % E) + bitrev5(k // E)
+    s_back = np.array([32 * (kk % E) + _bitrev5(kk // E) for kk in k])
+    np.testing.assert_array_equal(s_back, np.arange(n))

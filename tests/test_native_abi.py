@@ -1,0 +1,60 @@
+"""The C-ABI library builds, loads without a GPU and exports every symbol include/ptyg.h declares."""
+
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from ptylab_gb300 import _build, _native
+
+    if not _native.LIB_PATH.exists():
+        _build.build()
+    return _native.load_library()
+
+
+def declared_functions():
+    text = (ROOT / "include" / "ptyg.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:PTYG_API\s+)?(?:int|const char\*)\s+(ptyg_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_bound_functions():
+    from ptylab_gb300 import _native
+
+    assert declared_functions() == _native.exported_symbols()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_version_and_error_string_without_gpu(lib):
+    assert lib.ptyg_version() == 1000
+    assert isinstance(lib.ptyg_last_error(), bytes)
+
+
+def test_invalid_geometry_is_rejected_before_touching_a_device(lib):
+    import ctypes as C
+
+    from ptylab_gb300 import _native
+
+    g = _native.Geometry(Np=48, No=64, nosm=1, npsm=1, nslice=1, num_frames=1, num_scans=1)
+    plan = C.c_void_p()
+    st = lib.ptyg_plan_create(C.byref(g), C.byref(plan))
+    assert st == _native.PTYG_ERR_UNSUPPORTED
+    assert b"Np=48" in lib.ptyg_last_error()
+    with pytest.raises(NotImplementedError):
+        _native.check(st, "ptyg_plan_create")
+
+
+def test_status_codes_map_to_reference_exceptions():
+    from ptylab_gb300 import _native
+
+    assert _native._EXC[_native.PTYG_ERR_INVALID] is ValueError
+    assert _native._EXC[_native.PTYG_ERR_UNSUPPORTED] is NotImplementedError
+    assert _native._EXC[_native.PTYG_ERR_DEVICE] is ImportError
