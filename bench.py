@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Throughput of the mPIE position loop on GB300: positions*iterations/s.
+
+Workload (the configuration the headline metric is quoted on): CPM mPIE,
+npsm = 4 probe modes, Np = 128, No = 512, 400 Fermat-spiral positions,
+alpha = beta = 0.25, friction 0.7, feedback 0.3, random position order and the
+reference's momentum draws (PtyLab/Engines/mPIE.py:96-195).  Seeded synthetic
+data (Gaussian-random-field object in amplitude [0.6, 1] and phase [0, 2*pi],
+Hermite-Gauss probe modes with powers 1:0.5:0.25:0.125, 1e6-photon Poisson
+intensities) stand in for measured scans.
+
+One step = one reconstruction iteration (every position once) over a batch
+of G independent scans, one thread-block cluster per scan, in one kernel
+launch; G is the number of clusters the GPU holds at once.  `value` is timed
+with CUDA events on the launching stream with all inputs resident in HBM; the
+batch streams G x 26 MB of intensities per step, more than L2 (129 MB), so no
+L2 flush is needed.  `e2e` runs the public API (ptylab_gb300.Engines.mPIE(...)
+.reconstruct()) on one scan from host NumPy arrays to host NumPy arrays.
+
+`--impl reference` times the reference algorithm's CPU implementation (the
+NumPy oracle, oracle/ptyoracle.py) on all host cores: one independent scan per
+process.  Under torchrun every rank reconstructs its own batch (weak scaling);
+rank 0 prints one JSON line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import multiprocessing as mp
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NP, NO, NPOS, NPSM = 128, 512, 400, 4
+METRIC = "positions*iterations/s, mPIE CPM npsm=4 Np=128 No=512 400 positions (1 GB300)"
+UNIT = "positions*iterations/s"
+WORKLOAD = "mPIE CPM Fraunhofer, npsm=4, nosm=1, Np=128, No=512, 400 Fermat positions, random order, momentum"
+
+
+def c1_spec(seed):
+    from ptylab_gb300.simulate import ScanSpec
+
+    return ScanSpec(
+        Np=NP, No=NO, num_positions=NPOS, npsm=NPSM, step_fraction=0.3, probe_radius_fraction=1 / 4,
+        photons=1e6, phase_max=2 * np.pi, amp_min=0.6, sigma_px=4.0, seed=seed,
+    )
+
+
+def make_scan(seed):
+    from ptylab_gb300.simulate import cpm_problem
+
+    d, p, rec, _, _ = cpm_problem(c1_spec(seed), engine_seed=seed)
+    p.positionOrder = "random"
+    return d, p, rec
+
+
+def scan_orders(seed, iters, nf):
+    """Per-iteration orders and momentum flags drawn as the reference draws them
+    (BaseEngine.py:646-653 shuffle from the third iteration, mPIE.py:170)."""
+    rs = np.random.RandomState(seed)
+    orders, flags = [], []
+    for it in range(iters):
+        idx = np.arange(nf)
+        if it >= 2:
+            rs.shuffle(idx)
+        orders.append(idx)
+        flags.append(rs.rand(nf) > 0.95)
+    return np.concatenate(orders).astype(np.int32), np.concatenate(flags).astype(np.uint8)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    QUERY = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, device_index):
+        self.proc = None
+        self.path = None
+        self.device_index = device_index
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.proc = subprocess.Popen(
+            ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+             "-i", str(self.device_index)],
+            stdout=open(self.path, "w"), stderr=subprocess.DEVNULL,
+        )
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r.split(", ") for r in Path(self.path).read_text().splitlines() if r.strip()]
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i].strip() == "Active"})
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons,
+            "samples": len(rows),
+        }
+
+
+# ------------------------------------------------------------------ peaks
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        j = json.loads(p.read_text())
+        return float(j["hbm_gbs"]), "measured", float(j.get("sm_max_mhz", 2070.0))
+    return 6800.0, "fallback", 2070.0
+
+
+def algorithmic_counts(flags_per_step, nscans):
+    """Per step (one launch): bytes and FP32 flops of the algorithm, not of the code.
+    Per position: object patch read + write (16*Np^2 B), intensities (4*Np^2 B);
+    the probe stays on chip.  Per momentum step: object and probe read (X, buffer,
+    momentum) and written (X, buffer, momentum): 48*(No^2 + npsm*Np^2) B.
+    Flops: 5*N*log2(N) per complex 2D transform of N = Np^2 points, two per mode,
+    plus 60 flops per pixel per mode of elementwise work."""
+    n2 = NP * NP
+    per_pos_bytes = 20 * n2
+    mom_bytes = 48 * (NO * NO + NPSM * n2)
+    bytes_ = nscans * NPOS * per_pos_bytes + flags_per_step * mom_bytes
+    per_pos_flops = NPSM * (2 * 5 * n2 * np.log2(n2) + 60 * n2)
+    flops = nscans * NPOS * per_pos_flops + flags_per_step * 12 * (NO * NO + NPSM * n2)
+    return float(bytes_), float(flops), float(per_pos_bytes), float(per_pos_flops)
+
+
+# ------------------------------------------------------------------ gb300 arm
+def run_gb300(args, rank, world, local_rank):
+    import torch
+
+    from ptylab_gb300 import DummyMonitor, Engines, _native
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    lib = _native.require(local_rank)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def geometry(nscans):
+        return _native.Geometry(Np=NP, No=NO, nosm=1, npsm=NPSM, nslice=1, num_frames=NPOS, num_scans=nscans,
+                                engine=_native.ENGINES["mPIE"], propagator=0, fftshift=0, fpm=0,
+                                cluster=args.cluster)
+
+    probe_plan = C.c_void_p()
+    _native.check(lib.ptyg_plan_create(C.byref(geometry(1)), C.byref(probe_plan)))
+    cl, th, sm, maxc = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    _native.check(lib.ptyg_plan_info(probe_plan, C.byref(cl), C.byref(th), C.byref(sm), C.byref(maxc)))
+    lib.ptyg_plan_destroy(probe_plan)
+    G = args.scans if args.scans > 0 else max(1, maxc.value)
+    iters = args.warmup + args.steps
+
+    def build_batch(nscans, seed0):
+        keep, plan = [], C.c_void_p()
+        _native.check(lib.ptyg_plan_create(C.byref(geometry(nscans)), C.byref(plan)))
+        mom_total = 0
+        flag_counts = np.zeros(iters, dtype=np.int64)
+        for s in range(nscans):
+            seed = seed0 + s
+            d, p, rec = make_scan(seed)
+            t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)  # noqa: E731
+            obj = t(rec.object, torch.complex64)
+            prb = t(rec.probe, torch.complex64)
+            bufs = [obj.clone(), torch.zeros_like(obj), prb.clone(), torch.zeros_like(prb)]
+            pos = t(rec.positions.astype(np.int32), torch.int32)
+            data = t(d.ptychogram, torch.float32)
+            order, flags = scan_orders(seed, iters, NPOS)
+            flag_counts += flags.reshape(iters, NPOS).sum(axis=1).astype(np.int64)
+            od, fd = t(order, torch.int32), t(flags, torch.uint8)
+            b = _native.ScanBuffers(object=obj.data_ptr(), probe=prb.data_ptr(), positions=pos.data_ptr(),
+                                    order=od.data_ptr(), momentum_flags=fd.data_ptr(),
+                                    object_buffer=bufs[0].data_ptr(), object_momentum=bufs[1].data_ptr(),
+                                    probe_buffer=bufs[2].data_ptr(), probe_momentum=bufs[3].data_ptr())
+            _native.check(lib.ptyg_plan_bind_scan(plan, s, C.byref(b), data.data_ptr(), sptr))
+            _native.check(lib.ptyg_plan_set_order(plan, s, od.data_ptr(), fd.data_ptr(), iters * NPOS, sptr))
+            keep += [obj, prb, pos, data, od, fd, b] + bufs
+        return plan, keep, flag_counts
+
+    u = _native.UpdateParams(beta_object=0.25, beta_probe=0.25, alpha_object=0.25, alpha_probe=0.25,
+                             reg_object=1.0, reg_probe=1.0, friction=0.7, feedback=0.3, probe_weight=1.0,
+                             slice_beta=0.9)
+
+    def timed(plan, nsteps, nwarm):
+        for w in range(nwarm):
+            _native.check(lib.ptyg_plan_run(plan, C.byref(u), w * NPOS, NPOS, 0, sptr))
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(nsteps):
+            _native.check(lib.ptyg_plan_run(plan, C.byref(u), (nwarm + k) * NPOS, NPOS, 0, sptr))
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        return e0.elapsed_time(e1) / 1e3
+
+    # batched, device-resident: the headline
+    plan, keep, flag_counts = build_batch(G, 1000 * rank + 1)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    t = timed(plan, args.steps, args.warmup)
+    clk = clocks.stop()
+    lib.ptyg_plan_destroy(plan)
+    del keep
+    if world > 1:
+        tt = torch.tensor([t], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * G * NPOS * args.steps / t
+    ms_per_step = t / args.steps * 1e3
+    flags_timed = float(flag_counts[args.warmup:].sum()) / args.steps
+    bytes_step, flops_step, per_pos_bytes, per_pos_flops = algorithmic_counts(flags_timed, G)
+    hbm_peak, peak_kind, _ = measured_peaks()
+    achieved_gbs = bytes_step / (t / args.steps) / 1e9
+    props = torch.cuda.get_device_properties(dev)
+    sm_max = (clk or {}).get("sm_max_mhz") or 2070.0
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved_tf = flops_step / (t / args.steps) / 1e12
+
+    out = {}
+    if rank == 0:
+        # one scan alone: latency view of the same kernel
+        plan1, keep1, _ = build_batch(1, 7)
+        t1 = timed(plan1, min(args.steps, 50), args.warmup)
+        lib.ptyg_plan_destroy(plan1)
+        del keep1
+        single = {"value": NPOS * min(args.steps, 50) / t1, "us_per_position": t1 / (min(args.steps, 50) * NPOS) * 1e6}
+
+        # end to end through the public API, host NumPy in and out
+        d, p, rec = make_scan(99)
+        eng = Engines.mPIE(rec, d, p, DummyMonitor())
+        eng.numIterations = args.warmup
+        eng.reconstruct()
+        d, p, rec = make_scan(99)
+        eng = Engines.mPIE(rec, d, p, DummyMonitor())
+        eng.numIterations = args.steps
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        eng.reconstruct()
+        torch.cuda.synchronize(dev)
+        te = time.perf_counter() - t0
+        h2d = d.ptychogram.nbytes + 3 * rec.object.nbytes + 3 * rec.probe.nbytes + NPOS * 2 * 4 + args.steps * NPOS * 5
+        d2h = 3 * rec.object.nbytes + 3 * rec.probe.nbytes + args.steps * NPOS * 8 + NPOS * NP * NP * 4
+        e2e = {"value": NPOS * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+               "d2h_bytes_per_step": int(d2h / args.steps), "scans": 1,
+               "api": "ptylab_gb300.Engines.mPIE(...).reconstruct(), NumPy in/out"}
+
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 (FP32 complex; FP64 error sums and momentum arithmetic)",
+            "data": "synthetic: seeded Fermat scans, GRF objects, Hermite-Gauss probes, 1e6-photon Poisson",
+            "config": {
+                "workload": WORKLOAD, "scans_per_gpu": G, "cluster_ctas_per_scan": cl.value,
+                "threads_per_cta": th.value, "smem_per_cta": sm.value, "parallelism": f"replicas x{world}",
+                "l2": f"no flush: each step streams {G} x {NPOS * NP * NP * 4 / 1e6:.1f} MB of intensities (> 129 MB L2)",
+                "step": "one iteration over every position of every scan, one kernel launch",
+            },
+            "roofline": {
+                "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_position": per_pos_bytes, "bytes_per_launch": bytes_step,
+            },
+            "roofline_fp32": {
+                "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
+                "peak_kind": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock",
+                "flops_per_position": per_pos_flops,
+            },
+            "gpu_launches": args.steps,
+            "clocks": clk,
+            "single_scan": single,
+            "e2e": e2e,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(args.cpu_iters)
+    return out
+
+
+# ------------------------------------------------------------------ CPU legs
+def _oracle_scan(seed):
+    from oracle import ptyoracle as O
+
+    d, p, rec = make_scan(seed)
+    g = O.Geometry(Np=NP, No=NO, dxp=rec.dxp, wavelength=rec.wavelength, zo=rec.zo, npsm=NPSM)
+    s = O.Settings(engine="mPIE", order="random", alphaObject=0.25, alphaProbe=0.25,
+                   entrancePupilDiameter=d.entrancePupilDiameter)
+    st = O.State(object=rec.object.copy(), probe=rec.probe.copy())
+    return O.OracleEngine(s, g, st, d.ptychogram, rec.positions, d.energyAtPos)
+
+
+def _oracle_worker(args):
+    seed, warm, steps, barrier = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    eng = _oracle_scan(seed)
+    np.random.seed(seed)
+    eng.reconstruct(warm)
+    if barrier is not None:
+        barrier.wait()
+    t0 = time.perf_counter()
+    eng.reconstruct(steps)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(iters):
+    """The oracle's mPIE on this host, one core, one C1 scan, `iters` iterations."""
+    t = _oracle_worker((5, 1, iters, None))
+    return {"value": NPOS * iters / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"one C1 scan, {iters} iterations x {NPOS} positions after 1 warm-up iteration"}
+
+
+def run_reference(args):
+    ncores = os.cpu_count() or 1
+    nproc = args.ref_procs if args.ref_procs > 0 else ncores
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as m:
+        barrier = m.Barrier(nproc)
+        with ctx.Pool(nproc) as pool:
+            times = pool.map(_oracle_worker, [(11 + i, args.warmup_ref, args.steps, barrier) for i in range(nproc)])
+    t = max(times)
+    value = nproc * NPOS * args.steps / t
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (NumPy complex64, as the reference)",
+        "data": "synthetic: seeded Fermat scans, GRF objects, Hermite-Gauss probes, 1e6-photon Poisson",
+        "config": {"workload": WORKLOAD, "scans": nproc, "parallelism": f"{nproc} processes, one scan each"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
+                         "sample": f"{nproc} independent C1 scans, {args.steps} iterations each, after {args.warmup_ref} warm-up"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scans", type=int, default=0, help="independent scans per GPU (0: as many as fit at once)")
+    ap.add_argument("--cluster", type=int, default=0, help="CTAs per scan (0: the library's choice)")
+    ap.add_argument("--cpu-iters", type=int, default=8, help="iterations of the one-core CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-procs", type=int, default=0)
+    ap.add_argument("--warmup-ref", type=int, default=1)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            # reference CPU steps are ~1 s each: cap the sample so the run stays within minutes
+            args.steps = min(args.steps, 10)
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    out = run_gb300(args, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

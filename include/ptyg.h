@@ -142,6 +142,17 @@ PTYG_API int ptyg_plan_set_tables(ptyg_plan* plan, const void* fresnel_q, const 
 PTYG_API int ptyg_plan_bind_scan(ptyg_plan* plan, int scan, const ptyg_scan_buffers* buffers, const float* ptychogram,
                         void* stream);
 
+/* Point scan `scan` at a new order array (and mPIE momentum flags) of
+ * `length` slots without reloading its data; ptyg_plan_run's slots index it.
+ * The bind call sets length = num_frames. */
+PTYG_API int ptyg_plan_set_order(ptyg_plan* plan, int scan, const int32_t* order, const uint8_t* momentum_flags,
+                                 int length, void* stream);
+
+/* Launch shape the plan chose: CTAs per scan (cluster size), threads per CTA,
+ * dynamic shared memory per CTA, and how many such clusters can be resident
+ * on the device at once (independent scans that run concurrently). */
+PTYG_API int ptyg_plan_info(ptyg_plan* plan, int* cluster, int* threads, int* smem_bytes, int* max_active_clusters);
+
 /* Process order slots [start, start+count) of every bound scan: for each
  * slot, position order[slot] goes through gather -> propagate -> intensity
  * projection -> back-propagate -> object/probe update (-> momentum step).

@@ -97,6 +97,10 @@ _SIGNATURES = {
     "ptyg_plan_set_tables": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
     "ptyg_plan_bind_scan": [C.c_void_p, C.c_int, C.POINTER(ScanBuffers), C.c_void_p, C.c_void_p],
     "ptyg_plan_run": [C.c_void_p, C.POINTER(UpdateParams), C.c_int, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_plan_set_order": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p],
+    "ptyg_plan_info": [
+        C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+    ],
     "ptyg_plan_frame_errors": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_detector_error": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_status": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p],

@@ -197,6 +197,7 @@ struct ScanOwned {
   unsigned* red = nullptr;
   int* status = nullptr;
   bool bound = false;
+  int orderLen = 0;
   ptyg_scan_buffers buf = {};
 };
 
@@ -415,6 +416,7 @@ extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffe
   d.red = o.red;
   d.status = o.status;
   o.bound = true;
+  o.orderLen = p->g.num_frames;
   PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &d, sizeof(ScanDev), cudaMemcpyHostToDevice, st), "scan upload");
   // the host copy must outlive the async copy: hScans is owned by the plan
   return PTYG_OK;
@@ -428,8 +430,10 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
     if (!p->scans[s].bound) return fail(PTYG_ERR_INVALID, "scan %d is not bound", s);
   if (count == 0) return PTYG_OK;
   const ptyg_geometry& g = p->g;
-  if ((long long)start + count > g.num_frames)
-    return fail(PTYG_ERR_INVALID, "order slots [%d, %d) exceed num_frames=%d", start, start + count, g.num_frames);
+  for (int s = 0; s < g.num_scans; ++s)
+    if ((long long)start + count > p->scans[s].orderLen)
+      return fail(PTYG_ERR_INVALID, "order slots [%d, %d) exceed the %d slots of scan %d", start, start + count,
+                  p->scans[s].orderLen, s);
   cudaStream_t st = (cudaStream_t)stream;
   if (g.propagator == PTYG_FRESNEL && !p->fresnelQ) return fail(PTYG_ERR_INVALID, "Fresnel table not set");
   if (g.propagator == PTYG_ASP && !p->aspH) return fail(PTYG_ERR_INVALID, "ASP transfer function not set");
@@ -478,6 +482,36 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
   a.bethSlice = u->slice_beta;
   cudaError_t e = ptyg::launch_engine(a, g.num_scans, p->threads, p->smem, st);
   if (e != cudaSuccess) return cuda_fail(e, "engine launch");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_set_order(ptyg_plan* p, int scan, const int32_t* order, const uint8_t* momentum_flags,
+                                   int length, void* stream) {
+  if (!p || !order) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  if (!p->scans[scan].bound) return fail(PTYG_ERR_INVALID, "scan %d is not bound", scan);
+  if (length < 1) return fail(PTYG_ERR_INVALID, "length=%d", length);
+  if (p->g.engine == PTYG_MPIE && !momentum_flags) return fail(PTYG_ERR_INVALID, "mPIE needs momentum flags");
+  p->hScans[scan].order = order;
+  p->hScans[scan].momentum = momentum_flags;
+  p->scans[scan].orderLen = length;
+  PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &p->hScans[scan], sizeof(ScanDev), cudaMemcpyHostToDevice,
+                            (cudaStream_t)stream),
+            "scan upload");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_info(ptyg_plan* p, int* cluster, int* threads, int* smem_bytes, int* max_active_clusters) {
+  if (!p) return fail(PTYG_ERR_INVALID, "null plan");
+  if (cluster) *cluster = p->C;
+  if (threads) *threads = p->threads;
+  if (smem_bytes) *smem_bytes = (int)p->smem;
+  if (max_active_clusters) {
+    int n = 0;
+    cudaError_t e = ptyg::engine_max_clusters(p->g.Np, p->g.nosm, p->g.npsm, p->C, p->threads, p->smem, &n);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveClusters");
+    *max_active_clusters = n;
+  }
   return PTYG_OK;
 }
 
