@@ -75,6 +75,23 @@ PTYG_API int ptyg_device_init(int device);
 PTYG_API int ptyg_propagate(int propagator, int direction, int fftshift, int Np, int batch, const void* in, void* out,
                    const void* table, void* scratch, void* stream);
 
+/* The propagators of ptyg_propagate for callers that cannot allocate GPU
+ * memory: code inside a host framework that owns every device allocation, a
+ * real-time acquisition callback where cudaMalloc's implicit synchronisation
+ * would stall the pipeline, or a process that has reserved all of HBM for its
+ * own buffers.  No counterpart in the reference (PtyLab has no C interface);
+ * it exists for these callers only.  The call allocates nothing: its scratch
+ * is an 8 MiB array built into the library, held by every GPU that loads it
+ * until the process exits, so batch*Np*Np must not exceed 1,048,576 points
+ * (larger batches fail with PTYG_ERR_INVALID).  The first call on a device
+ * resolves and fills that device's built-in arrays (a synchronous copy), so
+ * make it before any stream capture.  All calls share the one scratch array:
+ * calls that overlap on the GPU (different streams, or threads) race and must
+ * be serialised by the caller.  Same arguments as ptyg_propagate, without
+ * `scratch`. */
+PTYG_API int ptyg_propagate_noalloc(int propagator, int direction, int fftshift, int Np, int batch, const void* in,
+                                    void* out, const void* table, void* stream);
+
 /* ------------------------------------------------------------------------
  * Engine plans: the drop-in for the position loop of ePIE.reconstruct_stepwise
  * (PtyLab/Engines/ePIE.py:78-112), mPIE.reconstruct (mPIE.py:276-333),

@@ -92,6 +92,9 @@ _SIGNATURES = {
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
     ],
+    "ptyg_propagate_noalloc": [
+        C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+    ],
     "ptyg_plan_create": [C.POINTER(Geometry), C.POINTER(C.c_void_p)],
     "ptyg_plan_destroy": [C.c_void_p],
     "ptyg_plan_set_tables": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],

@@ -31,6 +31,14 @@ static int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+namespace ptyg {
+// Record a failure for ptyg_last_error() from other translation units.
+int set_last_error(int code, const char* msg) {
+  g_last_error = msg;
+  return code;
+}
+}  // namespace ptyg
+
 static int cuda_fail(cudaError_t e, const char* what) {
   if (e == cudaErrorMemoryAllocation) return fail(PTYG_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
   if (e == cudaErrorNotSupported) return fail(PTYG_ERR_UNSUPPORTED, "%s: configuration not supported", what);

@@ -88,7 +88,7 @@ __global__ void prop_row_kernel(const float2* __restrict__ in, float2* __restric
 // memory; one warp transforms one column (optionally: transform, multiply by
 // a Fourier-plane filter, transform again), then the block is written back.
 template <int E>
-__global__ void prop_col_kernel(const float2* __restrict__ in, float2* __restrict__ out, int batch, ColOp op,
+__global__ void prop_col_kernel(const float2* in, float2* out, int batch, ColOp op,
                                 const float2* __restrict__ twiddle) {
   constexpr int NP = 32 * E;
   constexpr int CB = 8;

@@ -46,6 +46,8 @@ cudaError_t mul_window(float2* x, const float* w, long long n, long long nw, cud
 cudaError_t gram(const float2* p, int modes, long long n, double2* G, cudaStream_t st);
 cudaError_t mix_modes(const float2* V, const float2* p, float2* out, int modes, long long n, cudaStream_t st);
 
+int set_last_error(int code, const char* msg);
+
 size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine);
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 bool engine_modes_supported(int Np, int nosm, int npsm);
