@@ -30,6 +30,10 @@ FLAGS = [
     "-Xcompiler",
     "-fvisibility=hidden",
     "--expt-relaxed-constexpr",
+    # approximate division and square root (a few ulp): the intensity
+    # projection and update weights stay far inside the 1e-4 parity budget
+    "-prec-div=false",
+    "-prec-sqrt=false",
     f"-I{ROOT / 'include'}",
     f"-I{CSRC}",
 ]

@@ -202,6 +202,7 @@ struct ScanOwned {
   double* errPart = nullptr;
   double* err = nullptr;
   float* detErr = nullptr;
+  float* tileMax = nullptr;
   unsigned* red = nullptr;
   int* status = nullptr;
   bool bound = false;
@@ -235,6 +236,7 @@ static void plan_free(ptyg_plan* p) {
     cudaFree(s.errPart);
     cudaFree(s.err);
     cudaFree(s.detErr);
+    cudaFree(s.tileMax);
     cudaFree(s.red);
     cudaFree(s.status);
   }
@@ -242,18 +244,23 @@ static void plan_free(ptyg_plan* p) {
   delete p;
 }
 
-static int choose_cluster(const ptyg_geometry& g, int* C, int* threads) {
-  int c = g.cluster;
-  if (c <= 0) c = g.Np / 8;  // 8 rows per CTA
-  if (c > 16) c = 16;
-  if (c < 1) c = 1;
-  if (g.Np % c != 0 || (c & (c - 1)) != 0) return fail(PTYG_ERR_INVALID, "cluster=%d must be a power of two dividing Np", c);
-  const int L = g.Np / c;
-  int w = L < 8 ? L : 8;
-  if (w < 4) w = 4;
-  *C = c;
-  *threads = 32 * w;
-  return PTYG_OK;
+// One warp per 1D-transform task of a pass (K modes x L lines), 4..16 warps.
+static int engine_threads(const ptyg_geometry& g, int C) {
+  const int tasks = g.nosm * g.npsm * (g.Np / C);
+  const int w = tasks < 4 ? 4 : (tasks > 16 ? 16 : tasks);
+  return 32 * w;
+}
+
+// Cluster sizes to try, best first: 8 rows per CTA (more CTAs, shorter
+// passes), then 16.  A requested size (geometry.cluster) goes first.
+static std::vector<int> cluster_candidates(const ptyg_geometry& g) {
+  std::vector<int> c;
+  if (g.cluster > 0) c.push_back(g.cluster);
+  for (int L : {8, 16}) {
+    const int cc = g.Np / L;
+    if (cc >= 1 && cc <= 16) c.push_back(cc);
+  }
+  return c;
 }
 
 extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan) {
@@ -281,32 +288,31 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   if (!p) return fail(PTYG_ERR_OOM, "host allocation");
   p->g = g;
   p->device = dev;
-  r = choose_cluster(g, &p->C, &p->threads);
-  if (r) {
-    plan_free(p);
-    return r;
-  }
   int maxSmem = 0;
   cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  // largest cluster (<= the requested one) that fits in shared memory and can be co-scheduled
-  for (;;) {
-    p->smem = ptyg::engine_smem_bytes(g.Np, p->C, g.nosm, g.npsm, g.engine);
+  // the first instantiated cluster shape that fits in shared memory and can be co-scheduled
+  bool found = false;
+  for (int c : cluster_candidates(g)) {
+    if (!ptyg::engine_shape_supported(g.Np, c)) continue;
+    p->C = c;
+    p->threads = engine_threads(g, c);
+    p->smem = ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.engine);
+    if ((int)p->smem > maxSmem) continue;
     int nclusters = 0;
-    cudaError_t e = cudaSuccess;
-    if ((int)p->smem <= maxSmem) {
-      e = ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, p->C, p->threads, p->smem, &nclusters);
-      if (e != cudaSuccess) cudaGetLastError();
+    cudaError_t e = ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, c, p->threads, p->smem, &nclusters);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      continue;
     }
-    if (e == cudaSuccess && nclusters > 0) break;
-    if (p->C == 1) {
-      plan_free(p);
-      return fail(PTYG_ERR_UNSUPPORTED, "no launchable cluster shape (needs %zu B shared memory per CTA, max %d)",
-                  p->smem, maxSmem);
+    if (nclusters > 0) {
+      found = true;
+      break;
     }
-    p->C /= 2;
-    const int L = g.Np / p->C;
-    const int w = L < 8 ? (L < 4 ? 4 : L) : 8;
-    p->threads = 32 * w;
+  }
+  if (!found) {
+    plan_free(p);
+    return fail(PTYG_ERR_UNSUPPORTED, "no launchable cluster shape for Np=%d nosm=%d npsm=%d (shared memory %zu B, max %d)",
+                g.Np, g.nosm, g.npsm, p->smem, maxSmem);
   }
   const size_t np2 = (size_t)g.Np * g.Np;
   const int K = g.nosm * g.npsm;
@@ -321,6 +327,10 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
     if (e == cudaSuccess) e = cudaMalloc(&o.err, (size_t)g.num_frames * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&o.red, 2 * ptyg::RED_BANK * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&o.status, sizeof(int));
+    if (e == cudaSuccess && g.engine == PTYG_QNEWTON) {
+      const int tpr = (g.No + ptyg::TILE - 1) / ptyg::TILE;
+      e = cudaMalloc(&o.tileMax, (size_t)tpr * tpr * sizeof(float));
+    }
     if (e == cudaSuccess) e = cudaMemset(o.status, 0, sizeof(int));
     if (e != cudaSuccess) {
       plan_free(p);
@@ -423,6 +433,7 @@ extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffe
   d.detErr = o.detErr;
   d.red = o.red;
   d.status = o.status;
+  d.tileMax = o.tileMax;
   o.bound = true;
   o.orderLen = p->g.num_frames;
   PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &d, sizeof(ScanDev), cudaMemcpyHostToDevice, st), "scan upload");
@@ -478,6 +489,7 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
   a.count = count;
   a.writeDetErr = det;
   a.cluster = p->C;
+  a.tilesPerRow = (g.No + ptyg::TILE - 1) / ptyg::TILE;
   a.betaO = u->beta_object;
   a.betaP = u->beta_probe;
   a.alphaO = u->alpha_object;

@@ -50,22 +50,36 @@ PTYG_DEV float ld_cg(const float* p) { return __ldcg(p); }
 
 PTYG_DEV unsigned bitrev5(unsigned l) { return __brev(l) >> 27; }
 
-// ------------------------------------------------- 16th roots of unity, W16^m
-// exp(-2*pi*i*m/16) for m = 0..7 (forward sign).  Values of cos/sin(k*pi/8).
-PTYG_DEV float2 w16(int m) {
+// ------------------------------------------------- in-register small DFTs
+// Multiply by W_16^m (forward sign exp(-2*pi*i*m/16)), m a compile-time
+// constant after unrolling; the trivial rotations cost no multiplies.
+template <bool INV>
+PTYG_DEV float2 mul_w16(float2 a, int m) {
   const float c1 = 0.92387953251128674f;  // cos(pi/8)
   const float s1 = 0.38268343236508978f;  // sin(pi/8)
   const float h = 0.70710678118654752f;   // sqrt(1/2)
-  switch (m & 7) {
-    case 0: return make_float2(1.f, 0.f);
-    case 1: return make_float2(c1, -s1);
-    case 2: return make_float2(h, -h);
-    case 3: return make_float2(s1, -c1);
-    case 4: return make_float2(0.f, -1.f);
-    case 5: return make_float2(-s1, -c1);
-    case 6: return make_float2(-h, -h);
-    default: return make_float2(-c1, -s1);
+  // forward W16^m = (cos, -sin); the inverse uses the conjugate
+  float c, sn;
+  switch (m & 15) {
+    case 0: return a;
+    case 4: return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);  // * (+i) / (-i)
+    case 8: return make_float2(-a.x, -a.y);
+    case 12: return INV ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+    case 2: c = h; sn = h; break;
+    case 6: c = -h; sn = h; break;
+    case 10: c = -h; sn = -h; break;
+    case 14: c = h; sn = -h; break;
+    case 1: c = c1; sn = s1; break;
+    case 3: c = s1; sn = c1; break;
+    case 5: c = -s1; sn = c1; break;
+    case 7: c = -c1; sn = s1; break;
+    case 9: c = -c1; sn = -s1; break;
+    case 11: c = -s1; sn = -c1; break;
+    case 13: c = s1; sn = -c1; break;
+    default: c = c1; sn = -s1; break;  // 15
   }
+  if (!INV) sn = -sn;
+  return make_float2(fmaf(a.x, c, -a.y * sn), fmaf(a.x, sn, a.y * c));
 }
 
 template <int E>
@@ -85,8 +99,8 @@ PTYG_DEV int rev_bits(int i) {
   return r;
 }
 
-// In-register E-point DFT, natural order in and out.  Radix-2 decimation in
-// frequency followed by a compile-time bit-reversal (register renaming).
+// In-register E-point DFT (E <= 16), natural order in and out: radix-2
+// decimation in frequency, then a compile-time bit reversal (register renaming).
 template <int E, bool INV>
 PTYG_DEV void dft_reg(float2 (&v)[E]) {
   if constexpr (E > 1) {
@@ -99,9 +113,7 @@ PTYG_DEV void dft_reg(float2 (&v)[E]) {
           const float2 a = v[start + m];
           const float2 b = v[start + m + span];
           v[start + m] = cadd(a, b);
-          float2 w = w16(m * (16 / (2 * span)));
-          if (INV) w.y = -w.y;
-          v[start + m + span] = cmul(csub(a, b), w);
+          v[start + m + span] = mul_w16<INV>(csub(a, b), m * (16 / (2 * span)));
         }
       }
     }
@@ -113,70 +125,128 @@ PTYG_DEV void dft_reg(float2 (&v)[E]) {
   }
 }
 
-// Per-lane twiddles of the five cross-lane stages: W_{2h}^(lane mod h) for
-// h = 16, 8, 4, 2, 1 (forward sign), read from the N-point table.
-struct LaneTw {
-  float2 w[5];
+// One warp transforms one line of N = 32*E points (see the layout note at the
+// top).  Per-lane twiddles live in registers for the life of the object:
+// W_N^(lane*k1) for k1 = 1..E-1, and for the cross-lane stages h = 16, 8, 4
+// W_(2h)^(lane mod h) on upper lanes (1 on lower lanes).  Stage h = 2 needs
+// only the rotation by -i and stage h = 1 no twiddle at all.
+template <int E>
+struct WarpFFT {
+  float2 tl[E > 1 ? E - 1 : 1];
+  float2 ts[3];
+  unsigned lane;
+
+  // `tw` is the N-entry table W_N^m (global or shared memory).
+  PTYG_DEV void init(const float2* tw, unsigned ln) {
+    lane = ln;
+#pragma unroll
+    for (int k = 1; k < E; ++k) tl[k - 1] = tw[lane * k];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int h = 16 >> s;
+      ts[s] = (lane & h) ? tw[(lane & (h - 1)) * (16 * E / h)] : make_float2(1.f, 0.f);
+    }
+  }
+
+  // natural -> Fourier layout, unnormalised, exp(-i...), on M lines at once
+  // (independent lines interleave, hiding shuffle latency)
+  template <int M>
+  PTYG_DEV void fwdm(float2 (&v)[M][E]) const {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      dft_reg<E, false>(v[m]);
+#pragma unroll
+      for (int k = 1; k < E; ++k) v[m][k] = cmul(v[m][k], tl[k - 1]);
+    }
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      const int h = 16 >> s;
+      const float sg = (lane & h) ? -1.f : 1.f;
+      const bool rot = (s == 3) && (lane & 2) && (lane & 1);
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+          float2 o;
+          o.x = __shfl_xor_sync(0xffffffffu, v[m][r].x, h);
+          o.y = __shfl_xor_sync(0xffffffffu, v[m][r].y, h);
+          // lower lane: mine + other ; upper lane: (other - mine) * w
+          float2 t = make_float2(fmaf(sg, v[m][r].x, o.x), fmaf(sg, v[m][r].y, o.y));
+          if (s < 3) t = cmul(t, ts[s]);
+          else if (s == 3) t = rot ? make_float2(t.y, -t.x) : t;
+          v[m][r] = t;
+        }
+      }
+    }
+  }
+
+  // Fourier layout -> natural, unnormalised, exp(+i...), on M lines at once
+  template <int M>
+  PTYG_DEV void invm(float2 (&v)[M][E]) const {
+#pragma unroll
+    for (int s = 4; s >= 0; --s) {
+      const int h = 16 >> s;
+      const bool upper = (lane & h) != 0;
+      const float sg = upper ? -1.f : 1.f;
+      const bool rot = (s == 3) && upper && (lane & 1);
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+          // the upper lane pre-multiplies its own value by conj(w); then
+          // lower: mine + other ; upper: other - mine
+          float2 c = v[m][r];
+          if (s < 3) c = cmulc(ts[s], c);
+          else if (s == 3) c = rot ? make_float2(-c.y, c.x) : c;
+          float2 o;
+          o.x = __shfl_xor_sync(0xffffffffu, c.x, h);
+          o.y = __shfl_xor_sync(0xffffffffu, c.y, h);
+          v[m][r] = make_float2(fmaf(sg, c.x, o.x), fmaf(sg, c.y, o.y));
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+#pragma unroll
+      for (int k = 1; k < E; ++k) v[m][k] = cmulc(tl[k - 1], v[m][k]);
+      dft_reg<E, true>(v[m]);
+    }
+  }
+
+  PTYG_DEV void fwd(float2 (&v)[E]) const { fwdm<1>(reinterpret_cast<float2(&)[1][E]>(v)); }
+  PTYG_DEV void inv(float2 (&v)[E]) const { invm<1>(reinterpret_cast<float2(&)[1][E]>(v)); }
 };
 
-template <int E>
-PTYG_DEV LaneTw lane_twiddles(const float2* tw /* N = 32*E entries */, unsigned lane) {
-  LaneTw t;
-#pragma unroll
-  for (int s = 0; s < 5; ++s) {
-    const int h = 16 >> s;
-    t.w[s] = tw[(lane & (h - 1)) * (16 * E / h)];
+// Run `ntasks` independent line transforms over the warps of the CTA, two
+// per warp at a time: load(task, v) fills a line, store(task, v) consumes the
+// transformed line.  A __syncwarp separates the loads of a pair from its
+// stores, so a task may store in place of what it loaded.
+template <int E, bool INV, class LoadF, class StoreF>
+PTYG_DEV void fft_tasks(const WarpFFT<E>& F, int ntasks, LoadF&& load, StoreF&& store) {
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int t = warp;
+  for (; t + nw < ntasks; t += 2 * nw) {
+    float2 v[2][E];
+    load(t, v[0]);
+    load(t + nw, v[1]);
+    if (INV)
+      F.template invm<2>(v);
+    else
+      F.template fwdm<2>(v);
+    __syncwarp();
+    store(t, v[0]);
+    store(t + nw, v[1]);
   }
-  return t;
-}
-
-// Forward: natural -> Fourier layout, unnormalised.
-template <int E>
-PTYG_DEV void fft_fwd(float2 (&v)[E], const float2* tw, const LaneTw& lt, unsigned lane) {
-  dft_reg<E, false>(v);
-#pragma unroll
-  for (int k1 = 1; k1 < E; ++k1) v[k1] = cmul(v[k1], tw[lane * k1]);
-#pragma unroll
-  for (int s = 0; s < 5; ++s) {
-    const int h = 16 >> s;
-    const bool upper = (lane & h) != 0;
-    const float sg = upper ? -1.f : 1.f;
-    const float2 w = upper ? lt.w[s] : make_float2(1.f, 0.f);
-#pragma unroll
-    for (int r = 0; r < E; ++r) {
-      float2 o;
-      o.x = __shfl_xor_sync(0xffffffffu, v[r].x, h);
-      o.y = __shfl_xor_sync(0xffffffffu, v[r].y, h);
-      // lower lane: mine + other ; upper lane: (other - mine) * w
-      const float2 s2 = make_float2(fmaf(sg, v[r].x, o.x), fmaf(sg, v[r].y, o.y));
-      v[r] = cmul(s2, w);
-    }
+  if (t < ntasks) {
+    float2 v[E];
+    load(t, v);
+    if (INV)
+      F.inv(v);
+    else
+      F.fwd(v);
+    __syncwarp();
+    store(t, v);
   }
-}
-
-// Inverse: Fourier layout -> natural, unnormalised (sum with exp(+i...)).
-template <int E>
-PTYG_DEV void fft_inv(float2 (&v)[E], const float2* tw, const LaneTw& lt, unsigned lane) {
-#pragma unroll
-  for (int s = 4; s >= 0; --s) {
-    const int h = 16 >> s;
-    const bool upper = (lane & h) != 0;
-    const float2 wc = cconj(lt.w[s]);
-#pragma unroll
-    for (int r = 0; r < E; ++r) {
-      float2 o;
-      o.x = __shfl_xor_sync(0xffffffffu, v[r].x, h);
-      o.y = __shfl_xor_sync(0xffffffffu, v[r].y, h);
-      // lower: mine + conj(w)*other ; upper: other - conj(w)*mine
-      const float2 p = upper ? o : v[r];
-      const float2 q = upper ? v[r] : o;
-      const float2 t = cmul(q, wc);
-      v[r] = upper ? csub(p, t) : cadd(p, t);
-    }
-  }
-#pragma unroll
-  for (int k1 = 1; k1 < E; ++k1) v[k1] = cmulc(tw[lane * k1], v[k1]);
-  dft_reg<E, true>(v);
 }
 
 // Index helpers for the two layouts.

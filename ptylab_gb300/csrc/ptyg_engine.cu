@@ -5,22 +5,34 @@
 // clusters reconstructs G independent scans.  The cluster walks the positions
 // of one iteration in the order the host drew (PtyLab/Engines/BaseEngine.py:637-665)
 // and, for each position, runs the body of ePIE.py:84-105 / mPIE.py:280-332 /
-// qNewton.py:69-90 as a sequence of passes separated by cluster barriers:
+// qNewton.py:69-90 as passes separated by cluster barriers.  CTA c owns rows
+// [c*L, (c+1)*L) of every row pass and Fourier-layout columns [c*L, (c+1)*L)
+// of every column pass (L = Np/C), so it always updates the same probe rows
+// and keeps them in shared memory for the whole launch.
 //
-//   A  row pass     : gather object rows (coalesced), exit waves O_o*P_p for every
-//                     (object mode, probe mode), [Fresnel chirp], [centring sign],
-//                     forward row FFT -> work buffer; maxima for the update norms
-//   B  column pass  : forward column FFT, I_est = sum_k |Psi_k|^2, FP64 partial of
-//                     sum |I_meas - I_est|, Psi_k *= sqrt(I_meas/(I_est+1e-10)),
-//                     inverse column FFT (BaseEngine.py:870-1012)
-//   C  row pass     : inverse row FFT, [sign], [conj chirp] -> eswUpdate; DELTA;
-//                     object patch and probe updates; scatter object rows
+// Data moves between the passes through distributed shared memory: a row
+// pass writes each transformed row straight into the shared-memory column
+// block of the CTA that owns those columns, and a column pass writes back into
+// the row owners' row buffers, so the 2D transpose never touches L2.  The
+// norm maxima are reduced with cluster-scope atomics into rank 0's shared
+// memory, and each position's measured intensities are prefetched one
+// position ahead with cp.async into a double buffer.
 //
-// ASP adds a transfer-function column pass on each side of a real-space
-// projection row pass (Operators.py:155-230).  CTA c of the cluster owns rows
-// [c*L, (c+1)*L) of every row pass and Fourier-layout columns [c*L, (c+1)*L) of
-// every column pass (L = Np/C), so each CTA always updates the same probe rows:
-// the probe stays in shared memory for the whole launch.
+// Work is split into warp tasks, one 1D transform of one mode each, so a CTA
+// runs K*L independent transforms per pass (K = nosm*npsm); everything that
+// couples modes (the estimated intensity, the object step's sum over probe
+// modes, the probe step's sum over object modes) is done afterwards by a
+// pixel loop over shared memory in a fixed order, so results are deterministic.
+//
+//   A  stage the object patch rows; maxima of the update norms; tasks: exit
+//      wave O_o*P_p [*chirp][*sign], forward row FFT -> work buffer
+//   B  stage the CTA's column block; tasks: forward column FFT; pixels:
+//      I_est, FP64 error partial, frac = sqrt(I_meas/(I_est+1e-10)); tasks:
+//      * frac / Np^2, inverse column FFT; write back
+//   C  tasks: inverse row FFT, [sign], [conj chirp], DELTA = eswUpdate - esw;
+//      pixels: object and probe steps (qNewton: whole-object max first)
+// ASP replaces B by transfer-function column passes around a real-space
+// projection row pass (Operators.py:155-230).
 #include <cooperative_groups.h>
 
 #include "ptyg_common.cuh"
@@ -29,6 +41,20 @@
 namespace cg = cooperative_groups;
 
 namespace ptyg {
+
+// Address of `local` in the shared memory of cluster rank `rank`.
+template <class T>
+PTYG_DEV T* dsmem(T* local, int rank) {
+  return cg::this_cluster().map_shared_rank(local, (unsigned)rank);
+}
+
+PTYG_DEV void cp_async16(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+PTYG_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+PTYG_DEV void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+PTYG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 PTYG_DEV void cluster_sync(int C) {
   if (C > 1) {
@@ -53,8 +79,9 @@ PTYG_DEV double warp_sum(double v) {
   return v;
 }
 
-// Max-reduce NV values over the CTA and fold them into the cluster slots with
-// one atomicMax per value per CTA.  `scratch` holds 32*NV floats.
+// Max-reduce NV values over the CTA and fold them into the cluster slots (rank
+// 0's shared memory) with one cluster-scope atomicMax per value per CTA
+// (non-negative floats order like their bits).
 template <int NV>
 PTYG_DEV void block_max_to_slots(float (&v)[NV], float* scratch, unsigned* slots, const int* idx) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -71,7 +98,7 @@ PTYG_DEV void block_max_to_slots(float (&v)[NV], float* scratch, unsigned* slots
   }
 }
 
-// Sum a double over the CTA; thread 0 receives the result.
+// Sum over the CTA; thread 0 receives the result.
 PTYG_DEV double block_sum(double v, double* scratch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   v = warp_sum(v);
@@ -83,103 +110,140 @@ PTYG_DEV double block_sum(double v, double* scratch) {
   return t;
 }
 
-PTYG_DEV float slot_value(const unsigned* slots, int i) {
-  return __uint_as_float(__ldcg(slots + i));
+// max over one TILE x TILE object tile of sum_o |O_o|, this lane's share
+// (8 pixels per lane; the caller reduces across the warp).
+PTYG_DEV float tile_max(const ScanDev& s, int ty, int tx, int nosm, int No, size_t No2, int lane) {
+  float m = 0.f;
+#pragma unroll
+  for (int q = 0; q < TILE * TILE / 32; ++q) {
+    const int idx = q * 32 + lane;
+    const int y = ty * TILE + idx / TILE, x = tx * TILE + idx % TILE;
+    if (y < No && x < No) {
+      float sum = 0.f;
+      for (int o = 0; o < nosm; ++o) sum += cabs(ld_cg(s.object + o * No2 + (size_t)y * No + x));
+      m = fmaxf(m, sum);
+    }
+  }
+  return m;
 }
 
-// ------------------------------------------------------------------ passes
-// Column pass over the CTA's Fourier-layout columns.  MODE 0: intensity
-// projection (Fraunhofer/Fresnel); MODE 1: multiply by H (or conj(H)) / Np^2.
-template <int E, int MK, int MODE>
-PTYG_DEV double column_pass(const EngineArgs& a, const ScanDev& s, int frame, int crank, int L, int K,
-                            float2* tile, const float2* tw, const LaneTw& lt, const float2* H, bool conjH) {
+PTYG_DEV float slot_value(const unsigned* slots, int i) {
+  return __uint_as_float(*reinterpret_cast<const volatile unsigned*>(slots + i));
+}
+
+// Shared-memory layout of one CTA, in complex64 units.
+struct Smem {
+  float2* probe;    // npsm * L * NP, the CTA's probe rows (resident all launch)
+  float2* obj;      // nosm * L * NP, this position's object patch rows
+  float2* tile;     // K * NP * (L+1): the CTA's column block (written by every CTA)
+  float2* rows;     // K * L * NP: the CTA's rows, Fourier layout along x
+  float2* U;        // qNewton probe numerators, npsm * L * NP
+  float* fr;        // L * NP projection factors
+  float* dat;       // 2 x L * NP measured intensities (double buffer)
+  unsigned* slots;  // 2 * RED_BANK norm slots (used on rank 0)
+  double* redD;     // 32
+  float* redF;      // 4 * 32
+};
+
+__host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int nosm, int npsm, bool qn) {
+  const size_t LN = (size_t)L * NP;
+  return (size_t)npsm * LN + (size_t)nosm * LN + (size_t)K * NP * (L + 1) + (size_t)K * LN + (qn ? npsm * LN : 0);
+}
+
+// A row task's transformed row (Fourier layout: register r, lane l is slot
+// 32r + l) goes to the column blocks of the CTAs owning those slots.
+template <int E, int L>
+PTYG_DEV void scatter_row(const Smem& sm, const float2 (&v)[E], int k, int y) {
   constexpr int NP = 32 * E;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  constexpr int ld = L + 1;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    const int sx = 32 * r + lane;
+    const int owner = sx / L, c = sx - (sx / L) * L;
+    *dsmem(&sm.tile[(k * NP + y) * ld + c], owner) = v[r];
+  }
+}
+
+// A column task's result (natural order along y) goes back to the row buffers
+// of the CTAs owning those rows, at Fourier-layout slot sx.
+template <int E, int L>
+PTYG_DEV void scatter_column(const Smem& sm, const float2 (&v)[E], int k, int sx) {
+  constexpr int NP = 32 * E;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const int y = lane + 32 * j;
+    const int owner = y / L, ly = y - (y / L) * L;
+    *dsmem(&sm.rows[(k * L + ly) * NP + sx], owner) = v[j];
+  }
+}
+
+// Column pass that multiplies the spectrum by H (or conj H) / Np^2 between a
+// forward and an inverse column transform (ASP, Operators.py:155-230); the
+// result goes to the row owners' row buffers.
+template <int E, int L>
+PTYG_DEV void column_filter(const Smem& sm, const WarpFFT<E>& F, const float2* H, bool conjH, int crank, int K) {
+  constexpr int NP = 32 * E;
+  constexpr int ld = L + 1;
+  const int lane = threadIdx.x & 31;
   const int sx0 = crank * L;
-  const int ld = L + 1;
-  // stage the column block of every mode (rows of L contiguous complex64)
-  for (int idx = threadIdx.x; idx < K * NP * L; idx += blockDim.x) {
-    const int k = idx / (NP * L);
-    const int rem = idx - k * NP * L;
-    const int y = rem / L;
-    const int c = rem - y * L;
-    tile[(k * NP + y) * ld + c] = ld_cg(s.work + (size_t)k * NP * NP + (size_t)y * NP + sx0 + c);
-  }
-  __syncthreads();
   const float inv2 = 1.f / (float)(NP * NP);
-  double err = 0.0;
-  for (int c = warp; c < L; c += nw) {
-    const int sx = sx0 + c;
-    float2 v[MK][E];
+  fft_tasks<E, false>(
+      F, K * L,
+      [&](int t, float2(&v)[E]) {
+        const int k = t / L, c = t % L;
 #pragma unroll
-    for (int k = 0; k < MK; ++k) {
-      if (k < K) {
+        for (int j = 0; j < E; ++j) v[j] = sm.tile[(k * NP + lane + 32 * j) * ld + c];
+      },
+      [&](int t, float2(&v)[E]) {
+        const int k = t / L, c = t % L;
+        const float2* h = H + (size_t)(sx0 + c) * NP;
 #pragma unroll
-        for (int jj = 0; jj < E; ++jj) v[k][jj] = tile[(k * NP + lane + 32 * jj) * ld + c];
-        fft_fwd<E>(v[k], tw, lt, lane);
-      }
-    }
-    if (MODE == 0) {
-      const float* I = s.data + ((size_t)frame * NP + sx) * NP;
-      float* de = (a.writeDetErr && s.detErr) ? s.detErr + ((size_t)frame * NP + sx) * NP : nullptr;
-#pragma unroll
-      for (int r = 0; r < E; ++r) {
-        float ie = 0.f;
-#pragma unroll
-        for (int k = 0; k < MK; ++k)
-          if (k < K) ie += cabs2(v[k][r]);
-        ie *= inv2;
-        const float im = __ldg(I + r * 32 + lane);
-        const float d = fabsf(im - ie);
-        err += (double)d;
-        if (de) de[r * 32 + lane] = d;
-        const float f = sqrtf(im / (ie + 1e-10f)) * inv2;
-#pragma unroll
-        for (int k = 0; k < MK; ++k)
-          if (k < K) v[k][r] = cscale(v[k][r], f);
-      }
-    } else {
-      const float2* h = H + (size_t)sx * NP;
-#pragma unroll
-      for (int r = 0; r < E; ++r) {
-        float2 hv = __ldg(h + r * 32 + lane);
-        if (conjH) hv.y = -hv.y;
-        hv = cscale(hv, inv2);
-#pragma unroll
-        for (int k = 0; k < MK; ++k)
-          if (k < K) v[k][r] = cmul(v[k][r], hv);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < MK; ++k) {
-      if (k < K) {
-        fft_inv<E>(v[k], tw, lt, lane);
-#pragma unroll
-        for (int jj = 0; jj < E; ++jj) tile[(k * NP + lane + 32 * jj) * ld + c] = v[k][jj];
-      }
-    }
-  }
+        for (int r = 0; r < E; ++r) {
+          float2 hv = __ldg(h + r * 32 + lane);
+          if (conjH) hv.y = -hv.y;
+          sm.tile[(k * NP + 32 * r + lane) * ld + c] = cscale(cmul(v[r], hv), inv2);
+        }
+      });
   __syncthreads();
-  for (int idx = threadIdx.x; idx < K * NP * L; idx += blockDim.x) {
-    const int k = idx / (NP * L);
-    const int rem = idx - k * NP * L;
-    const int y = rem / L;
-    const int c = rem - y * L;
-    st_cg(s.work + (size_t)k * NP * NP + (size_t)y * NP + sx0 + c, tile[(k * NP + y) * ld + c]);
-  }
-  return err;
+  fft_tasks<E, true>(
+      F, K * L,
+      [&](int t, float2(&v)[E]) {
+        const int k = t / L, c = t % L;
+#pragma unroll
+        for (int r = 0; r < E; ++r) v[r] = sm.tile[(k * NP + 32 * r + lane) * ld + c];
+      },
+      [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm, v, t / L, sx0 + t % L); });
 }
 
 // ------------------------------------------------------------------ kernel
-template <int E, int MO, int MP>
-__global__ void __launch_bounds__(256, 1) engine_kernel(const EngineArgs a) {
+// Prefetch the measured intensities of order slot `it` (if it exists and is a
+// valid frame) into dat[it & 1]: the CTA's L*NP block is contiguous in both
+// layouts (Fourier [frame][sx][sy] columns sx0.., or natural rows line0..).
+template <int NP, int L>
+PTYG_DEV void prefetch_data(const EngineArgs& a, const ScanDev& s, const Smem& sm, int it, int blk0) {
+  if (it < a.count) {
+    const int frame = s.order[a.start + it];
+    if (frame >= 0 && frame < a.numFrames) {
+      const float* src = s.data + ((size_t)frame * NP + blk0) * NP;
+      float* dst = sm.dat + (it & 1) * L * NP;
+      for (int i = threadIdx.x; i < L * NP / 4; i += blockDim.x) cp_async16(dst + 4 * i, src + 4 * i);
+    }
+  }
+  cp_async_commit();
+}
+
+// E: Np / 32 points per lane; L: rows (and Fourier columns) per CTA, so the
+// cluster has C = Np / L CTAs.  Both compile-time so index arithmetic is shifts.
+template <int E, int L>
+__global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   constexpr int NP = 32 * E;
-  constexpr int MK = MO * MP;
-  const int C = a.cluster;
+  constexpr int C = NP / L;
+  constexpr int LN = L * NP, ld = L + 1;
   const int crank = (int)(blockIdx.x % (unsigned)C);
   const ScanDev s = a.scans[blockIdx.x / C];
-  const int L = NP / C;
-  const int line0 = crank * L;
+  const int line0 = crank * L, sx0 = crank * L;
   const unsigned lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int nosm = a.nosm, npsm = a.npsm, K = nosm * npsm, No = a.No;
@@ -187,409 +251,436 @@ __global__ void __launch_bounds__(256, 1) engine_kernel(const EngineArgs a) {
   const bool fresnel = a.prop == PROP_FRESNEL;
   const bool asp = a.prop == PROP_ASP;
   const int eng = a.engine;
+  const size_t No2 = (size_t)No * No;
+  const int blk0 = asp ? line0 : sx0;
 
   extern __shared__ float4 smem_f4[];
-  float2* tw = reinterpret_cast<float2*>(smem_f4);
-  float2* probeS = tw + NP;                     // npsm * L * NP
-  float2* tile = probeS + npsm * L * NP;         // K * NP * (L + 1)
-  float2* U = tile + K * NP * (L + 1);           // qNewton: npsm * L * NP
-  double* redD = reinterpret_cast<double*>(U + (eng == ENG_QNEWTON ? npsm * L * NP : 0));
-  float* redF = reinterpret_cast<float*>(redD + 32);
+  Smem sm;
+  sm.probe = reinterpret_cast<float2*>(smem_f4);
+  sm.obj = sm.probe + npsm * LN;
+  sm.tile = sm.obj + nosm * LN;
+  sm.rows = sm.tile + K * NP * ld;
+  sm.U = sm.rows + K * LN;
+  sm.fr = reinterpret_cast<float*>(sm.U + (eng == ENG_QNEWTON ? npsm * LN : 0));
+  sm.dat = sm.fr + LN;
+  sm.slots = reinterpret_cast<unsigned*>(sm.dat + 2 * LN);
+  sm.redD = reinterpret_cast<double*>(sm.slots + 2 * RED_BANK);
+  sm.redF = reinterpret_cast<float*>(sm.redD + 32);
+  unsigned* slots0 = dsmem(sm.slots, 0);
 
-  for (int i = threadIdx.x; i < NP; i += blockDim.x) tw[i] = a.twiddle[i];
-  for (int i = threadIdx.x; i < npsm * L * NP; i += blockDim.x) {
-    const int p = i / (L * NP);
-    const int rem = i - p * L * NP;
-    probeS[i] = s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem];
+  for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
+    const int p = i / LN, rem = i - (i / LN) * LN;
+    sm.probe[i] = s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem];
   }
-  if (crank == 0 && threadIdx.x < 2 * RED_BANK) s.red[threadIdx.x] = 0u;
+  if (threadIdx.x < 2 * RED_BANK) sm.slots[threadIdx.x] = 0u;
+  prefetch_data<NP, L>(a, s, sm, 0, blk0);
+  WarpFFT<E> F;
+  F.init(a.twiddle, lane);
+  if (eng == ENG_QNEWTON) {
+    // all tile maxima once per launch
+    const int nt = a.tilesPerRow * a.tilesPerRow;
+    for (int t = crank * nw + warp; t < nt; t += C * nw) {
+      const float v = warp_max(tile_max(s, t / a.tilesPerRow, t % a.tilesPerRow, nosm, No, No2, lane));
+      if (lane == 0) s.tileMax[t] = v;
+    }
+  }
   __syncthreads();
   cluster_sync(C);
-  const LaneTw lt = lane_twiddles<E>(tw, lane);
+
+  const float inv2 = 1.f / (float)(NP * NP);
 
   for (int it = 0; it < a.count; ++it) {
+    prefetch_data<NP, L>(a, s, sm, it + 1, blk0);
     const int frame = s.order[a.start + it];
-    const int row0 = s.positions[2 * frame];
-    const int col0 = s.positions[2 * frame + 1];
-    if (frame < 0 || frame >= a.numFrames || row0 < 0 || col0 < 0 || row0 > No - NP || col0 > No - NP) {
+    const int row0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame] : -1;
+    const int col0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame + 1] : -1;
+    if (row0 < 0 || col0 < 0 || row0 > No - NP || col0 > No - NP) {
       if (crank == 0 && threadIdx.x == 0) atomicCAS(s.status, 0, 2);
       continue;  // uniform across the cluster
     }
-    unsigned* red = s.red + (it & 1) * RED_BANK;
-    unsigned* redNext = s.red + ((it & 1) ^ 1) * RED_BANK;
+    unsigned* red = slots0 + (it & 1) * RED_BANK;
+    const float* dat = sm.dat + (it & 1) * LN;
 
-    // ---------------- A: exit waves and forward row FFT
+    // ---------------- A: stage the patch rows, norms, exit waves, row FFT
+    for (int i = threadIdx.x; i < nosm * LN; i += blockDim.x) {
+      const int o = i / LN, rem = i - (i / LN) * LN;
+      const int l = rem / NP, x = rem - (rem / NP) * NP;
+      sm.obj[i] = ld_cg(s.object + o * No2 + (size_t)(row0 + line0 + l) * No + col0 + x);
+    }
+    __syncthreads();
     {
       float mx[3] = {0.f, 0.f, 0.f};  // max of sum_p|P|^2, sum_o|O|^2, sum_p|P|
-      for (int l = warp; l < L; l += nw) {
-        const int y = line0 + l;
-        const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
-        float2 O[MO][E];
-#pragma unroll
-        for (int o = 0; o < MO; ++o) {
-          if (o < nosm) {
-            const float2* src = s.object + (size_t)o * No * No + (size_t)(row0 + y) * No + col0 + lane;
-#pragma unroll
-            for (int jj = 0; jj < E; ++jj) O[o][jj] = ld_cg(src + 32 * jj);
-          }
+      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+        float sp2 = 0.f, sp1 = 0.f, so2 = 0.f;
+        for (int p = 0; p < npsm; ++p) {
+          const float q = cabs2(sm.probe[p * LN + i]);
+          sp2 += q;
+          sp1 += sqrtf(q);
         }
-#pragma unroll
-        for (int jj = 0; jj < E; ++jj) {
-          float so2 = 0.f;
-#pragma unroll
-          for (int o = 0; o < MO; ++o)
-            if (o < nosm) so2 += cabs2(O[o][jj]);
-          mx[1] = fmaxf(mx[1], so2);
-        }
-        float sp2[E], sp1[E];
-#pragma unroll
-        for (int jj = 0; jj < E; ++jj) sp2[jj] = sp1[jj] = 0.f;
-#pragma unroll
-        for (int p = 0; p < MP; ++p) {
-          if (p < npsm) {
-            float2 P[E];
-#pragma unroll
-            for (int jj = 0; jj < E; ++jj) {
-              P[jj] = probeS[(p * L + l) * NP + lane + 32 * jj];
-              const float q = cabs2(P[jj]);
-              sp2[jj] += q;
-              sp1[jj] += sqrtf(q);
-            }
-#pragma unroll
-            for (int o = 0; o < MO; ++o) {
-              if (o < nosm) {
-                float2 v[E];
-#pragma unroll
-                for (int jj = 0; jj < E; ++jj) {
-                  float2 e = cmul(O[o][jj], P[jj]);
-                  if (fresnel) e = cmul(e, __ldg(a.fresnelQ + y * NP + lane + 32 * jj));
-                  v[jj] = cscale(e, sg);
-                }
-                fft_fwd<E>(v, tw, lt, lane);
-                float2* dst = s.work + (size_t)(o * npsm + p) * NP * NP + (size_t)y * NP + lane;
-#pragma unroll
-                for (int r = 0; r < E; ++r) st_cg(dst + 32 * r, v[r]);
-              }
-            }
-          }
-        }
-#pragma unroll
-        for (int jj = 0; jj < E; ++jj) {
-          mx[0] = fmaxf(mx[0], sp2[jj]);
-          mx[2] = fmaxf(mx[2], sp1[jj]);
-        }
+        for (int o = 0; o < nosm; ++o) so2 += cabs2(sm.obj[o * LN + i]);
+        mx[0] = fmaxf(mx[0], sp2);
+        mx[1] = fmaxf(mx[1], so2);
+        mx[2] = fmaxf(mx[2], sp1);
       }
       const int idx[3] = {RED_PMAX2, RED_OMAX2, RED_PMAX1};
-      block_max_to_slots<3>(mx, redF, red, idx);
+      block_max_to_slots<3>(mx, sm.redF, red, idx);
     }
+    fft_tasks<E, false>(
+        F, K * L,
+        [&](int t, float2(&v)[E]) {
+          const int k = t / L, l = t % L;
+          const int o = k / npsm, p = k - (k / npsm) * npsm;
+          const int y = line0 + l;
+          const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int x = lane + 32 * j;
+            float2 e = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[(p * L + l) * NP + x]);
+            if (fresnel) e = cmul(e, __ldg(a.fresnelQ + y * NP + x));
+            v[j] = cscale(e, sg);
+          }
+        },
+        [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm, v, t / L, line0 + t % L); });
+    cp_async_wait_prev();  // this position's intensities
     cluster_sync(C);
 
     double err = 0.0;
     if (!asp) {
-      // ---------------- B: Fourier-plane intensity projection
-      err = column_pass<E, MK, 0>(a, s, frame, crank, L, K, tile, tw, lt, nullptr, false);
-    } else {
-      // ---------------- ASP: B (xH), C (real-space projection), D (x conj H)
-      column_pass<E, MK, 1>(a, s, frame, crank, L, K, tile, tw, lt, a.aspH, false);
-      cluster_sync(C);
-      for (int l = warp; l < L; l += nw) {
-        const int y = line0 + l;
-        float2 v[MK][E];
+      // ---------------- B: Fourier-plane intensity projection (BaseEngine.py:870-1012)
+      fft_tasks<E, false>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+            const int k = t / L, c = t % L;
 #pragma unroll
-        for (int k = 0; k < MK; ++k) {
-          if (k < K) {
-            const float2* src = s.work + (size_t)k * NP * NP + (size_t)y * NP + lane;
+            for (int j = 0; j < E; ++j) v[j] = sm.tile[(k * NP + lane + 32 * j) * ld + c];
+          },
+          [&](int t, float2(&v)[E]) {
+            const int k = t / L, c = t % L;
 #pragma unroll
-            for (int r = 0; r < E; ++r) v[k][r] = ld_cg(src + 32 * r);
-            fft_inv<E>(v[k], tw, lt, lane);
-          }
-        }
-        const float* I = s.data + ((size_t)frame * NP + y) * NP + lane;
-        float* de = (a.writeDetErr && s.detErr) ? s.detErr + ((size_t)frame * NP + y) * NP + lane : nullptr;
-#pragma unroll
-        for (int jj = 0; jj < E; ++jj) {
+            for (int r = 0; r < E; ++r) sm.tile[(k * NP + 32 * r + lane) * ld + c] = v[r];
+          });
+      __syncthreads();
+      {
+        float e = 0.f;
+        const bool det = a.writeDetErr && s.detErr;
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          const int c = i / NP, sy = i - (i / NP) * NP;
           float ie = 0.f;
-#pragma unroll
-          for (int k = 0; k < MK; ++k)
-            if (k < K) ie += cabs2(v[k][jj]);
-          const float im = __ldg(I + 32 * jj);
+          for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[(k * NP + sy) * ld + c]);
+          ie *= inv2;
+          const float im = dat[i];
           const float d = fabsf(im - ie);
-          err += (double)d;
-          if (de) de[32 * jj] = d;
-          const float f = sqrtf(im / (ie + 1e-10f));
-#pragma unroll
-          for (int k = 0; k < MK; ++k)
-            if (k < K) v[k][jj] = cscale(v[k][jj], f);
+          e += d;
+          if (det) s.detErr[((size_t)frame * NP + sx0) * NP + i] = d;
+          sm.fr[i] = sqrtf(im / (ie + 1e-10f)) * inv2;
         }
-#pragma unroll
-        for (int k = 0; k < MK; ++k) {
-          if (k < K) {
-            fft_fwd<E>(v[k], tw, lt, lane);
-            float2* dst = s.work + (size_t)k * NP * NP + (size_t)y * NP + lane;
-#pragma unroll
-            for (int r = 0; r < E; ++r) st_cg(dst + 32 * r, v[k][r]);
-          }
-        }
+        err = (double)e;
       }
       __syncthreads();
+      fft_tasks<E, true>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+            const int k = t / L, c = t % L;
+#pragma unroll
+            for (int r = 0; r < E; ++r)
+              v[r] = cscale(sm.tile[(k * NP + 32 * r + lane) * ld + c], sm.fr[c * NP + 32 * r + lane]);
+          },
+          [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm, v, t / L, sx0 + t % L); });
+    } else {
+      // ---------------- ASP: x H, real-space projection, x conj(H)
+      column_filter<E, L>(sm, F, a.aspH, false, crank, K);
       cluster_sync(C);
-      column_pass<E, MK, 1>(a, s, frame, crank, L, K, tile, tw, lt, a.aspH, true);
+      fft_tasks<E, true>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+            const float2* row = sm.rows + t * NP;
+#pragma unroll
+            for (int r = 0; r < E; ++r) v[r] = row[32 * r + lane];
+          },
+          [&](int t, float2(&v)[E]) {
+            float2* row = sm.rows + t * NP;
+#pragma unroll
+            for (int j = 0; j < E; ++j) row[lane + 32 * j] = v[j];
+          });
+      __syncthreads();
+      {
+        float e = 0.f;
+        const bool det = a.writeDetErr && s.detErr;
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          float ie = 0.f;
+          for (int k = 0; k < K; ++k) ie += cabs2(sm.rows[k * LN + i]);
+          const float im = dat[i];
+          const float d = fabsf(im - ie);
+          e += d;
+          if (det) s.detErr[((size_t)frame * NP + line0) * NP + i] = d;
+          sm.fr[i] = sqrtf(im / (ie + 1e-10f));
+        }
+        err = (double)e;
+      }
+      __syncthreads();
+      fft_tasks<E, false>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+            const int l = t % L;
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              const int x = lane + 32 * j;
+              v[j] = cscale(sm.rows[t * NP + x], sm.fr[l * NP + x]);
+            }
+          },
+          [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm, v, t / L, line0 + t % L); });
+      cluster_sync(C);
+      column_filter<E, L>(sm, F, a.aspH, true, crank, K);
     }
     {
-      const double t = block_sum(err, redD);
+      const double t = block_sum(err, sm.redD);
       if (threadIdx.x == 0) s.errPart[(size_t)frame * C + crank] = t;
     }
-    if (crank == 0 && threadIdx.x < RED_BANK) redNext[threadIdx.x] = 0u;
+    if (crank == 0 && threadIdx.x < RED_BANK) sm.slots[((it & 1) ^ 1) * RED_BANK + threadIdx.x] = 0u;
     cluster_sync(C);
 
-    // ---------------- C: inverse row FFT, DELTA, object and probe updates
-    // Streams over probe modes: for each p the lines of all object modes are
-    // inverse transformed, DELTA_{o,p} formed, the object numerator accumulated
-    // and probe mode p updated, so only one probe mode is live at a time.
+    // ---------------- C: inverse row FFT and DELTA per mode
+    fft_tasks<E, true>(
+        F, K * L,
+        [&](int t, float2(&v)[E]) {
+          const float2* row = sm.rows + t * NP;
+#pragma unroll
+          for (int r = 0; r < E; ++r) v[r] = row[32 * r + lane];
+        },
+        [&](int t, float2(&v)[E]) {
+          const int k = t / L, l = t % L;
+          const int o = k / npsm, p = k - (k / npsm) * npsm;
+          const int y = line0 + l;
+          const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
+          float2* row = sm.rows + t * NP;
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int x = lane + 32 * j;
+            float2 u = cscale(v[j], sg);
+            if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + x), u);
+            const float2 esw = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[(p * L + l) * NP + x]);
+            row[x] = csub(u, esw);
+          }
+        });
+    __syncthreads();
+
+    // ---------------- C: object and probe steps, pixel by pixel
     {
       const float pmax2 = slot_value(red, RED_PMAX2);
       const float omax2 = slot_value(red, RED_OMAX2);
       const float pmax1 = slot_value(red, RED_PMAX1);
       const float invPmax2 = 1.f / pmax2, invOmax2 = 1.f / omax2, invPmax1 = 1.f / pmax1;
       const float stepP = a.betaP * a.weightP;
-      for (int l = warp; l < L; l += nw) {
-        const int y = line0 + l;
-        const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
-        float2 O[MO][E], accO[MO][E];
-        float gP[MO][E];
+      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+        float2 O[MAX_OBJECT_MODES], accO[MAX_OBJECT_MODES];
+        float gP[MAX_OBJECT_MODES];
 #pragma unroll
-        for (int o = 0; o < MO; ++o) {
+        for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
           if (o < nosm) {
-            const float2* src = s.object + (size_t)o * No * No + (size_t)(row0 + y) * No + col0 + lane;
-#pragma unroll
-            for (int jj = 0; jj < E; ++jj) {
-              O[o][jj] = ld_cg(src + 32 * jj);
-              accO[o][jj] = make_float2(0.f, 0.f);
-              const float q = cabs2(O[o][jj]);
-              if (eng == ENG_EPIE)
-                gP[o][jj] = invOmax2;                                    // ePIE.py:154-156
-              else if (eng == ENG_MPIE)
-                gP[o][jj] = 1.f / (a.alphaP * omax2 + (1.f - a.alphaP) * q);  // mPIE.py:262-264
-              else
-                gP[o][jj] = sqrtf(q) / (q + a.regP);  // qNewton.py:131-136 (1/Omax applied later)
-            }
+            O[o] = sm.obj[o * LN + i];
+            accO[o] = make_float2(0.f, 0.f);
+            const float q = cabs2(O[o]);
+            if (eng == ENG_EPIE)
+              gP[o] = invOmax2;  // ePIE.py:154-156
+            else if (eng == ENG_MPIE)
+              gP[o] = 1.f / (a.alphaP * omax2 + (1.f - a.alphaP) * q);  // mPIE.py:262-264
+            else
+              gP[o] = sqrtf(q) / (q + a.regP);  // qNewton.py:131-136 (1/Omax applied later)
           }
         }
+        for (int p = 0; p < npsm; ++p) {
+          const float2 P = sm.probe[p * LN + i];
+          const float q = cabs2(P);
+          float gO;
+          if (eng == ENG_EPIE) {
+            gO = invPmax2;  // ePIE.py:138-140
+          } else if (eng == ENG_MPIE) {
+            gO = 1.f / (a.alphaO * pmax2 + (1.f - a.alphaO) * q);  // mPIE.py:246-248
+            if (a.fpm) gO *= sqrtf(q) * invPmax2;                    // mPIE.py:237-243
+          } else {
+            gO = sqrtf(q) * invPmax1 / (q + a.regO);  // qNewton.py:113-119
+          }
+          float2 accP = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int p = 0; p < MP; ++p) {
-          if (p < npsm) {
-            float2 D[MO][E];
-#pragma unroll
-            for (int o = 0; o < MO; ++o) {
-              if (o < nosm) {
-                const float2* src = s.work + (size_t)(o * npsm + p) * NP * NP + (size_t)y * NP + lane;
-#pragma unroll
-                for (int r = 0; r < E; ++r) D[o][r] = ld_cg(src + 32 * r);
-                fft_inv<E>(D[o], tw, lt, lane);
-              }
-            }
-            float2* prow = (eng == ENG_QNEWTON ? U : probeS) + (p * L + l) * NP + lane;
-#pragma unroll
-            for (int jj = 0; jj < E; ++jj) {
-              const float2 P = probeS[(p * L + l) * NP + lane + 32 * jj];
-              const float q = cabs2(P);
-              float gO;
-              if (eng == ENG_EPIE) {
-                gO = invPmax2;  // ePIE.py:138-140
-              } else if (eng == ENG_MPIE) {
-                gO = 1.f / (a.alphaO * pmax2 + (1.f - a.alphaO) * q);  // mPIE.py:246-248
-                if (a.fpm) gO *= sqrtf(q) * invPmax2;                    // mPIE.py:237-243
-              } else {
-                gO = sqrtf(q) * invPmax1 / (q + a.regO);  // qNewton.py:113-119
-              }
-              float2 accP = make_float2(0.f, 0.f);
-#pragma unroll
-              for (int o = 0; o < MO; ++o) {
-                if (o < nosm) {
-                  float2 u = cscale(D[o][jj], sg);
-                  if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + lane + 32 * jj), u);
-                  const float2 d = csub(u, cmul(O[o][jj], P));  // DELTA = eswUpdate - esw
-                  accO[o][jj] = cadd(accO[o][jj], cscale(cmulc(P, d), gO));
-                  accP = cadd(accP, cscale(cmulc(O[o][jj], d), gP[o][jj]));
-                }
-              }
-              // qNewton keeps the numerator until the whole-object maximum is known
-              prow[32 * jj] = (eng == ENG_QNEWTON) ? accP : cadd(P, cscale(accP, stepP));
+          for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
+            if (o < nosm) {
+              const float2 d = sm.rows[(o * npsm + p) * LN + i];
+              accO[o] = cadd(accO[o], cscale(cmulc(P, d), gO));
+              accP = cadd(accP, cscale(cmulc(O[o], d), gP[o]));
             }
           }
+          if (eng == ENG_QNEWTON)
+            sm.U[p * LN + i] = accP;
+          else
+            sm.probe[p * LN + i] = cadd(P, cscale(accP, stepP));
         }
+        const int l = i / NP, x = i - (i / NP) * NP;
 #pragma unroll
-        for (int o = 0; o < MO; ++o) {
-          if (o < nosm) {
-            float2* dst = s.object + (size_t)o * No * No + (size_t)(row0 + y) * No + col0 + lane;
-#pragma unroll
-            for (int jj = 0; jj < E; ++jj) st_cg(dst + 32 * jj, cadd(O[o][jj], cscale(accO[o][jj], a.betaO)));
-          }
-        }
+        for (int o = 0; o < MAX_OBJECT_MODES; ++o)
+          if (o < nosm)
+            st_cg(s.object + o * No2 + (size_t)(row0 + line0 + l) * No + col0 + x,
+                  cadd(O[o], cscale(accO[o], a.betaO)));
       }
     }
 
     if (eng == ENG_QNEWTON) {
-      // whole-object max of sum_o |O_o| after the object update (qNewton.py:130)
+      // max over the whole object of sum_o |O_o| after the object step
+      // (qNewton.py:130), kept exactly with per-tile maxima: only the tiles
+      // the patch touched are recomputed, the others are read back.
       cluster_sync(C);
+      const int ty0 = row0 / TILE, ty1 = (row0 + NP - 1) / TILE;
+      const int tx0 = col0 / TILE, tx1 = (col0 + NP - 1) / TILE;
+      const int tw = tx1 - tx0 + 1, nPatchTiles = (ty1 - ty0 + 1) * tw;
       float m[1] = {0.f};
-      const size_t n2 = (size_t)No * No;
-      for (size_t i = (size_t)crank * blockDim.x + threadIdx.x; i < n2; i += (size_t)C * blockDim.x) {
-        float sum = 0.f;
-        for (int o = 0; o < nosm; ++o) sum += cabs(ld_cg(s.object + o * n2 + i));
-        m[0] = fmaxf(m[0], sum);
+      for (int t = crank * nw + warp; t < nPatchTiles; t += C * nw) {
+        const int ty = ty0 + t / tw, tx = tx0 + t % tw;
+        const float v = warp_max(tile_max(s, ty, tx, nosm, No, No2, lane));
+        m[0] = fmaxf(m[0], v);
+        if (lane == 0) s.tileMax[ty * a.tilesPerRow + tx] = v;
+      }
+      const int nt = a.tilesPerRow * a.tilesPerRow;
+      for (int t = crank * blockDim.x + threadIdx.x; t < nt; t += C * blockDim.x) {
+        const int ty = t / a.tilesPerRow, tx = t % a.tilesPerRow;
+        if (ty < ty0 || ty > ty1 || tx < tx0 || tx > tx1) m[0] = fmaxf(m[0], __ldcg(s.tileMax + t));
       }
       const int idx[1] = {RED_OMAXW};
-      block_max_to_slots<1>(m, redF, red, idx);
+      block_max_to_slots<1>(m, sm.redF, red, idx);
       cluster_sync(C);
       const float scale = a.betaP / slot_value(red, RED_OMAXW);
-      for (int i = threadIdx.x; i < npsm * L * NP; i += blockDim.x)
-        probeS[i] = cadd(probeS[i], cscale(U[i], scale));
+      for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) sm.probe[i] = cadd(sm.probe[i], cscale(sm.U[i], scale));
     }
 
     if (eng == ENG_MPIE && s.momentum && s.momentum[a.start + it]) {
-      // momentum step on the whole object and probe (mPIE.py:196-224), FP64 arithmetic
+      // momentum step on the whole object and probe (mPIE.py:196-224), in the
+      // reference's complex64 arithmetic and rounding order (no fused multiply-add):
+      //   M <- (buffer - X) + friction*M ;  X <- X - feedback*M ;  buffer <- X
       cluster_sync(C);
-      const double eta = a.frictionM, nu = a.feedbackM;
-      const size_t nobj = (size_t)nosm * No * No;
+      const float eta = a.frictionM, nu = a.feedbackM;
+      auto step = [&](float2 X, float2 B, float2 M, float2& Xn, float2& Mn) {
+        Mn = make_float2(__fadd_rn(__fsub_rn(B.x, X.x), __fmul_rn(eta, M.x)),
+                         __fadd_rn(__fsub_rn(B.y, X.y), __fmul_rn(eta, M.y)));
+        Xn = make_float2(__fsub_rn(X.x, __fmul_rn(nu, Mn.x)), __fsub_rn(X.y, __fmul_rn(nu, Mn.y)));
+      };
+      const size_t nobj = (size_t)nosm * No2;
       for (size_t i = (size_t)crank * blockDim.x + threadIdx.x; i < nobj; i += (size_t)C * blockDim.x) {
-        const float2 X = ld_cg(s.object + i), B = ld_cg(s.objectBuffer + i), M = ld_cg(s.objectMomentum + i);
-        const double mx = ((double)B.x - X.x) + eta * M.x, my = ((double)B.y - X.y) + eta * M.y;
-        const float2 Mn = make_float2((float)mx, (float)my);
-        const float2 Xn = make_float2((float)(X.x - nu * (double)Mn.x), (float)(X.y - nu * (double)Mn.y));
+        float2 Xn, Mn;
+        step(ld_cg(s.object + i), ld_cg(s.objectBuffer + i), ld_cg(s.objectMomentum + i), Xn, Mn);
         st_cg(s.objectMomentum + i, Mn);
         st_cg(s.object + i, Xn);
         st_cg(s.objectBuffer + i, Xn);
       }
-      for (int i = threadIdx.x; i < npsm * L * NP; i += blockDim.x) {
-        const int p = i / (L * NP);
-        const int rem = i - p * L * NP;
+      for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
+        const int p = i / LN, rem = i - (i / LN) * LN;
         const size_t gi = (size_t)p * NP * NP + (size_t)line0 * NP + rem;
-        const float2 X = probeS[i], B = s.probeBuffer[gi], M = s.probeMomentum[gi];
-        const double mx = ((double)B.x - X.x) + eta * M.x, my = ((double)B.y - X.y) + eta * M.y;
-        const float2 Mn = make_float2((float)mx, (float)my);
-        const float2 Xn = make_float2((float)(X.x - nu * (double)Mn.x), (float)(X.y - nu * (double)Mn.y));
+        float2 Xn, Mn;
+        step(sm.probe[i], s.probeBuffer[gi], s.probeMomentum[gi], Xn, Mn);
         s.probeMomentum[gi] = Mn;
         s.probeBuffer[gi] = Xn;
-        probeS[i] = Xn;
+        sm.probe[i] = Xn;
       }
     }
     __syncthreads();
     cluster_sync(C);
   }
+  cp_async_wait_all();
+  __syncthreads();
 
-  // write the probe rows back
-  for (int i = threadIdx.x; i < npsm * L * NP; i += blockDim.x) {
-    const int p = i / (L * NP);
-    const int rem = i - p * L * NP;
-    s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem] = probeS[i];
+  for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
+    const int p = i / LN, rem = i - (i / LN) * LN;
+    s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem] = sm.probe[i];
   }
+  // no CTA may exit while another can still write into its shared memory
+  cluster_sync(C);
 }
 
 // ------------------------------------------------------------------ launcher
 size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine) {
   const int L = Np / C;
-  const int K = nosm * npsm;
-  size_t n = (size_t)Np + (size_t)npsm * L * Np + (size_t)K * Np * (L + 1);
-  if (engine == ENG_QNEWTON) n += (size_t)npsm * L * Np;
-  return n * sizeof(float2) + 32 * sizeof(double) + 32 * 4 * sizeof(float) + 64;
+  const size_t LN = (size_t)L * Np;
+  const size_t n = smem_complex_elems(Np, L, nosm * npsm, nosm, npsm, engine == ENG_QNEWTON);
+  return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
+         4 * 32 * sizeof(float) + 64;
 }
 
-template <int E, int MO, int MP>
-static cudaError_t launch_t(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
-  auto kern = engine_kernel<E, MO, MP>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  if (a.cluster > 8) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-  }
+static cudaLaunchConfig_t launch_config(int cluster, int grid, int threads, size_t smem, cudaStream_t st,
+                                        cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(nscans * a.cluster);
+  cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(threads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = a.cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, a);
-}
-
-template <int E>
-static cudaError_t launch_e(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
-  if (a.nosm == 1 && a.npsm == 1) return launch_t<E, 1, 1>(a, nscans, threads, smem, st);
-  if (a.nosm == 1 && a.npsm <= 2) return launch_t<E, 1, 2>(a, nscans, threads, smem, st);
-  if (a.nosm == 1 && a.npsm <= 4) return launch_t<E, 1, 4>(a, nscans, threads, smem, st);
-  if constexpr (E <= 4) {
-    if (a.nosm <= 2 && a.npsm <= 4) return launch_t<E, 2, 4>(a, nscans, threads, smem, st);
-  }
-  return cudaErrorNotSupported;
-}
-
-template <int E, int MO, int MP>
-static cudaError_t clusters_t(int cluster, int threads, size_t smem, int* out) {
-  auto kern = engine_kernel<E, MO, MP>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  if (cluster > 8) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-  }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cluster);
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = smem;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = cluster;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaOccupancyMaxActiveClusters(out, (void*)kern, &cfg);
+  return cfg;
 }
 
-template <int E>
-static cudaError_t clusters_e(int nosm, int npsm, int cluster, int threads, size_t smem, int* out) {
-  if (nosm == 1 && npsm == 1) return clusters_t<E, 1, 1>(cluster, threads, smem, out);
-  if (nosm == 1 && npsm <= 2) return clusters_t<E, 1, 2>(cluster, threads, smem, out);
-  if (nosm == 1 && npsm <= 4) return clusters_t<E, 1, 4>(cluster, threads, smem, out);
-  if constexpr (E <= 4) {
-    if (nosm <= 2 && npsm <= 4) return clusters_t<E, 2, 4>(cluster, threads, smem, out);
-  }
+template <int E, int L>
+static cudaError_t prepare_t(size_t smem) {
+  auto kern = engine_kernel<E, L>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (32 * E / L > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+template <int E, int L>
+static cudaError_t launch_t(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
+  cudaError_t e = prepare_t<E, L>(smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = launch_config(a.cluster, nscans * a.cluster, threads, smem, st, attr);
+  return cudaLaunchKernelEx(&cfg, engine_kernel<E, L>, a);
+}
+
+template <int E, int L>
+static cudaError_t clusters_t(int threads, size_t smem, int* out) {
+  cudaError_t e = prepare_t<E, L>(smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = launch_config(32 * E / L, 32 * E / L, threads, smem, 0, attr);
+  return cudaOccupancyMaxActiveClusters(out, (void*)engine_kernel<E, L>, &cfg);
+}
+
+// Instantiated shapes: 8 or 16 rows per CTA, at most 16 CTAs per cluster.
+#define PTYG_ENGINE_SHAPES(X) X(1, 8) X(1, 16) X(2, 8) X(2, 16) X(4, 8) X(4, 16) X(8, 16)
+
+bool engine_shape_supported(int Np, int cluster) {
+  const int E = Np / 32, L = Np / cluster;
+#define PTYG_MATCH(e, l) \
+  if (E == e && L == l) return true;
+  PTYG_ENGINE_SHAPES(PTYG_MATCH)
+#undef PTYG_MATCH
+  return false;
+}
+
+cudaError_t engine_max_clusters(int Np, int nosm, int npsm, int cluster, int threads, size_t smem, int* out) {
+  (void)nosm;
+  (void)npsm;
+  *out = 0;
+  const int E = Np / 32, L = Np / cluster;
+#define PTYG_CALL(e, l) \
+  if (E == e && L == l) return clusters_t<e, l>(threads, smem, out);
+  PTYG_ENGINE_SHAPES(PTYG_CALL)
+#undef PTYG_CALL
   return cudaErrorNotSupported;
 }
 
-// How many clusters of this shape can be resident at once (0 = cannot launch).
-cudaError_t engine_max_clusters(int Np, int nosm, int npsm, int cluster, int threads, size_t smem, int* out) {
-  *out = 0;
-  switch (Np) {
-    case 32: return clusters_e<1>(nosm, npsm, cluster, threads, smem, out);
-    case 64: return clusters_e<2>(nosm, npsm, cluster, threads, smem, out);
-    case 128: return clusters_e<4>(nosm, npsm, cluster, threads, smem, out);
-    case 256: return clusters_e<8>(nosm, npsm, cluster, threads, smem, out);
-    default: return cudaErrorNotSupported;
-  }
-}
-
-// Returns cudaErrorNotSupported for mode counts without an instantiation.
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
-  switch (a.Np) {
-    case 32: return launch_e<1>(a, nscans, threads, smem, st);
-    case 64: return launch_e<2>(a, nscans, threads, smem, st);
-    case 128: return launch_e<4>(a, nscans, threads, smem, st);
-    case 256: return launch_e<8>(a, nscans, threads, smem, st);
-    default: return cudaErrorNotSupported;
-  }
+  const int E = a.Np / 32, L = a.Np / a.cluster;
+#define PTYG_CALL(e, l) \
+  if (E == e && L == l) return launch_t<e, l>(a, nscans, threads, smem, st);
+  PTYG_ENGINE_SHAPES(PTYG_CALL)
+#undef PTYG_CALL
+  return cudaErrorNotSupported;
 }
 
 bool engine_modes_supported(int Np, int nosm, int npsm) {
-  if (nosm == 1 && npsm <= 4) return true;
-  return nosm <= 2 && npsm <= 4 && Np <= 128;
+  (void)Np;
+  return nosm >= 1 && nosm <= MAX_OBJECT_MODES && npsm >= 1 && npsm <= 16;
 }
 
 }  // namespace ptyg

@@ -7,6 +7,9 @@
 namespace ptyg {
 
 enum Engine { ENG_EPIE = 0, ENG_MPIE = 1, ENG_QNEWTON = 2, ENG_E3PIE = 3 };
+
+// Object modes the pixel-update loop carries in registers.
+constexpr int MAX_OBJECT_MODES = 4;
 enum Propagator { PROP_FRAUNHOFER = 0, PROP_FRESNEL = 1, PROP_ASP = 2 };
 
 // Reduction slots (unsigned bit patterns of non-negative floats, max-reduced
@@ -40,7 +43,11 @@ struct ScanDev {
   float* detErr;           // optional [frame][Np*Np] |I_meas - I_est| (data layout)
   unsigned* red;           // 2 * RED_BANK reduction slots
   int* status;             // 0 = ok, else first error code seen
+  float* tileMax;          // qNewton: max of sum_o |O_o| per TILE x TILE object tile
 };
+
+// Side of the object tiles whose maxima qNewton keeps up to date.
+constexpr int TILE = 16;
 
 struct EngineArgs {
   const ScanDev* scans;
@@ -53,6 +60,7 @@ struct EngineArgs {
   int start, count;
   int writeDetErr;
   int cluster;
+  int tilesPerRow;         // ceil(No / TILE)
   float betaO, betaP, alphaO, alphaP, regO, regP, frictionM, feedbackM, weightP, bethSlice;
 };
 

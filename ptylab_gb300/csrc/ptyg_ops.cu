@@ -29,14 +29,13 @@ PTYG_DEV void natural_to_fourier(float2 (&v)[E], float2* buf, unsigned lane) {
 
 // Natural-order 1D transform of one line held by a warp.
 template <int E>
-PTYG_DEV void line_fft(float2 (&v)[E], bool inverse, const float2* tw, const LaneTw& lt, float2* buf,
-                       unsigned lane) {
+PTYG_DEV void line_fft(float2 (&v)[E], bool inverse, const WarpFFT<E>& F, float2* buf, unsigned lane) {
   if (!inverse) {
-    fft_fwd<E>(v, tw, lt, lane);
+    F.fwd(v);
     fourier_to_natural<E>(v, buf, lane);
   } else {
     natural_to_fourier<E>(v, buf, lane);
-    fft_inv<E>(v, tw, lt, lane);
+    F.inv(v);
   }
 }
 
@@ -51,7 +50,8 @@ __global__ void prop_row_kernel(const float2* __restrict__ in, float2* __restric
   __syncthreads();
   const unsigned lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const LaneTw lt = lane_twiddles<E>(tw, lane);
+  WarpFFT<E> F;
+  F.init(tw, lane);
   const long long line = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
   if (line >= (long long)batch * NP) return;
   const int y = (int)(line % NP);
@@ -68,7 +68,7 @@ __global__ void prop_row_kernel(const float2* __restrict__ in, float2* __restric
     }
     v[j] = cscale(x, sg);
   }
-  line_fft<E>(v, op.inverse != 0, tw, lt, wbuf + warp * NP, lane);
+  line_fft<E>(v, op.inverse != 0, F, wbuf + warp * NP, lane);
   float2* dst = out + line * NP;
 #pragma unroll
   for (int j = 0; j < E; ++j) {
@@ -110,13 +110,14 @@ __global__ void prop_col_kernel(const float2* in, float2* out, int batch, ColOp 
   __syncthreads();
   const unsigned lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const LaneTw lt = lane_twiddles<E>(tw, lane);
+  WarpFFT<E> F;
+  F.init(tw, lane);
   for (int c = warp; c < CB; c += nw) {
     const int x = c0 + c;
     float2 v[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = tile[(lane + 32 * j) * LD + c];
-    line_fft<E>(v, op.inverse1 != 0, tw, lt, wbuf + warp * NP, lane);
+    line_fft<E>(v, op.inverse1 != 0, F, wbuf + warp * NP, lane);
     if (op.filter) {
 #pragma unroll
       for (int j = 0; j < E; ++j) {
@@ -124,7 +125,7 @@ __global__ void prop_col_kernel(const float2* in, float2* out, int batch, ColOp 
         if (op.conjFilter) h.y = -h.y;
         v[j] = cmul(v[j], cscale(h, op.filterScale));
       }
-      line_fft<E>(v, op.inverse2 != 0, tw, lt, wbuf + warp * NP, lane);
+      line_fft<E>(v, op.inverse2 != 0, F, wbuf + warp * NP, lane);
     }
 #pragma unroll
     for (int j = 0; j < E; ++j) {

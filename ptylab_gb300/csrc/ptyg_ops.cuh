@@ -51,6 +51,7 @@ int set_last_error(int code, const char* msg);
 size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine);
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 bool engine_modes_supported(int Np, int nosm, int npsm);
+bool engine_shape_supported(int Np, int cluster);
 cudaError_t engine_max_clusters(int Np, int nosm, int npsm, int cluster, int threads, size_t smem, int* out);
 
 }  // namespace ptyg

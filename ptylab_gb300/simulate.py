@@ -123,3 +123,72 @@ def cpm_problem(spec: ScanSpec, engine_seed: int = 20240607):
     np.random.seed(engine_seed)
     rec.initializeObjectProbe()
     return d, p, rec, obj, probe
+
+
+@dataclass
+class FPMSpec:
+    """LED-array Fourier ptychography: grid x grid LEDs, low-res Np images of a
+    No x No high-resolution spectrum (the object's centred Fourier transform)."""
+
+    Np: int = 128
+    No: int = 512
+    grid: int = 15
+    pitch: float = 4e-3
+    zled: float = 80e-3
+    wavelength: float = 625e-9
+    dxd: float = 6.5e-6
+    magnification: float = 4.0
+    NA: float = 0.1
+    photons: float = 5e4
+    sigma_px: float = 4.0
+    seed: int = 20240607
+
+
+def simulate_fpm(spec: FPMSpec):
+    """Return (ptychogram float32, encoder metres, true object, pupil, dxp)."""
+    rng = np.random.default_rng(spec.seed)
+    Np, No = spec.Np, spec.No
+    dxp = spec.dxd / spec.magnification
+    c = (np.arange(spec.grid) - (spec.grid - 1) / 2) * spec.pitch
+    yy, xx = np.meshgrid(c, c, indexing="ij")
+    encoder = np.stack([yy.ravel(), xx.ravel()], axis=1)
+    amp = 0.5 + 0.5 * gaussian_random_field(rng, No, spec.sigma_px)
+    phase = np.pi * gaussian_random_field(rng, No, spec.sigma_px)
+    obj = amp * np.exp(1j * phase)
+    spectrum = np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(obj), norm="ortho"))
+    pupil_d = 2 * dxp**2 * Np * spec.NA / spec.wavelength
+    x = np.linspace(-Np / 2, Np / 2, Np) * dxp
+    X, Y = np.meshgrid(x, x)
+    pupil = (X**2 + Y**2) < (pupil_d / 2) ** 2
+    conv = -(1 / spec.wavelength) * dxp * Np
+    shift = np.round(conv * encoder / np.sqrt(encoder[:, 0] ** 2 + encoder[:, 1] ** 2 + spec.zled**2)[..., None])
+    pos = (shift + No // 2 - Np // 2).astype(int)
+    I = np.empty((len(pos), Np, Np), np.float64)
+    for j, (py, px) in enumerate(pos):
+        I[j] = np.abs(fft2c(spectrum[py : py + Np, px : px + Np] * pupil)) ** 2
+    I *= spec.photons / I.max()
+    I = rng.poisson(I).astype(np.float32)
+    return I, encoder, obj, pupil, dxp
+
+
+def fpm_problem(spec: FPMSpec, engine_seed: int = 20240607):
+    """ExperimentalData, Params and a Reconstruction (FPM: 'upsampled' object,
+    circular pupil) for `spec`, with PtyLab's FPM defaults ('NA' order,
+    probeBoundary, PtyLab/__init__.py:54-55)."""
+    I, encoder, obj, pupil, dxp = simulate_fpm(spec)
+    d = ExperimentalData(None, "FPM")
+    d.ptychogram = I
+    d.encoder = encoder
+    d.dxd = spec.dxd
+    d.zled = spec.zled
+    d.wavelength = spec.wavelength
+    d.magnification = spec.magnification
+    d.NA = spec.NA
+    d._setData()
+    p = Params()
+    p.positionOrder = "NA"
+    p.probeBoundary = True
+    rec = Reconstruction(d, p, No=spec.No)
+    np.random.seed(engine_seed)
+    rec.initializeObjectProbe()
+    return d, p, rec, obj, pupil
