@@ -11,7 +11,9 @@ intensities) stand in for measured scans.
 
 One step = one reconstruction iteration (every position once) over a batch
 of G independent scans, one thread-block cluster per scan, in one kernel
-launch; G is the number of clusters the GPU holds at once.  `value` is timed
+launch; G is the number of clusters the GPU holds at once in the library's
+throughput shape (16 rows per CTA).  `single_scan` times one scan alone in the
+latency shape (8 rows per CTA).  `value` is timed
 with CUDA events on the launching stream with all inputs resident in HBM; the
 batch streams G x 26 MB of intensities per step, more than L2 (129 MB), so no
 L2 flush is needed.  `e2e` runs the public API (ptylab_gb300.Engines.mPIE(...)
@@ -166,22 +168,22 @@ def run_gb300(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
 
-    def geometry(nscans):
+    def geometry(nscans, throughput):
         return _native.Geometry(Np=NP, No=NO, nosm=1, npsm=NPSM, nslice=1, num_frames=NPOS, num_scans=nscans,
                                 engine=_native.ENGINES["mPIE"], propagator=0, fftshift=0, fpm=0,
-                                cluster=args.cluster)
+                                cluster=args.cluster, throughput=throughput)
 
     probe_plan = C.c_void_p()
-    _native.check(lib.ptyg_plan_create(C.byref(geometry(1)), C.byref(probe_plan)))
+    _native.check(lib.ptyg_plan_create(C.byref(geometry(1, 1)), C.byref(probe_plan)))
     cl, th, sm, maxc = C.c_int(), C.c_int(), C.c_int(), C.c_int()
     _native.check(lib.ptyg_plan_info(probe_plan, C.byref(cl), C.byref(th), C.byref(sm), C.byref(maxc)))
     lib.ptyg_plan_destroy(probe_plan)
     G = args.scans if args.scans > 0 else max(1, maxc.value)
     iters = args.warmup + args.steps
 
-    def build_batch(nscans, seed0):
+    def build_batch(nscans, seed0, throughput):
         keep, plan = [], C.c_void_p()
-        _native.check(lib.ptyg_plan_create(C.byref(geometry(nscans)), C.byref(plan)))
+        _native.check(lib.ptyg_plan_create(C.byref(geometry(nscans, throughput)), C.byref(plan)))
         mom_total = 0
         flag_counts = np.zeros(iters, dtype=np.int64)
         for s in range(nscans):
@@ -226,7 +228,7 @@ def run_gb300(args, rank, world, local_rank):
         return e0.elapsed_time(e1) / 1e3
 
     # batched, device-resident: the headline
-    plan, keep, flag_counts = build_batch(G, 1000 * rank + 1)
+    plan, keep, flag_counts = build_batch(G, 1000 * rank + 1, 1)
     clocks = ClockSampler(local_rank)
     clocks.start()
     t = timed(plan, args.steps, args.warmup)
@@ -251,7 +253,7 @@ def run_gb300(args, rank, world, local_rank):
     out = {}
     if rank == 0:
         # one scan alone: latency view of the same kernel
-        plan1, keep1, _ = build_batch(1, 7)
+        plan1, keep1, _ = build_batch(1, 7, 0)
         t1 = timed(plan1, min(args.steps, 50), args.warmup)
         lib.ptyg_plan_destroy(plan1)
         del keep1

@@ -112,6 +112,9 @@ typedef struct ptyg_geometry {
   int32_t fftshift;    /* params.fftshiftSwitch: uncentred transforms, pre-shifted data */
   int32_t fpm;         /* operationMode == "FPM" (mPIE object step, mPIE.py:237-243) */
   int32_t cluster;     /* CTAs per scan (0 = choose) */
+  int32_t throughput;  /* 0: shortest time per position (8 rows per CTA);
+                          1: most positions per second over many scans (16
+                          rows per CTA: fewer CTAs per scan, more scans at once) */
 } ptyg_geometry;
 
 /* Engine scalars (ePIE.py:35-42, mPIE.py:233-245, qNewton.py:43-52,

@@ -51,6 +51,7 @@ class Geometry(C.Structure):
         ("fftshift", C.c_int32),
         ("fpm", C.c_int32),
         ("cluster", C.c_int32),
+        ("throughput", C.c_int32),
     ]
 
 

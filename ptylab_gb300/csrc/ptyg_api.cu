@@ -215,6 +215,7 @@ struct ptyg_plan {
   int device = 0;
   int C = 1;
   int threads = 256;
+  bool probeInSmem = true;
   size_t smem = 0;
   float2* fresnelQ = nullptr;
   float2* aspH = nullptr;
@@ -251,12 +252,14 @@ static int engine_threads(const ptyg_geometry& g, int C) {
   return 32 * w;
 }
 
-// Cluster sizes to try, best first: 8 rows per CTA (more CTAs, shorter
-// passes), then 16.  A requested size (geometry.cluster) goes first.
+// Cluster sizes to try, best first.  Latency: 8 rows per CTA (more CTAs,
+// shorter passes), then 16.  Throughput: 16 rows first (fewer CTAs per scan,
+// so more scans are resident at once).  A requested size goes first.
 static std::vector<int> cluster_candidates(const ptyg_geometry& g) {
   std::vector<int> c;
   if (g.cluster > 0) c.push_back(g.cluster);
-  for (int L : {8, 16}) {
+  const int order[2] = {g.throughput ? 16 : 8, g.throughput ? 8 : 16};
+  for (int L : order) {
     const int cc = g.Np / L;
     if (cc >= 1 && cc <= 16) c.push_back(cc);
   }
@@ -294,20 +297,24 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   bool found = false;
   for (int c : cluster_candidates(g)) {
     if (!ptyg::engine_shape_supported(g.Np, c)) continue;
-    p->C = c;
-    p->threads = engine_threads(g, c);
-    p->smem = ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.engine);
-    if ((int)p->smem > maxSmem) continue;
-    int nclusters = 0;
-    cudaError_t e = ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, c, p->threads, p->smem, &nclusters);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      continue;
+    for (bool psm : {true, false}) {
+      p->C = c;
+      p->probeInSmem = psm;
+      p->threads = engine_threads(g, c);
+      p->smem = ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.engine, psm);
+      if ((int)p->smem > maxSmem) continue;
+      int nclusters = 0;
+      cudaError_t e = ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, c, p->threads, p->smem, &nclusters);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      if (nclusters > 0) {
+        found = true;
+        break;
+      }
     }
-    if (nclusters > 0) {
-      found = true;
-      break;
-    }
+    if (found) break;
   }
   if (!found) {
     plan_free(p);
@@ -490,6 +497,7 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
   a.writeDetErr = det;
   a.cluster = p->C;
   a.tilesPerRow = (g.No + ptyg::TILE - 1) / ptyg::TILE;
+  a.probeInSmem = p->probeInSmem ? 1 : 0;
   a.betaO = u->beta_object;
   a.betaP = u->beta_probe;
   a.alphaO = u->alpha_object;

@@ -145,9 +145,11 @@ struct Smem {
   float* redF;      // 4 * 32
 };
 
-__host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int nosm, int npsm, bool qn) {
+__host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int nosm, int npsm, bool qn,
+                                                     bool probe_in_smem) {
   const size_t LN = (size_t)L * NP;
-  return (size_t)npsm * LN + (size_t)nosm * LN + (size_t)K * NP * (L + 1) + (size_t)K * LN + (qn ? npsm * LN : 0);
+  return (probe_in_smem ? (size_t)npsm * LN : 0) + (size_t)nosm * LN + (size_t)K * NP * (L + 1) + (size_t)K * LN +
+         (qn ? npsm * LN : 0);
 }
 
 // A row task's transformed row (Fourier layout: register r, lane l is slot
@@ -238,6 +240,7 @@ PTYG_DEV void prefetch_data(const EngineArgs& a, const ScanDev& s, const Smem& s
 // cluster has C = Np / L CTAs.  Both compile-time so index arithmetic is shifts.
 template <int E, int L>
 __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
+  // (512 threads x 128 registers: one CTA of 16 warps, or two of 8 warps, per SM)
   constexpr int NP = 32 * E;
   constexpr int C = NP / L;
   constexpr int LN = L * NP, ld = L + 1;
@@ -256,8 +259,12 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
 
   extern __shared__ float4 smem_f4[];
   Smem sm;
-  sm.probe = reinterpret_cast<float2*>(smem_f4);
-  sm.obj = sm.probe + npsm * LN;
+  // the CTA's probe rows: in shared memory when the layout fits (probeInSmem),
+  // else in place in global memory (only this CTA touches them)
+  const bool psm = a.probeInSmem != 0;
+  const int pst = psm ? LN : NP * NP;  // stride between probe modes
+  sm.probe = psm ? reinterpret_cast<float2*>(smem_f4) : s.probe + (size_t)line0 * NP;
+  sm.obj = reinterpret_cast<float2*>(smem_f4) + (psm ? npsm * LN : 0);
   sm.tile = sm.obj + nosm * LN;
   sm.rows = sm.tile + K * NP * ld;
   sm.U = sm.rows + K * LN;
@@ -268,9 +275,11 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   sm.redF = reinterpret_cast<float*>(sm.redD + 32);
   unsigned* slots0 = dsmem(sm.slots, 0);
 
-  for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
-    const int p = i / LN, rem = i - (i / LN) * LN;
-    sm.probe[i] = s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem];
+  if (psm) {
+    for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
+      const int p = i / LN, rem = i - (i / LN) * LN;
+      sm.probe[i] = s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem];
+    }
   }
   if (threadIdx.x < 2 * RED_BANK) sm.slots[threadIdx.x] = 0u;
   prefetch_data<NP, L>(a, s, sm, 0, blk0);
@@ -313,7 +322,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
       for (int i = threadIdx.x; i < LN; i += blockDim.x) {
         float sp2 = 0.f, sp1 = 0.f, so2 = 0.f;
         for (int p = 0; p < npsm; ++p) {
-          const float q = cabs2(sm.probe[p * LN + i]);
+          const float q = cabs2(sm.probe[p * pst + i]);
           sp2 += q;
           sp1 += sqrtf(q);
         }
@@ -335,7 +344,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
 #pragma unroll
           for (int j = 0; j < E; ++j) {
             const int x = lane + 32 * j;
-            float2 e = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[(p * L + l) * NP + x]);
+            float2 e = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[p * pst + l * NP + x]);
             if (fresnel) e = cmul(e, __ldg(a.fresnelQ + y * NP + x));
             v[j] = cscale(e, sg);
           }
@@ -458,7 +467,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
             const int x = lane + 32 * j;
             float2 u = cscale(v[j], sg);
             if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + x), u);
-            const float2 esw = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[(p * L + l) * NP + x]);
+            const float2 esw = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[p * pst + l * NP + x]);
             row[x] = csub(u, esw);
           }
         });
@@ -489,7 +498,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
           }
         }
         for (int p = 0; p < npsm; ++p) {
-          const float2 P = sm.probe[p * LN + i];
+          const float2 P = sm.probe[p * pst + i];
           const float q = cabs2(P);
           float gO;
           if (eng == ENG_EPIE) {
@@ -512,7 +521,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
           if (eng == ENG_QNEWTON)
             sm.U[p * LN + i] = accP;
           else
-            sm.probe[p * LN + i] = cadd(P, cscale(accP, stepP));
+            sm.probe[p * pst + i] = cadd(P, cscale(accP, stepP));
         }
         const int l = i / NP, x = i - (i / NP) * NP;
 #pragma unroll
@@ -547,7 +556,10 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
       block_max_to_slots<1>(m, sm.redF, red, idx);
       cluster_sync(C);
       const float scale = a.betaP / slot_value(red, RED_OMAXW);
-      for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) sm.probe[i] = cadd(sm.probe[i], cscale(sm.U[i], scale));
+      for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
+        const int p = i / LN, rem = i - (i / LN) * LN;
+        sm.probe[p * pst + rem] = cadd(sm.probe[p * pst + rem], cscale(sm.U[i], scale));
+      }
     }
 
     if (eng == ENG_MPIE && s.momentum && s.momentum[a.start + it]) {
@@ -573,10 +585,10 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
         const int p = i / LN, rem = i - (i / LN) * LN;
         const size_t gi = (size_t)p * NP * NP + (size_t)line0 * NP + rem;
         float2 Xn, Mn;
-        step(sm.probe[i], s.probeBuffer[gi], s.probeMomentum[gi], Xn, Mn);
+        step(sm.probe[p * pst + rem], s.probeBuffer[gi], s.probeMomentum[gi], Xn, Mn);
         s.probeMomentum[gi] = Mn;
         s.probeBuffer[gi] = Xn;
-        sm.probe[i] = Xn;
+        sm.probe[p * pst + rem] = Xn;
       }
     }
     __syncthreads();
@@ -585,19 +597,21 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   cp_async_wait_all();
   __syncthreads();
 
-  for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
-    const int p = i / LN, rem = i - (i / LN) * LN;
-    s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem] = sm.probe[i];
+  if (psm) {
+    for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
+      const int p = i / LN, rem = i - (i / LN) * LN;
+      s.probe[(size_t)p * a.nslice * NP * NP + (size_t)line0 * NP + rem] = sm.probe[i];
+    }
   }
   // no CTA may exit while another can still write into its shared memory
   cluster_sync(C);
 }
 
 // ------------------------------------------------------------------ launcher
-size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine) {
+size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine, bool probe_in_smem) {
   const int L = Np / C;
   const size_t LN = (size_t)L * Np;
-  const size_t n = smem_complex_elems(Np, L, nosm * npsm, nosm, npsm, engine == ENG_QNEWTON);
+  const size_t n = smem_complex_elems(Np, L, nosm * npsm, nosm, npsm, engine == ENG_QNEWTON, probe_in_smem);
   return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
          4 * 32 * sizeof(float) + 64;
 }

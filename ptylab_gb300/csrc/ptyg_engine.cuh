@@ -61,6 +61,7 @@ struct EngineArgs {
   int writeDetErr;
   int cluster;
   int tilesPerRow;         // ceil(No / TILE)
+  int probeInSmem;         // keep the CTA's probe rows in shared memory
   float betaO, betaP, alphaO, alphaP, regO, regP, frictionM, feedbackM, weightP, bethSlice;
 };
 

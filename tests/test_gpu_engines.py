@@ -256,3 +256,50 @@ def test_config3_fpm_qnewton_precision_vs_complex128(torch_cuda):
     print(msg)
     for k in keys:
         assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 5e-4, msg
+
+
+def _run_plan_c1(torch, cluster, nf=40, iters=3):
+    """mPIE, npsm = 4, Np = 128 through the C ABI with a given cluster size."""
+    from ptylab_gb300 import _native
+    from ptylab_gb300.simulate import ScanSpec, cpm_problem
+
+    lib = _native.require(0)
+    d, p, rec, _, _ = cpm_problem(ScanSpec(Np=128, No=320, num_positions=nf, npsm=4, probe_radius_fraction=0.25,
+                                           step_fraction=0.3, seed=3))
+    geom = _native.Geometry(Np=128, No=320, nosm=1, npsm=4, nslice=1, num_frames=nf, num_scans=1,
+                            engine=_native.ENGINES["mPIE"], propagator=0, fftshift=0, fpm=0, cluster=cluster)
+    plan = C.c_void_p()
+    _native.check(lib.ptyg_plan_create(C.byref(geom), C.byref(plan)))
+    cl, th, sm, mx = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    _native.check(lib.ptyg_plan_info(plan, C.byref(cl), C.byref(th), C.byref(sm), C.byref(mx)))
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dt)  # noqa: E731
+    obj, prb = t(rec.object, torch.complex64), t(rec.probe, torch.complex64)
+    bufs = [obj.clone(), torch.zeros_like(obj), prb.clone(), torch.zeros_like(prb)]
+    pos, data = t(rec.positions.astype(np.int32), torch.int32), t(d.ptychogram, torch.float32)
+    rs = np.random.RandomState(0)
+    order = t(np.concatenate([rs.permutation(nf) for _ in range(iters)]).astype(np.int32), torch.int32)
+    flags = t((rs.rand(iters * nf) > 0.8).astype(np.uint8), torch.uint8)
+    b = _native.ScanBuffers(object=obj.data_ptr(), probe=prb.data_ptr(), positions=pos.data_ptr(), order=order.data_ptr(),
+                            momentum_flags=flags.data_ptr(), object_buffer=bufs[0].data_ptr(),
+                            object_momentum=bufs[1].data_ptr(), probe_buffer=bufs[2].data_ptr(),
+                            probe_momentum=bufs[3].data_ptr())
+    _native.check(lib.ptyg_plan_bind_scan(plan, 0, C.byref(b), data.data_ptr(), None))
+    _native.check(lib.ptyg_plan_set_order(plan, 0, order.data_ptr(), flags.data_ptr(), iters * nf, None))
+    u = _native.UpdateParams(beta_object=0.25, beta_probe=0.25, alpha_object=0.25, alpha_probe=0.25, friction=0.7,
+                             feedback=0.3, probe_weight=1.0)
+    for k in range(iters):
+        _native.check(lib.ptyg_plan_run(plan, C.byref(u), k * nf, nf, 0, None))
+    torch.cuda.synchronize()
+    lib.ptyg_plan_destroy(plan)
+    return cl.value, sm.value, obj.cpu().numpy(), prb.cpu().numpy(), bufs[1].cpu().numpy()
+
+
+def test_cluster_shapes_agree(torch_cuda):
+    """16-CTA clusters (probe rows in shared memory) and 8-CTA clusters (probe
+    rows left in global memory, for layouts that exceed a CTA's shared memory)
+    compute the same reconstruction bit for bit."""
+    c16 = _run_plan_c1(torch_cuda, 16)
+    c8 = _run_plan_c1(torch_cuda, 8)
+    assert (c16[0], c8[0]) == (16, 8)
+    for a, b in zip(c16[2:], c8[2:]):
+        np.testing.assert_array_equal(a, b)
