@@ -2,8 +2,9 @@
 (``Engines.ePIE/mPIE/qNewton/e3PIE(reconstruction, experimentalData, params, monitor)``)."""
 
 from .BaseEngine import BaseEngine
+from .e3PIE import e3PIE
 from .ePIE import ePIE
 from .mPIE import mPIE
 from .qNewton import qNewton
 
-__all__ = ["BaseEngine", "ePIE", "mPIE", "qNewton"]
+__all__ = ["BaseEngine", "e3PIE", "ePIE", "mPIE", "qNewton"]

@@ -279,9 +279,12 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
     return fail(PTYG_ERR_UNSUPPORTED, "propagator %d is not on this path", g.propagator);
   if (g.propagator == PTYG_ASP && g.fftshift)
     return fail(PTYG_ERR_INVALID, "ASP propagatorType works only with fftshiftSwitch = False");
-  if (g.engine == PTYG_E3PIE)
-    return fail(PTYG_ERR_UNSUPPORTED, "e3PIE is not available in this build");
-  if (g.nslice != 1) return fail(PTYG_ERR_UNSUPPORTED, "nslice=%d needs the e3PIE engine", g.nslice);
+  if (g.engine == PTYG_E3PIE) {
+    if (g.nosm != 1) return fail(PTYG_ERR_UNSUPPORTED, "e3PIE with nosm=%d (object modes) is not on this path", g.nosm);
+    if (g.nslice > 6) return fail(PTYG_ERR_UNSUPPORTED, "e3PIE with nslice=%d > 6", g.nslice);
+  } else if (g.nslice != 1) {
+    return fail(PTYG_ERR_UNSUPPORTED, "nslice=%d needs the e3PIE engine", g.nslice);
+  }
   if (!ptyg::engine_modes_supported(g.Np, g.nosm, g.npsm))
     return fail(PTYG_ERR_UNSUPPORTED, "nosm=%d npsm=%d at Np=%d is not instantiated", g.nosm, g.npsm, g.Np);
   int dev;
@@ -301,10 +304,14 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
       p->C = c;
       p->probeInSmem = psm;
       p->threads = engine_threads(g, c);
-      p->smem = ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.engine, psm);
+      const bool e3 = g.engine == PTYG_E3PIE;
+      if (e3 && psm) continue;  // e3PIE keeps its probe slices in global memory
+      p->smem = e3 ? ptyg::e3pie_smem_bytes(g.Np, c, g.npsm)
+                   : ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.engine, psm);
       if ((int)p->smem > maxSmem) continue;
       int nclusters = 0;
-      cudaError_t e = ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, c, p->threads, p->smem, &nclusters);
+      cudaError_t e = e3 ? ptyg::e3pie_max_clusters(g.Np, c, p->threads, p->smem, &nclusters)
+                         : ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, c, p->threads, p->smem, &nclusters);
       if (e != cudaSuccess) {
         cudaGetLastError();
         continue;
@@ -334,6 +341,8 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
     if (e == cudaSuccess) e = cudaMalloc(&o.err, (size_t)g.num_frames * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&o.red, 2 * ptyg::RED_BANK * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&o.status, sizeof(int));
+    if (e == cudaSuccess && g.engine == PTYG_E3PIE)
+      e = cudaMalloc(&o.esw, (size_t)g.nslice * g.npsm * np2 * sizeof(float2));
     if (e == cudaSuccess && g.engine == PTYG_QNEWTON) {
       const int tpr = (g.No + ptyg::TILE - 1) / ptyg::TILE;
       e = cudaMalloc(&o.tileMax, (size_t)tpr * tpr * sizeof(float));
@@ -508,7 +517,9 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
   a.feedbackM = u->feedback;
   a.weightP = u->probe_weight;
   a.bethSlice = u->slice_beta;
-  cudaError_t e = ptyg::launch_engine(a, g.num_scans, p->threads, p->smem, st);
+  if (g.engine == PTYG_E3PIE && !p->sliceH) return fail(PTYG_ERR_INVALID, "e3PIE slice transfer function not set");
+  cudaError_t e = g.engine == PTYG_E3PIE ? ptyg::launch_e3pie(a, g.num_scans, p->threads, p->smem, st)
+                                         : ptyg::launch_engine(a, g.num_scans, p->threads, p->smem, st);
   if (e != cudaSuccess) return cuda_fail(e, "engine launch");
   return PTYG_OK;
 }

@@ -1,0 +1,405 @@
+// Persistent position-loop kernel for e3PIE, multislice ptychography
+// (PtyLab/Engines/e3PIE.py:71-225).
+//
+// Same cluster decomposition as ptyg_engine.cu (CTA c owns rows and
+// Fourier-layout columns [c*L, (c+1)*L); DSMEM transposes; cp.async intensity
+// prefetch).  Per position, with S slices and npsm probe modes (nosm = 1):
+//
+//   forward   esw_0 = O_0 * P_0;  for s = 1..S-1:
+//             P_s = ifft2(fft2(esw_{s-1}) * H),  esw_s = P_s * O_s    (e3PIE.py:99-115)
+//   detector  intensity projection of the last slice's exit waves     (e3PIE.py:118)
+//   backward  DELTA = eswUpdate - esw_{S-1}; for s = S-1..1:
+//             O_s += betaObject * sum_p conj(P_s) DELTA / max sum_p |P_s|^2
+//             P_s += 0.9 * conj(O_s) DELTA / max |O_s|^2
+//             DELTA = ifft2(fft2(P_s) * conj(H)) - esw_{s-1}          (e3PIE.py:125-160)
+//             then slice 0 with betaProbe                              (e3PIE.py:162-173)
+//
+// The object slices, the probe slices and the forward exit waves stay in
+// global memory (L2): at Np = 256 with four slices they would not fit in a
+// CTA's shared memory.  Only the last slice goes to the detector, which is all
+// the reference's update uses (it propagates every slice and keeps [-1]).
+#include "ptyg_engine_dev.cuh"
+
+namespace ptyg {
+
+constexpr int MAX_SLICES = 6;
+
+template <int E, int L>
+__global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
+  constexpr int NP = 32 * E;
+  constexpr int C = NP / L;
+  constexpr int LN = L * NP, ld = L + 1;
+  const int crank = (int)(blockIdx.x % (unsigned)C);
+  const ScanDev s = a.scans[blockIdx.x / C];
+  const int line0 = crank * L, sx0 = crank * L;
+  const unsigned lane = threadIdx.x & 31;
+  const int npsm = a.npsm, K = npsm, S = a.nslice, No = a.No;
+  const bool centred = a.centred != 0;
+  const bool fresnel = a.prop == PROP_FRESNEL;
+  const bool asp = a.prop == PROP_ASP;
+  const size_t No2 = (size_t)No * No;
+  const size_t NP2 = (size_t)NP * NP;
+  const int blk0 = asp ? line0 : sx0;
+
+  extern __shared__ float4 smem_f4[];
+  float2* tile = reinterpret_cast<float2*>(smem_f4);  // K * NP * ld
+  float2* rows = tile + K * NP * ld;                  // K * LN
+  float* fr = reinterpret_cast<float*>(rows + K * LN);
+  float* dat = fr + LN;  // 2 * LN
+  unsigned* slots = reinterpret_cast<unsigned*>(dat + 2 * LN);
+  double* redD = reinterpret_cast<double*>(slots + 2 * RED_BANK);
+  float* redF = reinterpret_cast<float*>(redD + 32);
+  unsigned* slots0 = dsmem(slots, 0);
+
+  if (threadIdx.x < 2 * RED_BANK) slots[threadIdx.x] = 0u;
+  prefetch_data<NP, L>(a, s, dat, 0, blk0);
+  WarpFFT<E> F;
+  F.init(a.twiddle, lane);
+  __syncthreads();
+  cluster_sync(C);
+
+  const float inv2 = 1.f / (float)NP2;
+
+  for (int it = 0; it < a.count; ++it) {
+    prefetch_data<NP, L>(a, s, dat, it + 1, blk0);
+    const int frame = s.order[a.start + it];
+    const int row0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame] : -1;
+    const int col0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame + 1] : -1;
+    if (row0 < 0 || col0 < 0 || row0 > No - NP || col0 > No - NP) {
+      if (crank == 0 && threadIdx.x == 0) atomicCAS(s.status, 0, 2);
+      continue;  // uniform across the cluster
+    }
+    unsigned* red = slots0 + (it & 1) * RED_BANK;
+    const float* datc = dat + (it & 1) * LN;
+    const size_t orow = (size_t)(row0 + line0) * No + col0;
+    // this CTA's rows of object slice sl, probe mode p of slice sl, exit wave (sl, p)
+    auto Ob = [&](int sl) { return s.object + sl * No2 + orow; };
+    auto Pb = [&](int p, int sl) { return s.probe + ((size_t)p * S + sl) * NP2 + (size_t)line0 * NP; };
+    auto Wb = [&](int sl, int p) { return s.eswStore + ((size_t)sl * npsm + p) * NP2 + (size_t)line0 * NP; };
+    // the detector transform's input factor at (row y, col x): centring sign, Fresnel chirp
+    auto detector_in = [&](float2 e, int y, int x) {
+      if (asp) return e;
+      if (fresnel) e = cmul(e, __ldg(a.fresnelQ + y * NP + x));
+      return (centred && ((y + x) & 1)) ? cscale(e, -1.f) : e;
+    };
+
+    // ---------------- norms of the pre-update object slices and of P_0
+    {
+      float m[MAX_SLICES + 1];
+#pragma unroll
+      for (int q = 0; q <= MAX_SLICES; ++q) m[q] = 0.f;
+      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+        const int l = i / NP, x = i % NP;
+#pragma unroll
+        for (int sl = 0; sl < MAX_SLICES; ++sl)
+          if (sl < S) m[sl] = fmaxf(m[sl], cabs2(ld_cg(Ob(sl) + (size_t)l * No + x)));
+        float sp = 0.f;
+        for (int p = 0; p < npsm; ++p) sp += cabs2(Pb(p, 0)[i]);
+        m[MAX_SLICES] = fmaxf(m[MAX_SLICES], sp);
+      }
+      const int idx[MAX_SLICES + 1] = {RED_SLICE_O,     RED_SLICE_O + 1, RED_SLICE_O + 2, RED_SLICE_O + 3,
+                                       RED_SLICE_O + 4, RED_SLICE_O + 5, RED_SLICE_P};
+      block_max_to_slots<MAX_SLICES + 1>(m, redF, red, idx);
+    }
+
+    // ---------------- slice 0 exit waves, forward row FFT
+    fft_tasks<E, false>(
+        F, K * L,
+        [&](int t, float2(&v)[E]) {
+          const int p = t / L, l = t % L;
+          const int y = line0 + l;
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int x = lane + 32 * j;
+            const float2 e = cmul(ld_cg(Ob(0) + (size_t)l * No + x), Pb(p, 0)[l * NP + x]);
+            Wb(0, p)[l * NP + x] = e;
+            v[j] = (S == 1) ? detector_in(e, y, x) : e;
+          }
+        },
+        [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+    cp_async_wait_prev();  // this position's intensities
+    cluster_sync(C);
+
+    // ---------------- forward through the slices
+    for (int sl = 1; sl < S; ++sl) {
+      column_filter<E, L>(tile, rows, F, a.sliceH, false, crank, K);
+      cluster_sync(C);
+      // P_s rows (natural order) into the row buffer and the probe's slice sl
+      fft_tasks<E, true>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+#pragma unroll
+            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + 32 * r + lane];
+          },
+          [&](int t, float2(&v)[E]) {
+            const int p = t / L, l = t % L;
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              const int x = lane + 32 * j;
+              rows[t * NP + x] = v[j];
+              Pb(p, sl)[l * NP + x] = v[j];
+            }
+          });
+      __syncthreads();
+      {
+        float m[1] = {0.f};
+        const bool last = sl == S - 1;
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          const int l = i / NP, x = i % NP;
+          const float2 O = ld_cg(Ob(sl) + (size_t)l * No + x);
+          float sp = 0.f;
+          for (int p = 0; p < npsm; ++p) {
+            const float2 P = rows[p * LN + i];
+            sp += cabs2(P);
+            const float2 e = cmul(P, O);
+            Wb(sl, p)[i] = e;
+            rows[p * LN + i] = last ? detector_in(e, line0 + l, x) : e;
+          }
+          m[0] = fmaxf(m[0], sp);
+        }
+        const int idx[1] = {RED_SLICE_P + sl};
+        block_max_to_slots<1>(m, redF, red, idx);
+      }
+      __syncthreads();
+      fft_tasks<E, false>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+#pragma unroll
+            for (int j = 0; j < E; ++j) v[j] = rows[t * NP + lane + 32 * j];
+          },
+          [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+      cluster_sync(C);
+    }
+
+    // ---------------- detector intensity projection (BaseEngine.py:870-1012)
+    double err = 0.0;
+    if (!asp) {
+      fft_tasks<E, false>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+            const int k = t / L, c = t % L;
+#pragma unroll
+            for (int j = 0; j < E; ++j) v[j] = tile[(k * NP + lane + 32 * j) * ld + c];
+          },
+          [&](int t, float2(&v)[E]) {
+            const int k = t / L, c = t % L;
+#pragma unroll
+            for (int r = 0; r < E; ++r) tile[(k * NP + 32 * r + lane) * ld + c] = v[r];
+          });
+      __syncthreads();
+      {
+        float e = 0.f;
+        const bool det = a.writeDetErr && s.detErr;
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          const int c = i / NP, sy = i % NP;
+          float ie = 0.f;
+          for (int k = 0; k < K; ++k) ie += cabs2(tile[(k * NP + sy) * ld + c]);
+          ie *= inv2;
+          const float im = datc[i];
+          const float d = fabsf(im - ie);
+          e += d;
+          if (det) s.detErr[((size_t)frame * NP + sx0) * NP + i] = d;
+          fr[i] = sqrtf(im / (ie + 1e-10f)) * inv2;
+        }
+        err = (double)e;
+      }
+      __syncthreads();
+      fft_tasks<E, true>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+            const int k = t / L, c = t % L;
+#pragma unroll
+            for (int r = 0; r < E; ++r)
+              v[r] = cscale(tile[(k * NP + 32 * r + lane) * ld + c], fr[c * NP + 32 * r + lane]);
+          },
+          [&](int t, float2(&v)[E]) { scatter_column<E, L>(rows, v, t / L, sx0 + t % L); });
+    } else {
+      column_filter<E, L>(tile, rows, F, a.aspH, false, crank, K);
+      cluster_sync(C);
+      fft_tasks<E, true>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+#pragma unroll
+            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + 32 * r + lane];
+          },
+          [&](int t, float2(&v)[E]) {
+#pragma unroll
+            for (int j = 0; j < E; ++j) rows[t * NP + lane + 32 * j] = v[j];
+          });
+      __syncthreads();
+      {
+        float e = 0.f;
+        const bool det = a.writeDetErr && s.detErr;
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          float ie = 0.f;
+          for (int k = 0; k < K; ++k) ie += cabs2(rows[k * LN + i]);
+          const float im = datc[i];
+          const float d = fabsf(im - ie);
+          e += d;
+          if (det) s.detErr[((size_t)frame * NP + line0) * NP + i] = d;
+          fr[i] = sqrtf(im / (ie + 1e-10f));
+        }
+        err = (double)e;
+      }
+      __syncthreads();
+      fft_tasks<E, false>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+            const int l = t % L;
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              const int x = lane + 32 * j;
+              v[j] = cscale(rows[t * NP + x], fr[l * NP + x]);
+            }
+          },
+          [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+      cluster_sync(C);
+      column_filter<E, L>(tile, rows, F, a.aspH, true, crank, K);
+    }
+    {
+      const double t = block_sum(err, redD);
+      if (threadIdx.x == 0) s.errPart[(size_t)frame * C + crank] = t;
+    }
+    if (crank == 0 && threadIdx.x < RED_BANK) slots[((it & 1) ^ 1) * RED_BANK + threadIdx.x] = 0u;
+    cluster_sync(C);
+
+    // ---------------- backward through the slices
+    for (int sl = S - 1; sl >= 0; --sl) {
+      // DELTA into the row buffer (natural order): the detector's back-propagated
+      // last slice minus esw_{S-1}, or the back-propagated P_{sl+1} minus esw_sl
+      const bool fromDetector = sl == S - 1;
+      fft_tasks<E, true>(
+          F, K * L,
+          [&](int t, float2(&v)[E]) {
+#pragma unroll
+            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + 32 * r + lane];
+          },
+          [&](int t, float2(&v)[E]) {
+            const int p = t / L, l = t % L;
+            const int y = line0 + l;
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              const int x = lane + 32 * j;
+              float2 u = v[j];
+              if (fromDetector && !asp) {
+                if (centred && ((y + x) & 1)) u = cscale(u, -1.f);
+                if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + x), u);
+              }
+              rows[t * NP + x] = csub(u, Wb(sl, p)[l * NP + x]);
+            }
+          });
+      __syncthreads();
+      // O_sl and P_sl steps (e3PIE.py:192-225) with the pre-update slices
+      {
+        const float invP = 1.f / slot_value(red, RED_SLICE_P + sl);
+        const float invO = 1.f / slot_value(red, RED_SLICE_O + sl);
+        const float stepP = (sl == 0) ? a.betaP : a.bethSlice;
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          const int l = i / NP, x = i % NP;
+          float2* op = Ob(sl) + (size_t)l * No + x;
+          const float2 O = ld_cg(op);
+          float2 acc = make_float2(0.f, 0.f);
+          for (int p = 0; p < npsm; ++p) {
+            float2* pp = Pb(p, sl) + i;
+            const float2 P = *pp;
+            const float2 d = rows[p * LN + i];
+            acc = cadd(acc, cmulc(P, d));
+            const float2 Pn = cadd(P, cscale(cmulc(O, d), stepP * invO));
+            *pp = Pn;
+            rows[p * LN + i] = Pn;
+          }
+          st_cg(op, cadd(O, cscale(acc, a.betaO * invP)));
+        }
+      }
+      if (sl > 0) {
+        // back-propagate the updated P_sl by conj(H)
+        __syncthreads();
+        fft_tasks<E, false>(
+            F, K * L,
+            [&](int t, float2(&v)[E]) {
+#pragma unroll
+              for (int j = 0; j < E; ++j) v[j] = rows[t * NP + lane + 32 * j];
+            },
+            [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+        cluster_sync(C);
+        column_filter<E, L>(tile, rows, F, a.sliceH, true, crank, K);
+        cluster_sync(C);
+      }
+    }
+    __syncthreads();
+    cluster_sync(C);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  cluster_sync(C);
+}
+
+// ------------------------------------------------------------------ launcher
+size_t e3pie_smem_bytes(int Np, int C, int npsm) {
+  const int L = Np / C;
+  const size_t LN = (size_t)L * Np;
+  const size_t n = (size_t)npsm * Np * (L + 1) + (size_t)npsm * LN;
+  // redF holds 32 floats per reduced value: MAX_SLICES + 1 of them
+  return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
+         8 * 32 * sizeof(float) + 64;
+}
+
+static cudaLaunchConfig_t e3_config(int cluster, int grid, int threads, size_t smem, cudaStream_t st,
+                                    cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+template <int E, int L>
+static cudaError_t e3_prepare(size_t smem) {
+  auto kern = e3pie_kernel<E, L>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (32 * E / L > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+#define PTYG_E3PIE_SHAPES(X) X(1, 8) X(1, 16) X(2, 8) X(2, 16) X(4, 8) X(4, 16) X(8, 16)
+
+cudaError_t e3pie_max_clusters(int Np, int cluster, int threads, size_t smem, int* out) {
+  *out = 0;
+  const int E = Np / 32, L = Np / cluster;
+#define PTYG_CALL(e, l)                                                     \
+  if (E == e && L == l) {                                                   \
+    cudaError_t err = e3_prepare<e, l>(smem);                               \
+    if (err != cudaSuccess) return err;                                     \
+    cudaLaunchAttribute attr[1];                                            \
+    cudaLaunchConfig_t cfg = e3_config(32 * e / l, 32 * e / l, threads, smem, 0, attr); \
+    return cudaOccupancyMaxActiveClusters(out, (void*)e3pie_kernel<e, l>, &cfg); \
+  }
+  PTYG_E3PIE_SHAPES(PTYG_CALL)
+#undef PTYG_CALL
+  return cudaErrorNotSupported;
+}
+
+cudaError_t launch_e3pie(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
+  const int E = a.Np / 32, L = a.Np / a.cluster;
+#define PTYG_CALL(e, l)                                                                   \
+  if (E == e && L == l) {                                                                 \
+    cudaError_t err = e3_prepare<e, l>(smem);                                             \
+    if (err != cudaSuccess) return err;                                                   \
+    cudaLaunchAttribute attr[1];                                                          \
+    cudaLaunchConfig_t cfg = e3_config(a.cluster, nscans * a.cluster, threads, smem, st, attr); \
+    return cudaLaunchKernelEx(&cfg, e3pie_kernel<e, l>, a);                              \
+  }
+  PTYG_E3PIE_SHAPES(PTYG_CALL)
+#undef PTYG_CALL
+  return cudaErrorNotSupported;
+}
+
+}  // namespace ptyg

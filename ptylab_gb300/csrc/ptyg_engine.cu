@@ -33,82 +33,9 @@
 //      pixels: object and probe steps (qNewton: whole-object max first)
 // ASP replaces B by transfer-function column passes around a real-space
 // projection row pass (Operators.py:155-230).
-#include <cooperative_groups.h>
-
-#include "ptyg_common.cuh"
-#include "ptyg_engine.cuh"
-
-namespace cg = cooperative_groups;
+#include "ptyg_engine_dev.cuh"
 
 namespace ptyg {
-
-// Address of `local` in the shared memory of cluster rank `rank`.
-template <class T>
-PTYG_DEV T* dsmem(T* local, int rank) {
-  return cg::this_cluster().map_shared_rank(local, (unsigned)rank);
-}
-
-PTYG_DEV void cp_async16(void* smem_dst, const void* gsrc) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
-}
-PTYG_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-PTYG_DEV void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-PTYG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-PTYG_DEV void cluster_sync(int C) {
-  if (C > 1) {
-    asm volatile(
-        "barrier.cluster.arrive.release.aligned;\n\t"
-        "barrier.cluster.wait.acquire.aligned;\n" ::
-            : "memory");
-  } else {
-    __syncthreads();
-  }
-}
-
-PTYG_DEV float warp_max(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-PTYG_DEV double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Max-reduce NV values over the CTA and fold them into the cluster slots (rank
-// 0's shared memory) with one cluster-scope atomicMax per value per CTA
-// (non-negative floats order like their bits).
-template <int NV>
-PTYG_DEV void block_max_to_slots(float (&v)[NV], float* scratch, unsigned* slots, const int* idx) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    const float m = warp_max(v[i]);
-    if (lane == 0) scratch[i * 32 + warp] = m;
-  }
-  __syncthreads();
-  if (threadIdx.x < NV) {
-    float m = 0.f;
-    for (int w = 0; w < nw; ++w) m = fmaxf(m, scratch[threadIdx.x * 32 + w]);
-    atomicMax(slots + idx[threadIdx.x], __float_as_uint(m));
-  }
-}
-
-// Sum over the CTA; thread 0 receives the result.
-PTYG_DEV double block_sum(double v, double* scratch) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  v = warp_sum(v);
-  if (lane == 0) scratch[warp] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < nw; ++w) t += scratch[w];
-  return t;
-}
 
 // max over one TILE x TILE object tile of sum_o |O_o|, this lane's share
 // (8 pixels per lane; the caller reduces across the warp).
@@ -125,10 +52,6 @@ PTYG_DEV float tile_max(const ScanDev& s, int ty, int tx, int nosm, int No, size
     }
   }
   return m;
-}
-
-PTYG_DEV float slot_value(const unsigned* slots, int i) {
-  return __uint_as_float(*reinterpret_cast<const volatile unsigned*>(slots + i));
 }
 
 // Shared-memory layout of one CTA, in complex64 units.
@@ -152,90 +75,7 @@ __host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int n
          (qn ? npsm * LN : 0);
 }
 
-// A row task's transformed row (Fourier layout: register r, lane l is slot
-// 32r + l) goes to the column blocks of the CTAs owning those slots.
-template <int E, int L>
-PTYG_DEV void scatter_row(const Smem& sm, const float2 (&v)[E], int k, int y) {
-  constexpr int NP = 32 * E;
-  constexpr int ld = L + 1;
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int r = 0; r < E; ++r) {
-    const int sx = 32 * r + lane;
-    const int owner = sx / L, c = sx - (sx / L) * L;
-    *dsmem(&sm.tile[(k * NP + y) * ld + c], owner) = v[r];
-  }
-}
-
-// A column task's result (natural order along y) goes back to the row buffers
-// of the CTAs owning those rows, at Fourier-layout slot sx.
-template <int E, int L>
-PTYG_DEV void scatter_column(const Smem& sm, const float2 (&v)[E], int k, int sx) {
-  constexpr int NP = 32 * E;
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int j = 0; j < E; ++j) {
-    const int y = lane + 32 * j;
-    const int owner = y / L, ly = y - (y / L) * L;
-    *dsmem(&sm.rows[(k * L + ly) * NP + sx], owner) = v[j];
-  }
-}
-
-// Column pass that multiplies the spectrum by H (or conj H) / Np^2 between a
-// forward and an inverse column transform (ASP, Operators.py:155-230); the
-// result goes to the row owners' row buffers.
-template <int E, int L>
-PTYG_DEV void column_filter(const Smem& sm, const WarpFFT<E>& F, const float2* H, bool conjH, int crank, int K) {
-  constexpr int NP = 32 * E;
-  constexpr int ld = L + 1;
-  const int lane = threadIdx.x & 31;
-  const int sx0 = crank * L;
-  const float inv2 = 1.f / (float)(NP * NP);
-  fft_tasks<E, false>(
-      F, K * L,
-      [&](int t, float2(&v)[E]) {
-        const int k = t / L, c = t % L;
-#pragma unroll
-        for (int j = 0; j < E; ++j) v[j] = sm.tile[(k * NP + lane + 32 * j) * ld + c];
-      },
-      [&](int t, float2(&v)[E]) {
-        const int k = t / L, c = t % L;
-        const float2* h = H + (size_t)(sx0 + c) * NP;
-#pragma unroll
-        for (int r = 0; r < E; ++r) {
-          float2 hv = __ldg(h + r * 32 + lane);
-          if (conjH) hv.y = -hv.y;
-          sm.tile[(k * NP + 32 * r + lane) * ld + c] = cscale(cmul(v[r], hv), inv2);
-        }
-      });
-  __syncthreads();
-  fft_tasks<E, true>(
-      F, K * L,
-      [&](int t, float2(&v)[E]) {
-        const int k = t / L, c = t % L;
-#pragma unroll
-        for (int r = 0; r < E; ++r) v[r] = sm.tile[(k * NP + 32 * r + lane) * ld + c];
-      },
-      [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm, v, t / L, sx0 + t % L); });
-}
-
 // ------------------------------------------------------------------ kernel
-// Prefetch the measured intensities of order slot `it` (if it exists and is a
-// valid frame) into dat[it & 1]: the CTA's L*NP block is contiguous in both
-// layouts (Fourier [frame][sx][sy] columns sx0.., or natural rows line0..).
-template <int NP, int L>
-PTYG_DEV void prefetch_data(const EngineArgs& a, const ScanDev& s, const Smem& sm, int it, int blk0) {
-  if (it < a.count) {
-    const int frame = s.order[a.start + it];
-    if (frame >= 0 && frame < a.numFrames) {
-      const float* src = s.data + ((size_t)frame * NP + blk0) * NP;
-      float* dst = sm.dat + (it & 1) * L * NP;
-      for (int i = threadIdx.x; i < L * NP / 4; i += blockDim.x) cp_async16(dst + 4 * i, src + 4 * i);
-    }
-  }
-  cp_async_commit();
-}
-
 // E: Np / 32 points per lane; L: rows (and Fourier columns) per CTA, so the
 // cluster has C = Np / L CTAs.  Both compile-time so index arithmetic is shifts.
 template <int E, int L>
@@ -282,7 +122,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
     }
   }
   if (threadIdx.x < 2 * RED_BANK) sm.slots[threadIdx.x] = 0u;
-  prefetch_data<NP, L>(a, s, sm, 0, blk0);
+  prefetch_data<NP, L>(a, s, sm.dat, 0, blk0);
   WarpFFT<E> F;
   F.init(a.twiddle, lane);
   if (eng == ENG_QNEWTON) {
@@ -299,7 +139,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   const float inv2 = 1.f / (float)(NP * NP);
 
   for (int it = 0; it < a.count; ++it) {
-    prefetch_data<NP, L>(a, s, sm, it + 1, blk0);
+    prefetch_data<NP, L>(a, s, sm.dat, it + 1, blk0);
     const int frame = s.order[a.start + it];
     const int row0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame] : -1;
     const int col0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame + 1] : -1;
@@ -349,7 +189,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
             v[j] = cscale(e, sg);
           }
         },
-        [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm, v, t / L, line0 + t % L); });
+        [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm.tile, v, t / L, line0 + t % L); });
     cp_async_wait_prev();  // this position's intensities
     cluster_sync(C);
 
@@ -394,10 +234,10 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
             for (int r = 0; r < E; ++r)
               v[r] = cscale(sm.tile[(k * NP + 32 * r + lane) * ld + c], sm.fr[c * NP + 32 * r + lane]);
           },
-          [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm, v, t / L, sx0 + t % L); });
+          [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm.rows, v, t / L, sx0 + t % L); });
     } else {
       // ---------------- ASP: x H, real-space projection, x conj(H)
-      column_filter<E, L>(sm, F, a.aspH, false, crank, K);
+      column_filter<E, L>(sm.tile, sm.rows, F, a.aspH, false, crank, K);
       cluster_sync(C);
       fft_tasks<E, true>(
           F, K * L,
@@ -437,9 +277,9 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
               v[j] = cscale(sm.rows[t * NP + x], sm.fr[l * NP + x]);
             }
           },
-          [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm, v, t / L, line0 + t % L); });
+          [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm.tile, v, t / L, line0 + t % L); });
       cluster_sync(C);
-      column_filter<E, L>(sm, F, a.aspH, true, crank, K);
+      column_filter<E, L>(sm.tile, sm.rows, F, a.aspH, true, crank, K);
     }
     {
       const double t = block_sum(err, sm.redD);

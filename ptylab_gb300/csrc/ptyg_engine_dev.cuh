@@ -1,0 +1,172 @@
+// Device helpers shared by the position-loop kernels (ptyg_engine.cu,
+// ptyg_e3pie.cu): cluster barrier and distributed shared memory, cp.async,
+// warp/CTA reductions into cluster slots, the DSMEM row/column transposes
+// and the transfer-function column pass.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "ptyg_common.cuh"
+#include "ptyg_engine.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace ptyg {
+
+// Address of `local` in the shared memory of cluster rank `rank`.
+template <class T>
+PTYG_DEV T* dsmem(T* local, int rank) {
+  return cg::this_cluster().map_shared_rank(local, (unsigned)rank);
+}
+
+PTYG_DEV void cp_async16(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+PTYG_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+PTYG_DEV void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+PTYG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+PTYG_DEV void cluster_sync(int C) {
+  if (C > 1) {
+    asm volatile(
+        "barrier.cluster.arrive.release.aligned;\n\t"
+        "barrier.cluster.wait.acquire.aligned;\n" ::
+            : "memory");
+  } else {
+    __syncthreads();
+  }
+}
+
+PTYG_DEV float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+PTYG_DEV double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Max-reduce NV values over the CTA and fold them into the cluster slots (rank
+// 0's shared memory) with one cluster-scope atomicMax per value per CTA
+// (non-negative floats order like their bits).
+template <int NV>
+PTYG_DEV void block_max_to_slots(float (&v)[NV], float* scratch, unsigned* slots, const int* idx) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const float m = warp_max(v[i]);
+    if (lane == 0) scratch[i * 32 + warp] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    float m = 0.f;
+    for (int w = 0; w < nw; ++w) m = fmaxf(m, scratch[threadIdx.x * 32 + w]);
+    atomicMax(slots + idx[threadIdx.x], __float_as_uint(m));
+  }
+}
+
+// Sum over the CTA; thread 0 receives the result.
+PTYG_DEV double block_sum(double v, double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < nw; ++w) t += scratch[w];
+  return t;
+}
+
+PTYG_DEV float slot_value(const unsigned* slots, int i) {
+  return __uint_as_float(*reinterpret_cast<const volatile unsigned*>(slots + i));
+}
+
+// A row task's transformed row (Fourier layout: register r, lane l is slot
+// 32r + l) goes to the column blocks of the CTAs owning those slots.
+template <int E, int L>
+PTYG_DEV void scatter_row(float2* tile, const float2 (&v)[E], int k, int y) {
+  constexpr int NP = 32 * E;
+  constexpr int ld = L + 1;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    const int sx = 32 * r + lane;
+    const int owner = sx / L, c = sx - (sx / L) * L;
+    *dsmem(&tile[(k * NP + y) * ld + c], owner) = v[r];
+  }
+}
+
+// A column task's result (natural order along y) goes back to the row buffers
+// of the CTAs owning those rows, at Fourier-layout slot sx.
+template <int E, int L>
+PTYG_DEV void scatter_column(float2* rows, const float2 (&v)[E], int k, int sx) {
+  constexpr int NP = 32 * E;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const int y = lane + 32 * j;
+    const int owner = y / L, ly = y - (y / L) * L;
+    *dsmem(&rows[(k * L + ly) * NP + sx], owner) = v[j];
+  }
+}
+
+// Column pass that multiplies the spectrum by H (or conj H) / Np^2 between a
+// forward and an inverse column transform (ASP, Operators.py:155-230); the
+// result goes to the row owners' row buffers.
+template <int E, int L>
+PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, const float2* H, bool conjH, int crank,
+                            int K) {
+  constexpr int NP = 32 * E;
+  constexpr int ld = L + 1;
+  const int lane = threadIdx.x & 31;
+  const int sx0 = crank * L;
+  const float inv2 = 1.f / (float)(NP * NP);
+  fft_tasks<E, false>(
+      F, K * L,
+      [&](int t, float2(&v)[E]) {
+        const int k = t / L, c = t % L;
+#pragma unroll
+        for (int j = 0; j < E; ++j) v[j] = tile[(k * NP + lane + 32 * j) * ld + c];
+      },
+      [&](int t, float2(&v)[E]) {
+        const int k = t / L, c = t % L;
+        const float2* h = H + (size_t)(sx0 + c) * NP;
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          float2 hv = __ldg(h + r * 32 + lane);
+          if (conjH) hv.y = -hv.y;
+          tile[(k * NP + 32 * r + lane) * ld + c] = cscale(cmul(v[r], hv), inv2);
+        }
+      });
+  __syncthreads();
+  fft_tasks<E, true>(
+      F, K * L,
+      [&](int t, float2(&v)[E]) {
+        const int k = t / L, c = t % L;
+#pragma unroll
+        for (int r = 0; r < E; ++r) v[r] = tile[(k * NP + 32 * r + lane) * ld + c];
+      },
+      [&](int t, float2(&v)[E]) { scatter_column<E, L>(rows, v, t / L, sx0 + t % L); });
+}
+
+// Prefetch the measured intensities of order slot `it` (if it exists and is a
+// valid frame) into dat[it & 1]: the CTA's L*NP block is contiguous in both
+// layouts (Fourier [frame][sx][sy] columns sx0.., or natural rows line0..).
+template <int NP, int L>
+PTYG_DEV void prefetch_data(const EngineArgs& a, const ScanDev& s, float* datBuf, int it, int blk0) {
+  if (it < a.count) {
+    const int frame = s.order[a.start + it];
+    if (frame >= 0 && frame < a.numFrames) {
+      const float* src = s.data + ((size_t)frame * NP + blk0) * NP;
+      float* dst = datBuf + (it & 1) * L * NP;
+      for (int i = threadIdx.x; i < L * NP / 4; i += blockDim.x) cp_async16(dst + 4 * i, src + 4 * i);
+    }
+  }
+  cp_async_commit();
+}
+
+}  // namespace ptyg

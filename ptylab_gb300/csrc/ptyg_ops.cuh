@@ -52,6 +52,9 @@ size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine, bool pro
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 bool engine_modes_supported(int Np, int nosm, int npsm);
 bool engine_shape_supported(int Np, int cluster);
+size_t e3pie_smem_bytes(int Np, int C, int npsm);
+cudaError_t e3pie_max_clusters(int Np, int cluster, int threads, size_t smem, int* out);
+cudaError_t launch_e3pie(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 cudaError_t engine_max_clusters(int Np, int nosm, int npsm, int cluster, int threads, size_t smem, int* out);
 
 }  // namespace ptyg

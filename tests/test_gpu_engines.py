@@ -17,7 +17,7 @@ from test_host_logic import containers
 
 pytestmark = pytest.mark.gpu
 TOL_FIXTURE = 1e-3
-IN_SCOPE = [n for n in fixture_names("reg_") + fixture_names("scan_") if "e3pie" not in n]
+IN_SCOPE = fixture_names("reg_") + fixture_names("scan_")
 
 
 @pytest.fixture(scope="module")
@@ -303,3 +303,43 @@ def test_cluster_shapes_agree(torch_cuda):
     assert (c16[0], c8[0]) == (16, 8)
     for a, b in zip(c16[2:], c8[2:]):
         np.testing.assert_array_equal(a, b)
+
+
+def test_config2_size_e3pie_precision_vs_complex128(torch_cuda):
+    """Multislice at the config-2 field size: Np = 256, four weak-phase slices
+    10 um apart, 13.5 nm wavelength, 20 nm pixels; 24 positions, 3 iterations.
+    The GB300 result is as close to a complex128 oracle run as the
+    reference's complex64 path (within 3x)."""
+    from oracle import ptyoracle as O
+    from ptylab_gb300 import DummyMonitor, Engines
+    from ptylab_gb300.simulate import ScanSpec, cpm_problem
+
+    spec = ScanSpec(Np=256, No=384, num_positions=24, probe_radius_fraction=0.2, step_fraction=0.35,
+                    wavelength=13.5e-9, zo=0.05, dxd=13.5e-9 * 0.05 / (256 * 20e-9), photons=1e5, phase_max=0.3, seed=9)
+    d, p, rec, _, _ = cpm_problem(spec)
+    rec.nslice = 4
+    rec.dz = 10e-6
+    rec.refrIndex = 1.0
+    np.random.seed(4)
+    rec.initializeObjectProbe()
+    obj0, prb0 = rec.object.copy(), rec.probe.copy()
+    eng = Engines.e3PIE(rec, d, p, DummyMonitor())
+    eng.numIterations = 3
+    eng.reconstruct()
+    g = O.Geometry(Np=256, No=384, dxp=rec.dxp, wavelength=rec.wavelength, zo=rec.zo, nslice=4, dz=10e-6)
+    s = O.Settings(engine="e3PIE", entrancePupilDiameter=d.entrancePupilDiameter)
+
+    def oracle(cdt, fdt):
+        st = O.State(object=obj0.astype(cdt), probe=prb0.astype(cdt))
+        return O.OracleEngine(s, g, st, d.ptychogram.astype(fdt), rec.positions, d.energyAtPos).reconstruct(3)
+
+    r64, r128 = oracle(np.complex64, np.float32), oracle(np.complex128, np.float64)
+    keys = ("object", "probe", "error")
+    gpu_vs_128 = {k: rel_err(getattr(rec, k), getattr(r128, k)) for k in keys}
+    ref_vs_128 = {k: rel_err(getattr(r64, k), getattr(r128, k)) for k in keys}
+    gpu_vs_64 = {k: rel_err(getattr(rec, k), getattr(r64, k)) for k in keys}
+    msg = f"e3PIE C2 size: gpu-c128 {gpu_vs_128} ref-c128 {ref_vs_128} gpu-ref {gpu_vs_64}"
+    print(msg)
+    for k in keys:
+        assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 1e-5, msg
+    assert rec.objectProd.shape == (1, 1, 1, 384, 384)

@@ -99,3 +99,11 @@ def test_fourier_layout_is_a_permutation(n):
     # the inverse used by from_fourier_layout: s = 32*(k % E) + bitrev5(k // E)
     s_back = np.array([32 * (kk % E) + _bitrev5(kk // E) for kk in k])
     np.testing.assert_array_equal(s_back, np.arange(n))
+
+
+def test_multislice_transfer_function_matches_the_oracle():
+    """e3PIE.py:62-69: aspw at dz, wavelength / refrIndex, Np, Lp."""
+    dz, lam, n, Np, dxp = 10e-6, 13.5e-9, 1.0, 256, 20e-9
+    np.testing.assert_array_equal(
+        _tables.multislice_tf(dz, lam, n, Np, Np * dxp), O.aspw_transfer_function(dz, lam / n, Np, Np * dxp)
+    )
