@@ -192,6 +192,30 @@ PTYG_API int ptyg_plan_detector_error(ptyg_plan* plan, int scan, float* out, voi
 PTYG_API int ptyg_plan_status(ptyg_plan* plan, int scan, int* host_status, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Differentiable multislice forward model and its adjoint (the model e3PIE
+ * inverts, PtyLab/Engines/e3PIE.py:99-118, with the Fraunhofer detector):
+ *   psi_0 = O_0[patch] P,  psi_s = ifft2(fft2(psi_{s-1}) H) O_s[patch],
+ *   I = sum_modes |fft2c(psi_{S-1})|^2.
+ * object (nslice, No, No), probe (npsm, Np, Np) complex64; slice_h the
+ * ifftshifted slice transfer function (Np*Np complex64, natural order).
+ * The adjoint accumulates dL/dRe + i dL/dIm of a real loss L into
+ * grad_object / grad_probe (caller zeroes them) given grad_intensity = dL/dI.
+ * Positions go in chunks of `chunk`; the adjoint recomputes each chunk's slice
+ * fields.  Workspace: ptyg_multislice_workspace_bytes() of device memory. */
+typedef struct ptyg_multislice {
+  int32_t Np, No, npsm, nslice, num_frames, chunk;
+} ptyg_multislice;
+
+PTYG_API size_t ptyg_multislice_workspace_bytes(const ptyg_multislice* geometry);
+PTYG_API int ptyg_multislice_forward(const ptyg_multislice* geometry, const void* object, const void* probe,
+                                     const int32_t* positions, const void* slice_h, float* intensity, void* workspace,
+                                     size_t workspace_bytes, void* stream);
+PTYG_API int ptyg_multislice_adjoint(const ptyg_multislice* geometry, const void* object, const void* probe,
+                                     const int32_t* positions, const void* slice_h, const float* grad_intensity,
+                                     void* grad_object, void* grad_probe, void* workspace, size_t workspace_bytes,
+                                     void* stream);
+
+/* ------------------------------------------------------------------------
  * Small per-iteration helpers of BaseEngine.applyConstraints
  * (BaseEngine.py:1440-1612) and orthogonalizeModes (utils.py:130-211).
  */

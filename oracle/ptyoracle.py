@@ -563,3 +563,38 @@ def run_fixture(fx, iters=None, dtype=None):
     eng = OracleEngine(s, g, st, np.asarray(i["ptychogram"], dtype=fdt), i["positions"], i["energyAtPos"])
     np.random.seed(int(m["seed"]))
     return eng.reconstruct(int(m["iters"]) if iters is None else iters)
+
+
+# ----------------------------------------------------------------------------
+# multislice forward model (the model e3PIE inverts) and its reference gradient
+# ----------------------------------------------------------------------------
+def multislice_forward(obj, probe, positions, H_shifted):
+    """I_j = sum_p |fft2c(psi_{S-1})|^2, psi_0 = O_0[patch] P, psi_s = ifft2(fft2(psi_{s-1}) H) O_s[patch]
+    (e3PIE.py:99-118 with the Fraunhofer detector); obj (S, No, No), probe (npsm, Np, Np)."""
+    S = obj.shape[0]
+    Np = probe.shape[-1]
+    out = np.empty((len(positions), Np, Np))
+    for j, (r, c) in enumerate(positions):
+        psi = obj[0, r : r + Np, c : c + Np] * probe
+        for s in range(1, S):
+            psi = np.fft.ifft2(np.fft.fft2(psi) * H_shifted) * obj[s, r : r + Np, c : c + Np]
+        out[j] = np.sum(np.abs(fft2c(psi)) ** 2, axis=0)
+    return out
+
+
+def e3pie_last_slice_delta(obj, probe, position, H_shifted, Imeas):
+    """For one position and one probe mode: the last slice's incident field
+    P_{S-1} and e3PIE's DELTA = eswUpdate - esw of the last slice after the
+    standard intensity projection (e3PIE.py:99-123, BaseEngine.py:870-1012)."""
+    S = obj.shape[0]
+    Np = probe.shape[-1]
+    r, c = position
+    P = probe
+    psi = obj[0, r : r + Np, c : c + Np] * P
+    for s in range(1, S):
+        P = np.fft.ifft2(np.fft.fft2(psi) * H_shifted)
+        psi = P * obj[s, r : r + Np, c : c + Np]
+    Psi = fft2c(psi)
+    Iest = np.sum(np.abs(Psi) ** 2, axis=0)
+    frac = np.sqrt(Imeas / (Iest + 1e-10))
+    return P, ifft2c(Psi * frac) - psi

@@ -84,7 +84,18 @@ class ScanBuffers(C.Structure):
     ]
 
 
-# name -> (restype, argtypes); every function returns an int status
+class Multislice(C.Structure):
+    _fields_ = [
+        ("Np", C.c_int32),
+        ("No", C.c_int32),
+        ("npsm", C.c_int32),
+        ("nslice", C.c_int32),
+        ("num_frames", C.c_int32),
+        ("chunk", C.c_int32),
+    ]
+
+
+# name -> argtypes; every function returns an int status unless listed in _RESTYPES
 _SIGNATURES = {
     "ptyg_version": [],
     "ptyg_last_error": None,
@@ -108,10 +119,21 @@ _SIGNATURES = {
     "ptyg_plan_frame_errors": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_detector_error": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_status": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p],
+    "ptyg_multislice_workspace_bytes": [C.POINTER(Multislice)],
+    "ptyg_multislice_forward": [
+        C.POINTER(Multislice), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+        C.c_void_p,
+    ],
+    "ptyg_multislice_adjoint": [
+        C.POINTER(Multislice), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+        C.c_void_p, C.c_size_t, C.c_void_p,
+    ],
     "ptyg_mul_window": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p],
     "ptyg_gram": [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p],
     "ptyg_mix_modes": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.c_void_p],
 }
+
+_RESTYPES = {"ptyg_last_error": C.c_char_p, "ptyg_multislice_workspace_bytes": C.c_size_t}
 
 _lock = threading.Lock()
 _lib = None
@@ -133,12 +155,8 @@ def load_library(path: Path | str | None = None):
         lib = C.CDLL(str(p))
         for name, args in _SIGNATURES.items():
             fn = getattr(lib, name)
-            if name == "ptyg_last_error":
-                fn.restype = C.c_char_p
-                fn.argtypes = []
-            else:
-                fn.restype = C.c_int
-                fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, C.c_int)
+            fn.argtypes = args if args is not None else []
         if path is None:
             _lib = lib
         return lib

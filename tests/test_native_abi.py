@@ -19,7 +19,7 @@ def lib():
 
 def declared_functions():
     text = (ROOT / "include" / "ptyg.h").read_text()
-    return sorted(set(re.findall(r"^\s*(?:PTYG_API\s+)?(?:int|const char\*)\s+(ptyg_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:PTYG_API\s+)?(?:int|size_t|const char\*)\s+(ptyg_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_header_declares_the_bound_functions():
