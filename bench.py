@@ -156,6 +156,22 @@ def algorithmic_counts(flags_per_step, nscans):
     return float(bytes_), float(flops), float(per_pos_bytes), float(per_pos_flops)
 
 
+# ------------------------------------------------------------------ ranks
+def reduce_over_ranks(seconds, units, device=None):
+    """Whole-job timing under torch.distributed: the slowest rank's time and
+    the units all ranks processed (weak scaling: every rank owns its scans)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(seconds), float(units)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 # ------------------------------------------------------------------ gb300 arm
 def run_gb300(args, rank, world, local_rank):
     import torch
@@ -235,11 +251,8 @@ def run_gb300(args, rank, world, local_rank):
     clk = clocks.stop()
     lib.ptyg_plan_destroy(plan)
     del keep
-    if world > 1:
-        tt = torch.tensor([t], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
-    value = world * G * NPOS * args.steps / t
+    t, units = reduce_over_ranks(t, G * NPOS * args.steps, dev)
+    value = units / t
     ms_per_step = t / args.steps * 1e3
     flags_timed = float(flag_counts[args.warmup:].sum()) / args.steps
     bytes_step, flops_step, per_pos_bytes, per_pos_flops = algorithmic_counts(flags_timed, G)
