@@ -45,7 +45,9 @@ enum ptyg_status {
   PTYG_ERR_DEVICE = -6       /* no usable sm_103a device (ImportError)       */
 };
 
-enum ptyg_engine { PTYG_EPIE = 0, PTYG_MPIE = 1, PTYG_QNEWTON = 2, PTYG_E3PIE = 3 };
+enum ptyg_engine { PTYG_EPIE = 0, PTYG_MPIE = 1, PTYG_QNEWTON = 2, PTYG_E3PIE = 3, PTYG_MQNEWTON = 4 };
+/* mqNewton.momentum_method (PtyLab/Engines/mqNewton.py:68-79, 142-182) */
+enum ptyg_momentum { PTYG_MOMENTUM = 0, PTYG_ADAM = 1, PTYG_NADAM = 2 };
 enum ptyg_propagator { PTYG_FRAUNHOFER = 0, PTYG_FRESNEL = 1, PTYG_ASP = 2 };
 enum ptyg_direction { PTYG_FORWARD = 0, PTYG_INVERSE = 1 };
 
@@ -95,8 +97,9 @@ PTYG_API int ptyg_propagate_noalloc(int propagator, int direction, int fftshift,
 /* ------------------------------------------------------------------------
  * Engine plans: the drop-in for the position loop of ePIE.reconstruct_stepwise
  * (PtyLab/Engines/ePIE.py:78-112), mPIE.reconstruct (mPIE.py:276-333),
- * qNewton.reconstruct (qNewton.py:67-90) and e3PIE.reconstruct
- * (e3PIE.py:229-313), with BaseEngine.intensityProjection
+ * qNewton.reconstruct (qNewton.py:67-90), mqNewton.reconstruct
+ * (mqNewton.py:81-140) and e3PIE.reconstruct (e3PIE.py:229-313), with
+ * BaseEngine.intensityProjection
  * (BaseEngine.py:870-1012) and getRMSD (BaseEngine.py:843-868).
  */
 typedef struct ptyg_geometry {
@@ -118,7 +121,12 @@ typedef struct ptyg_geometry {
 } ptyg_geometry;
 
 /* Engine scalars (ePIE.py:35-42, mPIE.py:233-245, qNewton.py:43-52,
- * e3PIE.py:186-195); probe_weight is mPIE's per-update weight (1). */
+ * e3PIE.py:186-195, mqNewton.py:50-66); probe_weight is mPIE's per-update
+ * weight (1).  The mqNewton fields are read by that engine only:
+ * beta1/beta2 are the Python floats themselves (the kernel rounds beta and
+ * 1 - beta to float32 as NumPy does), beta1_scale/beta2_scale the float32
+ * values of 1 - beta**itr for the iteration itr = loop + 1 that the launch
+ * belongs to (mqNewton.py:144-145), so one launch must not span iterations. */
 typedef struct ptyg_update_params {
   float beta_object, beta_probe;
   float alpha_object, alpha_probe;
@@ -126,11 +134,23 @@ typedef struct ptyg_update_params {
   float friction, feedback;
   float probe_weight;
   float slice_beta; /* e3PIE probe step for slices >= 1 (0.9 in e3PIE.py:280) */
+  int32_t momentum_method; /* enum ptyg_momentum */
+  double beta1, beta2;
+  float beta1_scale, beta2_scale;
+  float beta_object_m, beta_probe_m;
 } ptyg_update_params;
 
-/* Caller-owned device buffers of one scan.  Momentum/buffer pointers are
- * needed by mPIE only; momentum_flags by mPIE only (one byte per order slot,
- * nonzero -> momentum step after that position, mPIE.py:330-332). */
+/* Caller-owned device buffers of one scan.
+ *   mPIE: object/probe buffers and momenta, and momentum_flags (one byte per
+ *         order slot, nonzero -> momentum step after that position,
+ *         mPIE.py:330-332).
+ *   mqNewton: object_momentum and probe_momentum (the first moments),
+ *         probe_buffer, and second_moment = {v_object, v_probe}: a float32
+ *         device pair holding the value every element of objectMomentum_v /
+ *         probeMomentum_v carries (they start as zero arrays and every ADAM /
+ *         NADAM step adds a scalar, mqNewton.py:68-79, 142-153).  The object
+ *         buffer must equal the object when the run starts; it then stays
+ *         equal after every position, so the kernel does not read it. */
 typedef struct ptyg_scan_buffers {
   void* object;
   void* probe;
@@ -141,6 +161,7 @@ typedef struct ptyg_scan_buffers {
   void* object_momentum;
   void* probe_buffer;
   void* probe_momentum;
+  float* second_moment;
 } ptyg_scan_buffers;
 
 typedef struct ptyg_plan ptyg_plan;
@@ -175,7 +196,8 @@ PTYG_API int ptyg_plan_info(ptyg_plan* plan, int* cluster, int* threads, int* sm
 
 /* Process order slots [start, start+count) of every bound scan: for each
  * slot, position order[slot] goes through gather -> propagate -> intensity
- * projection -> back-propagate -> object/probe update (-> momentum step).
+ * projection -> back-propagate -> object/probe update (-> momentum step;
+ * mqNewton: an adaptive-momentum step on the whole object and probe).
  * flags bit 0: also record |I_meas - I_est| per pixel (detectorError). */
 PTYG_API int ptyg_plan_run(ptyg_plan* plan, const ptyg_update_params* params, int start, int count, int flags, void* stream);
 

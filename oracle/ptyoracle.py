@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  This module restates, in NumPy, the algorithm of the
 PtyLab.py reference (version 0.3.1) for the path the GB300 package accelerates:
-the ePIE / mPIE / qNewton / e3PIE position loops, the standard intensity
+the ePIE / mPIE / qNewton / mqNewton / e3PIE position loops, the standard intensity
 projection, the Fraunhofer / Fresnel / ASP propagators, the error metrics, the
 position order and the seeded initial guesses.  Only ``tests/``, the package's
 ``smoke()`` entry and ``bench.py``'s CPU-baseline leg may import it, and only as
@@ -245,9 +245,15 @@ class Settings:
     frictionM: float = 0.7
     regObject: float = 1.0
     regProbe: float = 1.0
+    # mqNewton (mqNewton.py:50-66)
+    beta1: float = 0.5
+    beta2: float = 0.5
+    betaObject_m: float = 0.25
+    betaProbe_m: float = 0.25
+    momentum_method: str = "ADAM"
 
 
-_DEFAULT_BETAS = {"ePIE": (0.25, 0.25), "mPIE": (0.25, 0.25), "qNewton": (1, 1), "e3PIE": (0.25, 0.25)}
+_DEFAULT_BETAS = {"ePIE": (0.25, 0.25), "mPIE": (0.25, 0.25), "qNewton": (1, 1), "mqNewton": (1, 1), "e3PIE": (0.25, 0.25)}
 
 
 @dataclass
@@ -261,6 +267,8 @@ class State:
     probeMomentum: Optional[np.ndarray] = None
     objectBuffer: Optional[np.ndarray] = None
     probeBuffer: Optional[np.ndarray] = None
+    objectMomentum_v: Optional[np.ndarray] = None
+    probeMomentum_v: Optional[np.ndarray] = None
     purityProbe: float = 1.0
 
 
@@ -280,7 +288,8 @@ class OracleEngine:
         self.betaObject = bo if s.betaObject is None else s.betaObject
         self.betaProbe = bp if s.betaProbe is None else s.betaProbe
         self.fftshiftFlag = False
-        self.momentumAcceleration = s.engine == "mPIE"
+        self.momentumAcceleration = s.engine in ("mPIE", "mqNewton")
+        self._loop = 0
         self.Xp = g.Xp if Xp is None else Xp
         self.Yp = g.Yp if Yp is None else Yp
         if s.engine == "mPIE":
@@ -290,6 +299,13 @@ class OracleEngine:
                 st.objectMomentum = np.zeros_like(st.object)
             if st.probeMomentum is None:
                 st.probeMomentum = np.zeros_like(st.probe)
+        if s.engine == "mqNewton":
+            # mqNewton.py:41-47: zero momenta, buffers from the guess at construction
+            st = self.st
+            st.objectMomentum = np.zeros_like(st.object)
+            st.probeMomentum = np.zeros_like(st.probe)
+            st.objectBuffer = st.object.copy()
+            st.probeBuffer = st.probe.copy()
         if s.engine == "e3PIE":
             # e3PIE.py:62-69: ifftshifted aspw TF for the slice spacing, complex128
             H = aspw_transfer_function(g.dz, g.wavelength / g.refrIndex, g.Np, g.Lp)
@@ -396,6 +412,39 @@ class OracleEngine:
         frac = np.abs(patch) / Omax * patch.conj() / (np.abs(patch) ** 2 + self.s.regProbe)
         return self.st.probe + self.betaProbe * np.sum(frac * D, axis=(0, 1, 3), keepdims=True)
 
+    def adaptive_step(self, grad, m, v, itr):  # mqNewton.py:142-182
+        """(update, first moment, second moment) of the chosen momentum method."""
+        s = self.s
+        if s.momentum_method == "momentum":
+            m = grad + s.frictionM * m
+            return m, m, v
+        b1s = 1 - s.beta1**itr
+        b2s = 1 - s.beta2**itr
+        nsq = np.linalg.norm(grad.ravel(), 2) ** 2
+        m = s.beta1 * m + (1 - s.beta1) * grad
+        v = s.beta2 * v + (1 - s.beta2) * nsq
+        m_hat = m / b1s
+        denom = (v / b2s) ** 0.5 + 1e-8
+        if s.momentum_method == "ADAM":
+            return m_hat / denom, m, v
+        if s.momentum_method == "NADAM":
+            return (s.beta1 * m_hat + grad * (1 - s.beta1) / b1s) / denom, m, v
+        raise AttributeError(s.momentum_method)
+
+    def mq_momentum(self):  # mqNewton.py:184-224
+        st, s = self.st, self.s
+        itr = self._loop + 1
+        u, st.objectMomentum, st.objectMomentum_v = self.adaptive_step(
+            st.objectBuffer - st.object, st.objectMomentum, st.objectMomentum_v, itr
+        )
+        st.object = st.object - s.betaObject_m * u
+        st.objectBuffer = st.object.copy()
+        u, st.probeMomentum, st.probeMomentum_v = self.adaptive_step(
+            st.probeBuffer - st.probe, st.probeMomentum, st.probeMomentum_v, itr
+        )
+        st.probe = st.probe - s.betaProbe_m * u
+        st.probeBuffer = st.probe.copy()
+
     def e3_object(self, patch, D, localProbe):  # e3PIE.py:192-208
         frac = localProbe.conj() / np.max(np.sum(np.abs(localProbe) ** 2, axis=(0, 1, 2)))
         return patch + self.betaObject * np.sum(frac * D, axis=(0, 2), keepdims=True)
@@ -428,6 +477,10 @@ class OracleEngine:
         elif eng == "qNewton":
             st.object[..., sy, sx] = self.qn_object(patch, D)
             st.probe = self.qn_probe(patch, D)
+        elif eng == "mqNewton":  # mqNewton.py:112-126
+            st.object[..., sy, sx] = self.qn_object(patch, D)
+            st.probe = self.qn_probe(patch, D)
+            self.mq_momentum()
         else:
             raise NotImplementedError(eng)
 
@@ -499,8 +552,13 @@ class OracleEngine:
             st.probeBuffer = st.probe.copy()
         if self.s.engine == "e3PIE":  # e3PIE.py:75
             st.esw = st.probe.copy()
+        if self.s.engine == "mqNewton" and self.s.momentum_method in ("ADAM", "NADAM"):
+            # initializeAdaptiveMomentum (mqNewton.py:68-79)
+            st.objectMomentum_v = st.objectMomentum.copy()
+            st.probeMomentum_v = st.probeMomentum.copy()
         nf = self.ptychogram.shape[0]
         for loop in range(num_iterations):
+            self._loop = loop
             order = position_order(self.s.order, nf, len(st.error), self.positions)
             for j in order:
                 draw = np.random.rand(1)[0] if self.s.engine == "mPIE" else None
@@ -547,6 +605,7 @@ def run_fixture(fx, iters=None, dtype=None):
         dz=float(i.get("dz", 0.0)),
     )
     s = Settings(
+        momentum_method=str(m.get("momentum_method", "ADAM")),
         engine=str(m["engine"]),
         propagator=str(m["propagator"]),
         order=str(m["order"]),

@@ -207,6 +207,7 @@ class BaseEngine(object):
         _native.check(lib.ptyg_plan_create(C.byref(geom), C.byref(plan)), "ptyg_plan_create")
         self._plan = plan
         self._set_tables()
+        self._device_extras()
         self._bind()
         self.params.gpuFlag = 1
 
@@ -229,6 +230,9 @@ class BaseEngine(object):
 
     def _slice_table(self):
         return None
+
+    def _device_extras(self):
+        """Engine-specific device state created before the scan is bound."""
 
     def _scan_buffers(self):
         rec = self.reconstruction

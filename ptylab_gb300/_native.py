@@ -24,7 +24,8 @@ PTYG_ERR_CUDA = -4
 PTYG_ERR_TIMEOUT = -5
 PTYG_ERR_DEVICE = -6
 
-ENGINES = {"ePIE": 0, "mPIE": 1, "qNewton": 2, "e3PIE": 3}
+ENGINES = {"ePIE": 0, "mPIE": 1, "qNewton": 2, "e3PIE": 3, "mqNewton": 4}
+MOMENTUM_METHODS = {"momentum": 0, "ADAM": 1, "NADAM": 2}
 PROPAGATORS = {"fraunhofer": 0, "fresnel": 1, "asp": 2}
 
 _EXC = {
@@ -67,6 +68,13 @@ class UpdateParams(C.Structure):
         ("feedback", C.c_float),
         ("probe_weight", C.c_float),
         ("slice_beta", C.c_float),
+        ("momentum_method", C.c_int32),
+        ("beta1", C.c_double),
+        ("beta2", C.c_double),
+        ("beta1_scale", C.c_float),
+        ("beta2_scale", C.c_float),
+        ("beta_object_m", C.c_float),
+        ("beta_probe_m", C.c_float),
     ]
 
 
@@ -81,6 +89,7 @@ class ScanBuffers(C.Structure):
         ("object_momentum", C.c_void_p),
         ("probe_buffer", C.c_void_p),
         ("probe_momentum", C.c_void_p),
+        ("second_moment", C.c_void_p),
     ]
 
 

@@ -274,7 +274,7 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   if (g.No < g.Np) return fail(PTYG_ERR_INVALID, "No=%d smaller than Np=%d", g.No, g.Np);
   if (g.nosm < 1 || g.npsm < 1 || g.nslice < 1 || g.num_frames < 1 || g.num_scans < 1)
     return fail(PTYG_ERR_INVALID, "mode/slice/frame/scan counts must be >= 1");
-  if (g.engine < PTYG_EPIE || g.engine > PTYG_E3PIE) return fail(PTYG_ERR_INVALID, "engine=%d", g.engine);
+  if (g.engine < PTYG_EPIE || g.engine > PTYG_MQNEWTON) return fail(PTYG_ERR_INVALID, "engine=%d", g.engine);
   if (g.propagator < PTYG_FRAUNHOFER || g.propagator > PTYG_ASP)
     return fail(PTYG_ERR_UNSUPPORTED, "propagator %d is not on this path", g.propagator);
   if (g.propagator == PTYG_ASP && g.fftshift)
@@ -343,7 +343,7 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
     if (e == cudaSuccess) e = cudaMalloc(&o.status, sizeof(int));
     if (e == cudaSuccess && g.engine == PTYG_E3PIE)
       e = cudaMalloc(&o.esw, (size_t)g.nslice * g.npsm * np2 * sizeof(float2));
-    if (e == cudaSuccess && g.engine == PTYG_QNEWTON) {
+    if (e == cudaSuccess && (g.engine == PTYG_QNEWTON || g.engine == PTYG_MQNEWTON)) {
       const int tpr = (g.No + ptyg::TILE - 1) / ptyg::TILE;
       e = cudaMalloc(&o.tileMax, (size_t)tpr * tpr * sizeof(float));
     }
@@ -419,6 +419,9 @@ extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffe
   if (p->g.engine == PTYG_MPIE &&
       (!b->object_buffer || !b->object_momentum || !b->probe_buffer || !b->probe_momentum))
     return fail(PTYG_ERR_INVALID, "mPIE needs object/probe buffers and momenta");
+  if (p->g.engine == PTYG_MQNEWTON &&
+      (!b->object_momentum || !b->probe_buffer || !b->probe_momentum || !b->second_moment))
+    return fail(PTYG_ERR_INVALID, "mqNewton needs object/probe momenta, the probe buffer and the second-moment pair");
   cudaStream_t st = (cudaStream_t)stream;
   ScanOwned& o = p->scans[scan];
   o.buf = *b;
@@ -450,6 +453,7 @@ extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffe
   d.red = o.red;
   d.status = o.status;
   d.tileMax = o.tileMax;
+  d.moment2 = b->second_moment;
   o.bound = true;
   o.orderLen = p->g.num_frames;
   PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &d, sizeof(ScanDev), cudaMemcpyHostToDevice, st), "scan upload");
@@ -517,6 +521,22 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
   a.feedbackM = u->feedback;
   a.weightP = u->probe_weight;
   a.bethSlice = u->slice_beta;
+  if (g.engine == PTYG_MQNEWTON) {
+    if (u->momentum_method < PTYG_MOMENTUM || u->momentum_method > PTYG_NADAM)
+      return fail(PTYG_ERR_INVALID, "momentum_method=%d", u->momentum_method);
+    if (!(u->beta1_scale != 0.f) || !(u->beta2_scale != 0.f))
+      return fail(PTYG_ERR_INVALID, "beta1_scale and beta2_scale (1 - beta**itr) must be nonzero");
+    a.momentum = u->momentum_method;
+    // NumPy rounds each Python float operand to float32 at the operation
+    a.b1 = (float)u->beta1;
+    a.omb1 = (float)(1.0 - u->beta1);
+    a.b2 = (float)u->beta2;
+    a.omb2 = (float)(1.0 - u->beta2);
+    a.b1s = u->beta1_scale;
+    a.b2s = u->beta2_scale;
+    a.betaOm = u->beta_object_m;
+    a.betaPm = u->beta_probe_m;
+  }
   if (g.engine == PTYG_E3PIE && !p->sliceH) return fail(PTYG_ERR_INVALID, "e3PIE slice transfer function not set");
   cudaError_t e = g.engine == PTYG_E3PIE ? ptyg::launch_e3pie(a, g.num_scans, p->threads, p->smem, st)
                                          : ptyg::launch_engine(a, g.num_scans, p->threads, p->smem, st);

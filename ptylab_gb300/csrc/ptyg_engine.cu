@@ -1,11 +1,11 @@
-// Persistent position-loop kernel for ePIE / mPIE / qNewton (CPM and FPM) with
-// the Fraunhofer, Fresnel and ASP propagators.
+// Persistent position-loop kernel for ePIE / mPIE / qNewton / mqNewton (CPM and
+// FPM) with the Fraunhofer, Fresnel and ASP propagators.
 //
 // One thread-block cluster of C CTAs reconstructs one scan; a grid of G
 // clusters reconstructs G independent scans.  The cluster walks the positions
 // of one iteration in the order the host drew (PtyLab/Engines/BaseEngine.py:637-665)
 // and, for each position, runs the body of ePIE.py:84-105 / mPIE.py:280-332 /
-// qNewton.py:69-90 as passes separated by cluster barriers.  CTA c owns rows
+// qNewton.py:69-90 / mqNewton.py:95-126 as passes separated by cluster barriers.  CTA c owns rows
 // [c*L, (c+1)*L) of every row pass and Fourier-layout columns [c*L, (c+1)*L)
 // of every column pass (L = Np/C), so it always updates the same probe rows
 // and keeps them in shared memory for the whole launch.
@@ -31,6 +31,8 @@
 //      * frac / Np^2, inverse column FFT; write back
 //   C  tasks: inverse row FFT, [sign], [conj chirp], DELTA = eswUpdate - esw;
 //      pixels: object and probe steps (qNewton: whole-object max first)
+//   M  mqNewton: gradient norms; adaptive-momentum step over the whole object
+//      (tiles spread over the cluster) and the CTA's probe rows
 // ASP replaces B by transfer-function column passes around a real-space
 // projection row pass (Operators.py:155-230).
 #include "ptyg_engine_dev.cuh"
@@ -66,6 +68,7 @@ struct Smem {
   unsigned* slots;  // 2 * RED_BANK norm slots (used on rank 0)
   double* redD;     // 32
   float* redF;      // 4 * 32
+  double* part;     // 32: mqNewton gradient-norm partials, [0,C) object, [C,2C) probe (rank 0)
 };
 
 __host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int nosm, int npsm, bool qn,
@@ -94,6 +97,8 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   const bool fresnel = a.prop == PROP_FRESNEL;
   const bool asp = a.prop == PROP_ASP;
   const int eng = a.engine;
+  const bool qn = eng == ENG_QNEWTON || eng == ENG_MQNEWTON;
+  const bool mq = eng == ENG_MQNEWTON;
   const size_t No2 = (size_t)No * No;
   const int blk0 = asp ? line0 : sx0;
 
@@ -108,11 +113,12 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   sm.tile = sm.obj + nosm * LN;
   sm.rows = sm.tile + K * NP * ld;
   sm.U = sm.rows + K * LN;
-  sm.fr = reinterpret_cast<float*>(sm.U + (eng == ENG_QNEWTON ? npsm * LN : 0));
+  sm.fr = reinterpret_cast<float*>(sm.U + (qn ? npsm * LN : 0));
   sm.dat = sm.fr + LN;
   sm.slots = reinterpret_cast<unsigned*>(sm.dat + 2 * LN);
   sm.redD = reinterpret_cast<double*>(sm.slots + 2 * RED_BANK);
   sm.redF = reinterpret_cast<float*>(sm.redD + 32);
+  sm.part = reinterpret_cast<double*>(sm.redF + 4 * 32);
   unsigned* slots0 = dsmem(sm.slots, 0);
 
   if (psm) {
@@ -125,7 +131,13 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   prefetch_data<NP, L>(a, s, sm.dat, 0, blk0);
   WarpFFT<E> F;
   F.init(a.twiddle, lane);
-  if (eng == ENG_QNEWTON) {
+  // mqNewton second moments: every CTA of the cluster carries the same values
+  float vO = 0.f, vP = 0.f;
+  if (mq && s.moment2) {
+    vO = s.moment2[0];
+    vP = s.moment2[1];
+  }
+  if (qn) {
     // all tile maxima once per launch
     const int nt = a.tilesPerRow * a.tilesPerRow;
     for (int t = crank * nw + warp; t < nt; t += C * nw) {
@@ -314,6 +326,7 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
     __syncthreads();
 
     // ---------------- C: object and probe steps, pixel by pixel
+    float gsqO = 0.f, gsqP = 0.f;  // mqNewton: sum |objectBuffer - object|^2, same for the probe
     {
       const float pmax2 = slot_value(red, RED_PMAX2);
       const float omax2 = slot_value(red, RED_OMAX2);
@@ -358,21 +371,32 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
               accP = cadd(accP, cscale(cmulc(O[o], d), gP[o]));
             }
           }
-          if (eng == ENG_QNEWTON)
+          if (qn)
             sm.U[p * LN + i] = accP;
           else
             sm.probe[p * pst + i] = cadd(P, cscale(accP, stepP));
         }
         const int l = i / NP, x = i - (i / NP) * NP;
 #pragma unroll
-        for (int o = 0; o < MAX_OBJECT_MODES; ++o)
-          if (o < nosm)
-            st_cg(s.object + o * No2 + (size_t)(row0 + line0 + l) * No + col0 + x,
-                  cadd(O[o], cscale(accO[o], a.betaO)));
+        for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
+          if (o < nosm) {
+            const float2 On = cadd(O[o], cscale(accO[o], a.betaO));
+            st_cg(s.object + o * No2 + (size_t)(row0 + line0 + l) * No + col0 + x, On);
+            if (mq) {
+              // gradient = objectBuffer - object (mqNewton.py:190): the buffer
+              // equals the object after every momentum step (nothing between
+              // positions or iterations touches one without the other), so
+              // it is the patch as it was before this step; kept for pass M
+              const float2 g = csub(O[o], On);
+              sm.obj[o * LN + i] = g;
+              gsqO += g.x * g.x + g.y * g.y;
+            }
+          }
+        }
       }
     }
 
-    if (eng == ENG_QNEWTON) {
+    if (qn) {
       // max over the whole object of sum_o |O_o| after the object step
       // (qNewton.py:130), kept exactly with per-tile maxima: only the tiles
       // the patch touched are recomputed, the others are read back.
@@ -398,7 +422,115 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
       const float scale = a.betaP / slot_value(red, RED_OMAXW);
       for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
         const int p = i / LN, rem = i - (i / LN) * LN;
-        sm.probe[p * pst + rem] = cadd(sm.probe[p * pst + rem], cscale(sm.U[i], scale));
+        const float2 Pn = cadd(sm.probe[p * pst + rem], cscale(sm.U[i], scale));
+        sm.probe[p * pst + rem] = Pn;
+        if (mq) {
+          // probeBuffer - probe (mqNewton.py:211); the buffer is read, not
+          // assumed: the probe constraints between iterations move the probe
+          // but not its buffer
+          const float2 g = csub(s.probeBuffer[(size_t)p * NP * NP + (size_t)line0 * NP + rem], Pn);
+          sm.U[i] = g;
+          gsqP += g.x * g.x + g.y * g.y;
+        }
+      }
+    }
+
+    if (mq) {
+      // ---------------- M: adaptive momentum (mqNewton.py:142-224) after every
+      // position, on the whole object and probe, in the reference's complex64
+      // rounding order: NumPy divides complex64 by a real-valued complex as a
+      // product with the correctly rounded reciprocal, hence __frcp_rn.
+      {
+        const double so = block_sum((double)gsqO, sm.redD);
+        __syncthreads();
+        const double sp = block_sum((double)gsqP, sm.redD);
+        if (threadIdx.x == 0) {
+          double* dst = dsmem(sm.part, 0);
+          dst[crank] = so;
+          dst[C + crank] = sp;
+        }
+      }
+      cluster_sync(C);
+      double tot;
+      {
+        // lanes [0,C) hold the object partials, [C,2C) the probe ones; the
+        // xor butterfly sums each group in the same order in every warp and CTA
+        const double* src = dsmem(sm.part, 0);
+        tot = (int)lane < 2 * C ? src[lane] : 0.0;
+#pragma unroll
+        for (int off = 1; off < C; off <<= 1) tot += __shfl_xor_sync(0xffffffffu, tot, off);
+      }
+      const double nsqO = __shfl_sync(0xffffffffu, tot, 0), nsqP = __shfl_sync(0xffffffffu, tot, C);
+      const int method = a.momentum;
+      const float rb1 = __frcp_rn(a.b1s);
+      float rdO = 1.f, rdP = 1.f;
+      if (method != MOM_PLAIN) {
+        // vt = beta2*vt + (1-beta2)*||grad||^2 ; 1/(sqrt(vt/(1-beta2^itr)) + 1e-8)
+        const float rb2 = __frcp_rn(a.b2s);
+        const float nO = __fsqrt_rn((float)nsqO), nP = __fsqrt_rn((float)nsqP);
+        vO = __fadd_rn(__fmul_rn(a.b2, vO), __fmul_rn(a.omb2, __fmul_rn(nO, nO)));
+        vP = __fadd_rn(__fmul_rn(a.b2, vP), __fmul_rn(a.omb2, __fmul_rn(nP, nP)));
+        rdO = __frcp_rn(__fadd_rn(__fsqrt_rn(__fmul_rn(vO, rb2)), 1e-8f));
+        rdP = __frcp_rn(__fadd_rn(__fsqrt_rn(__fmul_rn(vP, rb2)), 1e-8f));
+      }
+      // one component: first moment m (updated in place), returns X - beta_m*update
+      auto step1 = [&](float X, float g, float& m, float rd, float beta_m) {
+        float u;
+        if (method == MOM_PLAIN) {
+          m = __fadd_rn(g, __fmul_rn(a.frictionM, m));  // mqNewton.py:176-182
+          u = m;
+        } else {
+          m = __fadd_rn(__fmul_rn(a.b1, m), __fmul_rn(a.omb1, g));
+          const float mh = __fmul_rn(m, rb1);
+          if (method == MOM_ADAM)
+            u = __fmul_rn(mh, rd);  // mqNewton.py:142-153
+          else                      // mqNewton.py:155-174
+            u = __fmul_rn(__fadd_rn(__fmul_rn(a.b1, mh), __fmul_rn(__fmul_rn(g, a.omb1), rb1)), rd);
+        }
+        return __fsub_rn(X, __fmul_rn(beta_m, u));
+      };
+      // object: TILE x TILE tiles spread over the cluster's warps; the patch
+      // gradient is read from the row owners' shared memory; tile maxima of
+      // sum_o |O_o| are refreshed for the next position's probe step
+      const int nt = a.tilesPerRow * a.tilesPerRow;
+      for (int t = crank * nw + warp; t < nt; t += C * nw) {
+        const int ty = t / a.tilesPerRow, tx = t - ty * a.tilesPerRow;
+        float mx = 0.f;
+#pragma unroll 2
+        for (int q = 0; q < TILE * TILE / 32; ++q) {
+          const int idx = q * 32 + lane;
+          const int y = ty * TILE + idx / TILE, x = tx * TILE + idx % TILE;
+          if (y < No && x < No) {
+            const int r = y - row0, c = x - col0;
+            const bool in = (unsigned)r < (unsigned)NP && (unsigned)c < (unsigned)NP;
+            const float2* gsrc = in ? dsmem(sm.obj, r / L) + (r % L) * NP + c : nullptr;
+            float sum = 0.f;
+            for (int o = 0; o < nosm; ++o) {
+              const size_t gi = (size_t)o * No2 + (size_t)y * No + x;
+              const float2 g = in ? gsrc[o * LN] : make_float2(0.f, 0.f);
+              const float2 X = ld_cg(s.object + gi);
+              float2 M = ld_cg(s.objectMomentum + gi);
+              const float2 Xn = make_float2(step1(X.x, g.x, M.x, rdO, a.betaOm), step1(X.y, g.y, M.y, rdO, a.betaOm));
+              st_cg(s.objectMomentum + gi, M);
+              st_cg(s.object + gi, Xn);
+              sum += cabs(Xn);
+            }
+            mx = fmaxf(mx, sum);
+          }
+        }
+        mx = warp_max(mx);
+        if (lane == 0) s.tileMax[t] = mx;
+      }
+      // probe: the CTA's own rows
+      for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
+        const int p = i / LN, rem = i - (i / LN) * LN;
+        const size_t gi = (size_t)p * NP * NP + (size_t)line0 * NP + rem;
+        const float2 P = sm.probe[p * pst + rem], g = sm.U[i];
+        float2 M = s.probeMomentum[gi];
+        const float2 Pn = make_float2(step1(P.x, g.x, M.x, rdP, a.betaPm), step1(P.y, g.y, M.y, rdP, a.betaPm));
+        s.probeMomentum[gi] = M;
+        s.probeBuffer[gi] = Pn;
+        sm.probe[p * pst + rem] = Pn;
       }
     }
 
@@ -436,6 +568,10 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
   }
   cp_async_wait_all();
   __syncthreads();
+  if (mq && s.moment2 && crank == 0 && threadIdx.x == 0) {
+    s.moment2[0] = vO;
+    s.moment2[1] = vP;
+  }
 
   if (psm) {
     for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
@@ -451,9 +587,10 @@ __global__ void __launch_bounds__(512, 1) engine_kernel(const EngineArgs a) {
 size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine, bool probe_in_smem) {
   const int L = Np / C;
   const size_t LN = (size_t)L * Np;
-  const size_t n = smem_complex_elems(Np, L, nosm * npsm, nosm, npsm, engine == ENG_QNEWTON, probe_in_smem);
+  const bool qn = engine == ENG_QNEWTON || engine == ENG_MQNEWTON;
+  const size_t n = smem_complex_elems(Np, L, nosm * npsm, nosm, npsm, qn, probe_in_smem);
   return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
-         4 * 32 * sizeof(float) + 64;
+         4 * 32 * sizeof(float) + 32 * sizeof(double) + 64;
 }
 
 static cudaLaunchConfig_t launch_config(int cluster, int grid, int threads, size_t smem, cudaStream_t st,

@@ -6,7 +6,8 @@
 
 namespace ptyg {
 
-enum Engine { ENG_EPIE = 0, ENG_MPIE = 1, ENG_QNEWTON = 2, ENG_E3PIE = 3 };
+enum Engine { ENG_EPIE = 0, ENG_MPIE = 1, ENG_QNEWTON = 2, ENG_E3PIE = 3, ENG_MQNEWTON = 4 };
+enum Momentum { MOM_PLAIN = 0, MOM_ADAM = 1, MOM_NADAM = 2 };
 
 // Object modes the pixel-update loop carries in registers.
 constexpr int MAX_OBJECT_MODES = 4;
@@ -43,7 +44,8 @@ struct ScanDev {
   float* detErr;           // optional [frame][Np*Np] |I_meas - I_est| (data layout)
   unsigned* red;           // 2 * RED_BANK reduction slots
   int* status;             // 0 = ok, else first error code seen
-  float* tileMax;          // qNewton: max of sum_o |O_o| per TILE x TILE object tile
+  float* tileMax;          // qNewton/mqNewton: max of sum_o |O_o| per TILE x TILE object tile
+  float* moment2;          // mqNewton ADAM/NADAM: {v_object, v_probe}
 };
 
 // Side of the object tiles whose maxima qNewton keeps up to date.
@@ -63,6 +65,9 @@ struct EngineArgs {
   int tilesPerRow;         // ceil(No / TILE)
   int probeInSmem;         // keep the CTA's probe rows in shared memory
   float betaO, betaP, alphaO, alphaP, regO, regP, frictionM, feedbackM, weightP, bethSlice;
+  // mqNewton: method, float32 beta1, 1-beta1, beta2, 1-beta2, 1-beta^itr, step sizes
+  int momentum;
+  float b1, omb1, b2, omb2, b1s, b2s, betaOm, betaPm;
 };
 
 }  // namespace ptyg

@@ -18,9 +18,13 @@ What it writes, all under ``tests/golden/``:
   likewise checked against ``propagator_<name>.npz``.
 * ``scan_<name>.npz`` -- cases the regression dataset cannot exercise (its 16
   frames all round to one pixel position): a Fermat-spiral CPM scan with
-  random position order, mPIE momentum, mixed states, orthogonalisation,
-  fftshiftSwitch, Fresnel/ASP, multislice, and an FPM LED-array scan with
-  'NA' order and probeBoundary.  These are outputs of the unmodified reference.
+  random position order, mPIE momentum, mqNewton (ADAM, NADAM, plain
+  momentum), mixed states, orthogonalisation, fftshiftSwitch, Fresnel/ASP,
+  multislice, and an FPM LED-array scan with 'NA' order and probeBoundary.
+  These are outputs of the unmodified reference.
+
+``--only NAME [NAME ...]`` rewrites just those fixtures (file stems such as
+``scan_mqnewton_adam``); the others are left untouched.
 
 Every fixture stores its inputs (ptychogram, encoder, geometry scalars, the
 seeded initial object/probe, pixel positions) and outputs (object, probe, error
@@ -205,6 +209,11 @@ def run_case(ref, d, case):
     engine.numIterations = case["iters"]
     for k, v in case.get("engine_attrs", {}).items():
         setattr(engine, k, v)
+    if case.get("engine_attrs", {}).get("momentum_method") == "momentum":
+        # mqNewton's plain-momentum method passes objectMomentum_v through
+        # untouched, but reads it (mqNewton.py:188-199): give it one
+        rec.objectMomentum_v = np.zeros_like(rec.object)
+        rec.probeMomentum_v = np.zeros_like(rec.probe)
     positions = np.asarray(rec.positions).copy()
     # record the order each iteration used: 'NA' is np.argsort of LED distances,
     # whose tie order differs between NumPy's x86 and Arm sort kernels
@@ -241,9 +250,15 @@ def run_case(ref, d, case):
         error=np.asarray(rec.error, dtype=np.float64),
         errorAtPos=np.asarray(rec.errorAtPos, dtype=np.float64),
     )
-    if case["engine"] == "mPIE":
+    if case["engine"] in ("mPIE", "mqNewton"):
         outputs["objectMomentum"] = np.asarray(rec.objectMomentum)
         outputs["probeMomentum"] = np.asarray(rec.probeMomentum)
+    if case["engine"] == "mqNewton":
+        outputs["objectBuffer"] = np.asarray(rec.objectBuffer)
+        outputs["probeBuffer"] = np.asarray(rec.probeBuffer)
+        if case.get("engine_attrs", {}).get("momentum_method", "ADAM") != "momentum":
+            outputs["objectMomentum_v"] = np.asarray(rec.objectMomentum_v)
+            outputs["probeMomentum_v"] = np.asarray(rec.probeMomentum_v)
     if case.get("keep_detector_error", False):
         outputs["detectorError"] = np.asarray(rec.detectorError, dtype=np.float64)
     return inputs, outputs
@@ -311,11 +326,26 @@ SCAN_CONFIGS = {
     "qnewton": dict(engine="qNewton", order="random", iters=3),
     "e3pie": dict(engine="e3PIE", modes=(1, 1, 1, 3), iters=3, dz=2e-4),
     "e3pie_asp": dict(engine="e3PIE", propagator="ASP", modes=(1, 1, 1, 2), iters=2, dz=2e-4),
+    "mqnewton_adam": dict(engine="mqNewton", order="random", iters=3),
+    "mqnewton_nadam_orth": dict(
+        engine="mqNewton",
+        order="random",
+        modes=(1, 1, 2, 1),
+        iters=4,
+        engine_attrs=dict(momentum_method="NADAM"),
+        params=dict(orthogonalizationSwitch=True, orthogonalizationFrequency=2),
+    ),
+    "mqnewton_momentum": dict(engine="mqNewton", iters=3, engine_attrs=dict(momentum_method="momentum")),
 }
 
 FPM_CONFIGS = {
     "qnewton_fpm": dict(engine="qNewton", order="NA", iters=3, params=dict(probeBoundary=True)),
     "mpie_fpm": dict(engine="mPIE", order="NA", iters=3, params=dict(probeBoundary=True)),
+    # the FPM example's engine (example_scripts/exampleReconstructionFPM.py:66-75)
+    "mqnewton_nadam_fpm": dict(
+        engine="mqNewton", order="NA", iters=3, engine_attrs=dict(momentum_method="NADAM"),
+        params=dict(probeBoundary=True),
+    ),
 }
 
 
@@ -323,7 +353,9 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("reference", help="path to the PtyLab.py source tree")
     ap.add_argument("--out", default=str(HERE))
+    ap.add_argument("--only", nargs="*", default=None, help="fixture stems to (re)write")
     args = ap.parse_args()
+    wanted = (lambda stem: True) if not args.only else (lambda stem: stem in args.only)
 
     from refload import load_reference
 
@@ -358,6 +390,8 @@ def main():
 
     d = regression_dataset()
     for name, case in REG_CONFIGS.items():
+        if not wanted(f"reg_{name}"):
+            continue
         inputs, outputs = run_case(ref, d, case)
         g = np.load(gold / f"{name}.npz")
         for key in g.files:
@@ -368,6 +402,8 @@ def main():
         print(f"reg_{name}: matches {gold.name}/{name}.npz exactly")
 
     for prop in ("fraunhofer", "fresnel", "asp"):
+        if not wanted(f"prop_{prop}"):
+            continue
         inputs, outputs = run_propagator(ref, d, prop)
         g = np.load(gold / f"propagator_{prop}.npz")
         for key in g.files:
@@ -379,12 +415,16 @@ def main():
 
     ds = fermat_scan_dataset()
     for name, case in SCAN_CONFIGS.items():
+        if not wanted(f"scan_{name}"):
+            continue
         inputs, outputs = run_case(ref, ds, case)
         save(out / f"scan_{name}.npz", _meta(case, ds), inputs, outputs)
         print(f"scan_{name}: recorded (error {outputs['error'][-1]:.5g})")
 
     df = fpm_dataset()
     for name, case in FPM_CONFIGS.items():
+        if not wanted(f"scan_{name}"):
+            continue
         inputs, outputs = run_case(ref, df, case)
         save(out / f"scan_{name}.npz", _meta(case, df), inputs, outputs)
         print(f"scan_{name}: recorded (error {outputs['error'][-1]:.5g})")
@@ -409,6 +449,7 @@ def _meta(case, d):
         zled=d.get("zled", 0.0),
         magnification=d.get("magnification", 0.0),
         NA=d.get("NA", 0.0),
+        momentum_method=case.get("engine_attrs", {}).get("momentum_method", "ADAM"),
     )
 
 

@@ -38,6 +38,8 @@ def run_fixture_gpu(fx, engine_name=None, iters=None):
     rec.probe = i["init_probe"].copy()
     eng = getattr(Engines, engine_name or str(m["engine"]))(rec, d, p, DummyMonitor())
     eng.numIterations = int(m["iters"]) if iters is None else iters
+    if "momentum_method" in m and str(m["engine"]) == "mqNewton":
+        eng.momentum_method = str(m["momentum_method"])
     np.random.seed(int(m["seed"]))
     eng.reconstruct()
     return rec, eng
@@ -80,6 +82,17 @@ def test_engine_matches_reference_fixture(torch_cuda, name):
     if "objectMomentum" in target:
         assert rel_err(rec.objectMomentum, target["objectMomentum"]) < max(1e-2, 3 * floor["object"])
         assert rel_err(rec.probeMomentum, target["probeMomentum"]) < max(1e-2, 3 * floor["probe"])
+    if str(fx["meta_engine"]) == "mqNewton":
+        # the object buffer equals the final object; the probe buffer is the
+        # probe before the last iteration's constraints; the second moments
+        # are uniform arrays
+        np.testing.assert_array_equal(rec.objectBuffer, rec.object)
+        if "out_probeBuffer" in fx and platform_reproduces_order(fx):
+            assert rel_err(rec.probeBuffer, fx["out_probeBuffer"]) < max(TOL_FIXTURE, 3 * floor["probe"])
+        for key, part in (("objectMomentum_v", "object"), ("probeMomentum_v", "probe")):
+            if f"out_{key}" in fx and platform_reproduces_order(fx):
+                assert getattr(rec, key).shape == fx[f"out_{key}"].shape
+                assert rel_err(getattr(rec, key), fx[f"out_{key}"]) < max(1e-2, 3 * floor[part]), key
 
 
 def test_engine_runs_are_deterministic(torch_cuda):
@@ -256,6 +269,42 @@ def test_config3_fpm_qnewton_precision_vs_complex128(torch_cuda):
     print(msg)
     for k in keys:
         assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 5e-4, msg
+
+
+def test_config3_fpm_mqnewton_nadam_precision_vs_complex128(torch_cuda):
+    """The FPM example's engine (mqNewton, NADAM, beta1 = beta2 = 0.5,
+    exampleReconstructionFPM.py:66-75) at the LED-array configuration, 3
+    iterations: every position adds a momentum step over the whole 512 x 512
+    spectrum.  The GB300 result is as close to a complex128 oracle run as the
+    reference's complex64 path."""
+    from oracle import ptyoracle as O
+    from ptylab_gb300 import DummyMonitor, Engines
+    from ptylab_gb300.simulate import FPMSpec, fpm_problem
+
+    d, p, rec, _, _ = fpm_problem(FPMSpec())
+    obj0, prb0 = rec.object.copy(), rec.probe.copy()
+    positions = rec.positions.copy()
+    eng = Engines.mqNewton(rec, d, p, DummyMonitor())
+    eng.momentum_method = "NADAM"
+    eng.numIterations = 3
+    eng.reconstruct()
+    g = O.Geometry(Np=128, No=512, dxp=rec.dxp, wavelength=rec.wavelength, zo=rec.zo)
+    s = O.Settings(engine="mqNewton", momentum_method="NADAM", order="NA", operationMode="FPM",
+                   probeBoundary=True, entrancePupilDiameter=d.entrancePupilDiameter)
+
+    def oracle(cdt, fdt):
+        st = O.State(object=obj0.astype(cdt), probe=prb0.astype(cdt))
+        return O.OracleEngine(s, g, st, d.ptychogram.astype(fdt), positions, d.energyAtPos).reconstruct(3)
+
+    r64, r128 = oracle(np.complex64, np.float32), oracle(np.complex128, np.float64)
+    keys = ("object", "probe", "error", "objectMomentum", "probeMomentum")
+    gpu_vs_128 = {k: rel_err(getattr(rec, k), getattr(r128, k)) for k in keys}
+    ref_vs_128 = {k: rel_err(getattr(r64, k), getattr(r128, k)) for k in keys}
+    msg = f"mqNewton FPM: gpu-c128 {gpu_vs_128} ref-c128 {ref_vs_128}"
+    print(msg)
+    for k in keys:
+        assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 5e-4, msg
+    assert rel_err(rec.objectMomentum_v, r128.objectMomentum_v) <= 3 * rel_err(r64.objectMomentum_v, r128.objectMomentum_v) + 1e-4
 
 
 def _run_plan_c1(torch, cluster, nf=40, iters=3):

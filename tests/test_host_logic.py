@@ -107,3 +107,29 @@ def test_multislice_transfer_function_matches_the_oracle():
     np.testing.assert_array_equal(
         _tables.multislice_tf(dz, lam, n, Np, Np * dxp), O.aspw_transfer_function(dz, lam / n, Np, Np * dxp)
     )
+
+
+def test_mqnewton_host_logic():
+    """mqNewton.py:50-79: defaults, the method lookup, and the second moments
+    the kernel carries as scalars (uniform real arrays)."""
+    from ptylab_gb300 import DummyMonitor, Engines
+
+    fx = load_fixture("scan_mqnewton_adam")
+    m, i, d, p, rec = containers(fx)
+    rec.object, rec.probe = i["init_object"].copy(), i["init_probe"].copy()
+    rec.initialGuessObject, rec.initialGuessProbe = rec.object.copy(), rec.probe.copy()
+    eng = Engines.mqNewton(rec, d, p, DummyMonitor())
+    assert (eng.beta1, eng.beta2, eng.betaObject_m, eng.betaProbe_m, eng.momentum_method) == (0.5, 0.5, 0.25, 0.25, "ADAM")
+    assert p.momentumAcceleration
+    np.testing.assert_array_equal(rec.objectBuffer, rec.object)
+    assert not np.any(rec.objectMomentum) and rec.objectMomentum.shape == rec.object.shape
+    eng.initializeAdaptiveMomentum()
+    assert eng._second_moments() == [0.0, 0.0]
+    rec.objectMomentum_v = np.full(rec.object.shape, np.complex64(0.25))
+    assert eng._second_moments()[0] == 0.25
+    rec.objectMomentum_v.flat[3] = 1.0  # what a second reconstruct() produces
+    with pytest.raises(NotImplementedError):
+        eng._second_moments()
+    eng.momentum_method = "Adagrad"
+    with pytest.raises(AttributeError):
+        eng.initializeAdaptiveMomentum()
