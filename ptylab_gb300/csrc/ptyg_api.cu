@@ -245,10 +245,12 @@ static void plan_free(ptyg_plan* p) {
   delete p;
 }
 
-// One warp per 1D-transform task of a pass (K modes x L lines), 4..16 warps.
+// One warp per 1D-transform task of a pass (K modes x L lines), 4..16 warps
+// (mqNewton: 8, the bound its kernel is compiled for).
 static int engine_threads(const ptyg_geometry& g, int C) {
   const int tasks = g.nosm * g.npsm * (g.Np / C);
-  const int w = tasks < 4 ? 4 : (tasks > 16 ? 16 : tasks);
+  const int wmax = g.engine == PTYG_MQNEWTON ? 8 : 16;
+  const int w = tasks < 4 ? 4 : (tasks > wmax ? wmax : tasks);
   return 32 * w;
 }
 
@@ -311,7 +313,7 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
       if ((int)p->smem > maxSmem) continue;
       int nclusters = 0;
       cudaError_t e = e3 ? ptyg::e3pie_max_clusters(g.Np, c, p->threads, p->smem, &nclusters)
-                         : ptyg::engine_max_clusters(g.Np, g.nosm, g.npsm, c, p->threads, p->smem, &nclusters);
+                         : ptyg::engine_max_clusters(g.Np, g.engine, c, p->threads, p->smem, &nclusters);
       if (e != cudaSuccess) {
         cudaGetLastError();
         continue;
@@ -454,6 +456,7 @@ extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffe
   d.status = o.status;
   d.tileMax = o.tileMax;
   d.moment2 = b->second_moment;
+  d.vec4 = p->g.No % 2 == 0 && ((uintptr_t)b->object % 16) == 0 && ((uintptr_t)b->object_momentum % 16) == 0;
   o.bound = true;
   o.orderLen = p->g.num_frames;
   PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &d, sizeof(ScanDev), cudaMemcpyHostToDevice, st), "scan upload");
@@ -567,7 +570,7 @@ extern "C" int ptyg_plan_info(ptyg_plan* p, int* cluster, int* threads, int* sme
   if (smem_bytes) *smem_bytes = (int)p->smem;
   if (max_active_clusters) {
     int n = 0;
-    cudaError_t e = ptyg::engine_max_clusters(p->g.Np, p->g.nosm, p->g.npsm, p->C, p->threads, p->smem, &n);
+    cudaError_t e = ptyg::engine_max_clusters(p->g.Np, p->g.engine, p->C, p->threads, p->smem, &n);
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveClusters");
     *max_active_clusters = n;
   }

@@ -46,6 +46,7 @@ struct ScanDev {
   int* status;             // 0 = ok, else first error code seen
   float* tileMax;          // qNewton/mqNewton: max of sum_o |O_o| per TILE x TILE object tile
   float* moment2;          // mqNewton ADAM/NADAM: {v_object, v_probe}
+  int vec4;                // No even and object / objectMomentum 16-byte aligned: 16-byte accesses
 };
 
 // Side of the object tiles whose maxima qNewton keeps up to date.

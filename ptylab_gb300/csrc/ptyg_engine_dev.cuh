@@ -69,6 +69,27 @@ PTYG_DEV void block_max_to_slots(float (&v)[NV], float* scratch, unsigned* slots
   }
 }
 
+// Sum NV values over the CTA (scratch: NV * 32 doubles); thread 0 receives
+// the results in v.  Fixed order, so every run gives the same bits.
+template <int NV>
+PTYG_DEV void block_sum_n(double (&v)[NV], double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const double w = warp_sum(v[i]);
+    if (lane == 0) scratch[i * 32 + warp] = w;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t += scratch[i * 32 + w];
+      v[i] = t;
+    }
+  }
+}
+
 // Sum over the CTA; thread 0 receives the result.
 PTYG_DEV double block_sum(double v, double* scratch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;

@@ -1,4 +1,4 @@
-// Host-callable launchers of ptyg_ops.cu and ptyg_engine.cu.
+// Host-callable launchers of ptyg_ops.cu, ptyg_engine.cu, ptyg_engine_mq.cu and ptyg_e3pie.cu.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -55,6 +55,8 @@ bool engine_shape_supported(int Np, int cluster);
 size_t e3pie_smem_bytes(int Np, int C, int npsm);
 cudaError_t e3pie_max_clusters(int Np, int cluster, int threads, size_t smem, int* out);
 cudaError_t launch_e3pie(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
-cudaError_t engine_max_clusters(int Np, int nosm, int npsm, int cluster, int threads, size_t smem, int* out);
+cudaError_t engine_max_clusters(int Np, int engine, int cluster, int threads, size_t smem, int* out);
+cudaError_t engine_max_clusters_mq(int Np, int cluster, int threads, size_t smem, int* out);
+cudaError_t launch_engine_mq(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 
 }  // namespace ptyg

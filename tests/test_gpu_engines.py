@@ -307,6 +307,82 @@ def test_config3_fpm_mqnewton_nadam_precision_vs_complex128(torch_cuda):
     assert rel_err(rec.objectMomentum_v, r128.objectMomentum_v) <= 3 * rel_err(r64.objectMomentum_v, r128.objectMomentum_v) + 1e-4
 
 
+@pytest.mark.parametrize("pad", [0, 1])
+@pytest.mark.parametrize("method", ["ADAM", "NADAM", "momentum"])
+def test_mqnewton_positions_match_oracle(torch_cuda, pad, method):
+    """mqNewton's kernel position by position through the C ABI: the first
+    eight positions of an iteration against the oracle stepping through the
+    same positions.  Whole iterations of these CPM scans are chaotic (a 1-ulp
+    change of the initial object moves the result by 1e-2 after three
+    iterations, in the reference too), so the arithmetic is pinned here before
+    rounding differences can grow.  pad=1 grows the object by one row and
+    column: an odd size takes the 8-byte path of the momentum step, an even
+    one the 16-byte path."""
+    torch = torch_cuda
+    from oracle import ptyoracle as O
+    from ptylab_gb300 import _native
+
+    fx = load_fixture("scan_mqnewton_adam")
+    i = {k[3:]: fx[k] for k in fx if k.startswith("in_")}
+    Np, No = int(i["Np"]), int(i["No"]) + pad
+    obj0 = np.ones((1, 1, 1, 1, No, No), np.complex64)
+    obj0[..., : No - pad, : No - pad] = i["init_object"]
+    prb0 = i["init_probe"].astype(np.complex64)
+    data = i["ptychogram"].astype(np.float32)
+    positions = i["positions"].astype(np.int32)
+    nf, npos = data.shape[0], 8
+    order = np.arange(nf, dtype=np.int32)
+
+    lib = _native.require(0)
+    geom = _native.Geometry(Np=Np, No=No, nosm=1, npsm=1, nslice=1, num_frames=nf, num_scans=1,
+                            engine=_native.ENGINES["mqNewton"], propagator=0, fftshift=0, fpm=0, cluster=0)
+    plan = C.c_void_p()
+    _native.check(lib.ptyg_plan_create(C.byref(geom), C.byref(plan)))
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    t = dict(obj=dev(obj0), prb=dev(prb0), pos=dev(positions), order=dev(order), data=dev(data))
+    t.update(omom=torch.zeros_like(t["obj"]), pbuf=t["prb"].clone(), pmom=torch.zeros_like(t["prb"]),
+             m2=torch.zeros(2, dtype=torch.float32, device="cuda"))
+    b = _native.ScanBuffers(object=t["obj"].data_ptr(), probe=t["prb"].data_ptr(), positions=t["pos"].data_ptr(),
+                            order=t["order"].data_ptr(), object_momentum=t["omom"].data_ptr(),
+                            probe_buffer=t["pbuf"].data_ptr(), probe_momentum=t["pmom"].data_ptr(),
+                            second_moment=t["m2"].data_ptr())
+    _native.check(lib.ptyg_plan_bind_scan(plan, 0, C.byref(b), t["data"].data_ptr(), None))
+    u = _native.UpdateParams(beta_object=1, beta_probe=1, reg_object=1, reg_probe=1, friction=0.7, probe_weight=1,
+                             momentum_method=_native.MOMENTUM_METHODS[method], beta1=0.5, beta2=0.5,
+                             beta1_scale=0.5, beta2_scale=0.5, beta_object_m=0.25, beta_probe_m=0.25)
+    _native.check(lib.ptyg_plan_run(plan, C.byref(u), 0, npos, 0, None))
+    torch.cuda.synchronize()
+    st_gpu = C.c_int()
+    _native.check(lib.ptyg_plan_status(plan, 0, C.byref(st_gpu), None))
+    lib.ptyg_plan_destroy(plan)
+    assert st_gpu.value == 0
+    gpu = {k: t[n].cpu().numpy() for k, n in (("object", "obj"), ("probe", "prb"), ("objectMomentum", "omom"),
+                                              ("probeMomentum", "pmom"))}
+
+    def oracle(cdt, fdt):
+        g = O.Geometry(Np=Np, No=No, dxp=float(i["dxp"]), wavelength=float(i["wavelength"]), zo=float(i["zo"]))
+        s = O.Settings(engine="mqNewton", momentum_method=method, entrancePupilDiameter=float(i["entrancePupilDiameter"]))
+        st = O.State(object=obj0.astype(cdt), probe=prb0.astype(cdt))
+        eng = O.OracleEngine(s, g, st, data.astype(fdt), positions, i["energyAtPos"])
+        eng.prepare()
+        if method != "momentum":
+            st.objectMomentum_v = np.zeros_like(st.object)
+            st.probeMomentum_v = np.zeros_like(st.probe)
+        for j in order[:npos]:
+            eng.position(int(j))
+        return st
+
+    r64, r128 = oracle(np.complex64, np.float32), oracle(np.complex128, np.float64)
+    errs = {k: rel_err(gpu[k], getattr(r64, k)) for k in gpu}
+    floor = {k: rel_err(getattr(r64, k), getattr(r128, k)) for k in gpu}
+    msg = f"mqNewton {method} No={No}, {npos} positions: gpu-ref {errs} ref-c128 {floor}"
+    print(msg)
+    for k in gpu:
+        assert errs[k] < max(1e-4, 3 * floor[k]), msg
+    assert abs(float(t["m2"][0]) - float(np.real(r64.objectMomentum_v.flat[0]))) <= 1e-4 * abs(
+        float(np.real(r64.objectMomentum_v.flat[0]))) if method != "momentum" else True
+
+
 def _run_plan_c1(torch, cluster, nf=40, iters=3):
     """mPIE, npsm = 4, Np = 128 through the C ABI with a given cluster size."""
     from ptylab_gb300 import _native
