@@ -58,3 +58,46 @@ def test_status_codes_map_to_reference_exceptions():
     assert _native._EXC[_native.PTYG_ERR_INVALID] is ValueError
     assert _native._EXC[_native.PTYG_ERR_UNSUPPORTED] is NotImplementedError
     assert _native._EXC[_native.PTYG_ERR_DEVICE] is ImportError
+
+
+_C_TYPES = {"int32_t": "c_int", "float": "c_float", "double": "c_double"}
+
+
+def declared_structs():
+    """{struct name: [(field, ctype-ish)]} from the typedef'd structs of include/ptyg.h."""
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "ptyg.h").read_text(), flags=re.S)
+    out = {}
+    for name, body in re.findall(r"typedef struct (ptyg_\w+) \{(.*?)\} \1;", text, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            m = re.match(r"(?:const\s+)?(\w+)\s*(\**)\s*(.+)", decl)
+            base, ptr, names = m.groups()
+            for n in names.split(","):
+                n = n.strip()
+                star = ptr or ("*" if n.startswith("*") else "")
+                n = n.lstrip("*").strip()
+                fields.append((n, "c_void_p" if star else _C_TYPES.get(base, base)))
+        out[name] = fields
+    return out
+
+
+@pytest.mark.parametrize(
+    "cname,pyname",
+    [("ptyg_geometry", "Geometry"), ("ptyg_update_params", "UpdateParams"), ("ptyg_scan_buffers", "ScanBuffers"),
+     ("ptyg_multislice", "Multislice")],
+)
+def test_ctypes_structs_match_the_header(cname, pyname):
+    """Field names, order and types of the ctypes mirrors equal the C structs."""
+    import ctypes as C
+
+    from ptylab_gb300 import _native
+
+    want = declared_structs()[cname]
+    got = []
+    for n, t in getattr(_native, pyname)._fields_:
+        kind = {C.c_int32: "c_int", C.c_int: "c_int", C.c_float: "c_float", C.c_double: "c_double"}.get(t, "c_void_p")
+        got.append((n, kind))
+    assert got == want
