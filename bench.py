@@ -156,6 +156,12 @@ def algorithmic_counts(flags_per_step, nscans):
     return float(bytes_), float(flops), float(per_pos_bytes), float(per_pos_flops)
 
 
+# DRAM bytes per position of the batched launch, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum of a 15-scan launch / 6000
+# positions; the summary is profiles/engine_kernel_mpie_c1.md)
+TRAFFIC_PER_POSITION = 467_115
+
+
 # ------------------------------------------------------------------ ranks
 def reduce_over_ranks(seconds, units, device=None):
     """Whole-job timing under torch.distributed: the slowest rank's time and
@@ -304,7 +310,9 @@ def run_gb300(args, rank, world, local_rank):
             },
             "roofline": {
                 "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                "frac": achieved_gbs / hbm_peak, "traffic": TRAFFIC_PER_POSITION * G * NPOS, "peak_kind": peak_kind,
+                "traffic_note": "DRAM bytes per launch: ncu dram__bytes_read+write of one 15-scan launch "
+                                "(profiles/engine_kernel_mpie_c1.md) per position, times this launch's positions",
                 "algorithmic_bytes_per_position": per_pos_bytes, "bytes_per_launch": bytes_step,
             },
             "roofline_fp32": {
