@@ -48,6 +48,8 @@ enum ptyg_status {
 enum ptyg_engine { PTYG_EPIE = 0, PTYG_MPIE = 1, PTYG_QNEWTON = 2, PTYG_E3PIE = 3, PTYG_MQNEWTON = 4 };
 /* mqNewton.momentum_method (PtyLab/Engines/mqNewton.py:68-79, 142-182) */
 enum ptyg_momentum { PTYG_MOMENTUM = 0, PTYG_ADAM = 1, PTYG_NADAM = 2 };
+/* params.intensityConstraint (PtyLab/Engines/BaseEngine.py:913-961) */
+enum ptyg_intensity_constraint { PTYG_STANDARD = 0, PTYG_POISSION = 1, PTYG_EXPONENTIAL = 2, PTYG_FLUCTUATION = 3 };
 enum ptyg_propagator { PTYG_FRAUNHOFER = 0, PTYG_FRESNEL = 1, PTYG_ASP = 2 };
 enum ptyg_direction { PTYG_FORWARD = 0, PTYG_INVERSE = 1 };
 
@@ -193,6 +195,36 @@ PTYG_API int ptyg_plan_set_order(ptyg_plan* plan, int scan, const int32_t* order
  * dynamic shared memory per CTA, and how many such clusters can be resident
  * on the device at once (independent scans that run concurrently). */
 PTYG_API int ptyg_plan_info(ptyg_plan* plan, int* cluster, int* threads, int* smem_bytes, int* max_active_clusters);
+
+/* Intensity-projection switches (BaseEngine.intensityProjection,
+ * PtyLab/Engines/BaseEngine.py:870-1012; adaptiveDenoising :1805-1822);
+ * all zero = the standard projection.  Not for e3PIE plans. */
+typedef struct ptyg_projection {
+  int32_t intensity_constraint; /* enum ptyg_intensity_constraint */
+  int32_t adaptive_denoising;   /* params.adaptiveDenoisingSwitch */
+  int32_t background_mode;      /* params.backgroundModeSwitch: I_est += background, updated per position */
+  int32_t fourier_mask;         /* params.FourierMaskSwitch: errors (and the background update) weighted by W */
+  int32_t intensity_mask;       /* params.intensityMask: ESW *= frac * mask + mask - 1 */
+} ptyg_projection;
+
+/* Set the projection switches and their detector tables: W
+ * (experimentalData.W) and intensity_mask (reconstruction.intensity_mask),
+ * device float32 (Np, Np) in the ptychogram's layout (already fftshifted
+ * with it when fftshift), NULL where the switch is off.  Allocates each
+ * scan's background (set to 0.1, BaseEngine.py:361-364) and, for the
+ * fluctuation constraint, its per-frame intensity scaling (set to 1). */
+PTYG_API int ptyg_plan_set_projection(ptyg_plan* plan, const ptyg_projection* projection, const float* W,
+                                      const float* intensity_mask, void* stream);
+
+/* Background of scan `scan` (reconstruction.background), device float32
+ * (Np, Np) in the ptychogram's layout: load it into the plan, or read it out. */
+PTYG_API int ptyg_plan_set_background(ptyg_plan* plan, int scan, const float* background, void* stream);
+PTYG_API int ptyg_plan_get_background(ptyg_plan* plan, int scan, float* background, void* stream);
+
+/* The fluctuation constraint's scaling aleph of each frame as last computed
+ * (params.intensityScaling, BaseEngine.py:913-938), into `host_out`
+ * (num_frames doubles); synchronises. */
+PTYG_API int ptyg_plan_intensity_scaling(ptyg_plan* plan, int scan, double* host_out, void* stream);
 
 /* Process order slots [start, start+count) of every bound scan: for each
  * slot, position order[slot] goes through gather -> propagate -> intensity

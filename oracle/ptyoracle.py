@@ -245,6 +245,12 @@ class Settings:
     frictionM: float = 0.7
     regObject: float = 1.0
     regProbe: float = 1.0
+    # projection switches (Params.py:60-120; BaseEngine.py:870-1012)
+    intensityConstraint: str = "standard"
+    adaptiveDenoisingSwitch: bool = False
+    backgroundModeSwitch: bool = False
+    FourierMaskSwitch: bool = False
+    intensityMask: bool = False
     # mqNewton (mqNewton.py:50-66)
     beta1: float = 0.5
     beta2: float = 0.5
@@ -270,6 +276,8 @@ class State:
     objectMomentum_v: Optional[np.ndarray] = None
     probeMomentum_v: Optional[np.ndarray] = None
     purityProbe: float = 1.0
+    background: Optional[np.ndarray] = None  # backgroundModeSwitch (float64, Np x Np)
+    intensityScaling: Optional[np.ndarray] = None  # 'fluctuation': per-frame scaling (params.intensityScaling)
 
 
 class OracleEngine:
@@ -277,8 +285,11 @@ class OracleEngine:
     qNewton.py:63-99 or e3PIE.py:225-325, with BaseEngine's projection,
     error metrics and the in-scope constraints."""
 
-    def __init__(self, s: Settings, g: Geometry, state: State, ptychogram, positions, energyAtPos, Xp=None, Yp=None):
+    def __init__(self, s: Settings, g: Geometry, state: State, ptychogram, positions, energyAtPos, Xp=None, Yp=None,
+                 W=None, intensity_mask=None):
         self.s = s
+        self.W = W  # experimentalData.W (FourierMaskSwitch)
+        self.intensity_mask = intensity_mask  # reconstruction.intensity_mask (params.intensityMask)
         self.g = g
         self.st = state
         self.ptychogram = np.asarray(ptychogram)
@@ -318,7 +329,11 @@ class OracleEngine:
             raise ValueError("ASP propagatorType works only with fftshiftSwitch = False")
         if s.fftshift and not self.fftshiftFlag:  # _checkFFT BaseEngine.py:405-420
             self.ptychogram = np.fft.ifftshift(self.ptychogram, axes=(-1, -2))
+            if self.W is not None:
+                self.W = np.fft.ifftshift(self.W, axes=(-1, -2))
             self.fftshiftFlag = True
+        if s.backgroundModeSwitch:  # _checkMISC BaseEngine.py:361-364
+            st.background = 1e-1 * np.ones((g.Np, g.Np))
         if s.probePowerCorrectionSwitch:  # BaseEngine.py:227-235
             maxProbePower = np.sqrt(np.max(np.sum(self.ptychogram, (-1, -2))))
             st.probe = st.probe / np.sqrt(np.sum(st.probe * st.probe.conj())) * maxProbePower
@@ -339,26 +354,67 @@ class OracleEngine:
         if st.errorAtPos is None:
             st.errorAtPos = np.zeros((nf, 1), dtype=np.float32)
 
-    # BaseEngine.intensityProjection, standard constraint (BaseEngine.py:870-1012)
+    # BaseEngine.intensityProjection (BaseEngine.py:870-1012) with the
+    # standard / poission / exponential / fluctuation constraints, adaptive
+    # denoising (:1805-1822), the background mode and the Fourier / intensity
+    # masks; NumPy's dtype rules as in the reference (the float64 background
+    # is added in place to the float32 estimate, so the estimate stays float32)
     def intensity_projection(self, j, esw):
-        s = self.s
+        s, st = self.s, self.st
+        gimmel = 1e-10
         ESW = object2detector(esw, s.propagator, s.fftshift, self.g)
         Iest = np.sum(np.abs(ESW) ** 2, axis=(0, 1, 2))[-1]
+        if s.backgroundModeSwitch:
+            Iest += st.background
         Imeas = self.ptychogram[j]
         cur = abs(Imeas - Iest)  # getRMSD BaseEngine.py:843-868
         if s.saveMemory:
-            self.st.errorAtPos[j] = np.sum(cur)
+            self.st.errorAtPos[j] = np.sum(cur * self.W) if s.FourierMaskSwitch else np.sum(cur)
         else:
             self.st.detectorError[j] = cur
-        frac = np.sqrt(Imeas / (Iest + 1e-10))
-        ESW = ESW * frac
+        if s.adaptiveDenoisingSwitch:  # BaseEngine.adaptiveDenoising
+            Am = Imeas**0.5
+            Ae = np.abs(Iest) ** 0.5
+            noise = np.abs(np.mean(Am - Ae))
+            Am = Am - noise
+            Am[Am < 0] = 0
+            Imeas = Am**2
+        c = s.intensityConstraint
+        if c == "fluctuation":
+            if s.FourierMaskSwitch:
+                aleph = np.sum(Imeas * Iest * self.W) / np.sum(Imeas * Imeas * self.W)
+            else:
+                aleph = np.sum(Imeas * Iest) / np.sum(Imeas * Imeas)
+            st.intensityScaling[j] = aleph
+            frac = (1 + aleph) / 2 * Imeas / (Iest + gimmel)
+        elif c == "exponential":
+            x = cur / (Iest + gimmel)
+            W = np.exp(-0.05 * x)
+            frac = np.sqrt(Imeas / (Iest + gimmel))
+            frac = W * frac + (1 - W)
+        elif c == "poission":
+            frac = Imeas / (Iest + gimmel)
+        elif c == "standard":
+            frac = np.sqrt(Imeas / (Iest + gimmel))
+        else:
+            raise ValueError("intensity constraint not properly specified!")
+        if s.intensityMask:
+            ESW = ESW * (frac * self.intensity_mask + (self.intensity_mask - 1))
+        else:
+            ESW = ESW * frac
+        if s.backgroundModeSwitch:
+            upd = (1 + 1 / self.ptychogram.shape[0] * (np.sqrt(frac) - 1)) ** 2
+            st.background = st.background * upd * self.W if s.FourierMaskSwitch else st.background * upd
         return detector2object(ESW, s.propagator, s.fftshift, self.g)
 
     # BaseEngine.getErrorMetrics (BaseEngine.py:819-841)
     def error_metrics(self):
         st = self.st
         if not self.s.saveMemory:
-            st.errorAtPos = np.sum(np.abs(st.detectorError), axis=(-1, -2))
+            if self.s.FourierMaskSwitch:
+                st.errorAtPos = np.sum(np.abs(st.detectorError) * self.W, axis=(-1, -2))
+            else:
+                st.errorAtPos = np.sum(np.abs(st.detectorError), axis=(-1, -2))
         st.errorAtPos = st.errorAtPos / (self.energyAtPos + 1e-20)
         st.error = np.append(st.error, np.sum(st.errorAtPos))
 
@@ -615,11 +671,26 @@ def run_fixture(fx, iters=None, dtype=None):
         orthogonalizationSwitch=bool(m["orthogonalizationSwitch"]),
         orthogonalizationFrequency=int(m["orthogonalizationFrequency"]),
         entrancePupilDiameter=float(i["entrancePupilDiameter"]),
+        intensityConstraint=str(m.get("intensityConstraint", "standard")),
+        adaptiveDenoisingSwitch=bool(m.get("adaptiveDenoisingSwitch", False)),
+        backgroundModeSwitch=bool(m.get("backgroundModeSwitch", False)),
+        FourierMaskSwitch=bool(m.get("FourierMaskSwitch", False)),
+        intensityMask=bool(m.get("intensityMask", False)),
+        saveMemory=bool(m.get("saveMemory", False)),
+        probePowerCorrectionSwitch=bool(m.get("probePowerCorrectionSwitch", False)),
     )
     cdt = np.complex64 if dtype is None else dtype
     fdt = np.float64 if cdt == np.complex128 else np.float32
     st = State(object=np.array(i["init_object"], dtype=cdt), probe=np.array(i["init_probe"], dtype=cdt))
-    eng = OracleEngine(s, g, st, np.asarray(i["ptychogram"], dtype=fdt), i["positions"], i["energyAtPos"])
+    if "intensityScaling" in i:
+        st.intensityScaling = np.array(i["intensityScaling"], dtype=np.float64)
+    W = np.array(i["W"]) if "W" in i else None
+    mask = np.array(i["intensity_mask"]) if "intensity_mask" in i else None
+    if dtype is not None:
+        W = None if W is None else W.astype(fdt)
+        mask = None if mask is None else mask.astype(fdt)
+    eng = OracleEngine(s, g, st, np.asarray(i["ptychogram"], dtype=fdt), i["positions"], i["energyAtPos"],
+                       W=W, intensity_mask=mask)
     np.random.seed(int(m["seed"]))
     return eng.reconstruct(int(m["iters"]) if iters is None else iters)
 

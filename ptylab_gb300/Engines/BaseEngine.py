@@ -27,10 +27,7 @@ from ..Reconstruction import circ
 
 # Switches whose branches are not on this path; PtyLab default for all is off.
 _UNSUPPORTED = (
-    "backgroundModeSwitch",
     "CPSCswitch",
-    "FourierMaskSwitch",
-    "adaptiveDenoisingSwitch",
     "positionCorrectionSwitch",
     "OPRP",
     "objectTVregSwitch",
@@ -47,8 +44,14 @@ _UNSUPPORTED = (
     "PSDestimationSwitch",
     "TV_autofocus",
     "map_position_to_z_change",
-    "intensityMask",
 )
+
+
+def _host(x):
+    """A NumPy view of a host array or a torch tensor."""
+    if hasattr(x, "detach"):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
 
 
 def _torch():
@@ -77,10 +80,21 @@ class BaseEngine(object):
     # --------------------------------------------------------- validation
     def _check_supported(self):
         p, rec = self.params, self.reconstruction
-        if p.intensityConstraint != "standard":
-            raise NotImplementedError(
-                f"intensityConstraint {p.intensityConstraint!r}: only 'standard' is on this path (BaseEngine.py:954-961)"
-            )
+        ic = p.intensityConstraint
+        if ic == "interferometric":
+            raise NotImplementedError("intensityConstraint 'interferometric' is not supported by the GB300 engines")
+        if ic not in _native.INTENSITY_CONSTRAINTS:
+            raise ValueError("intensity constraint not properly specified!")  # BaseEngine.py:963-964
+        if ic == "fluctuation" and not hasattr(p, "intensityScaling"):
+            # the reference writes params.intensityScaling[positionIndex] (BaseEngine.py:931),
+            # which Params never creates: the caller must provide it
+            raise AttributeError("'Params' object has no attribute 'intensityScaling'")
+        if p.FourierMaskSwitch and getattr(self.experimentalData, "W", None) is None:
+            raise ValueError("FourierMaskSwitch needs experimentalData.W")
+        if getattr(p, "intensityMask", False) and getattr(rec, "intensity_mask", None) is None:
+            raise ValueError("params.intensityMask needs reconstruction.intensity_mask")
+        if self._projection_switches_on() and self.engine_name == "e3PIE":
+            raise NotImplementedError("the GB300 e3PIE runs the standard intensity projection only")
         for name in _UNSUPPORTED:
             if getattr(p, name, False):
                 raise NotImplementedError(f"params.{name} is not supported by the GB300 engines")
@@ -99,17 +113,32 @@ class BaseEngine(object):
             )
         if self.params.propagatorType == "ASP" and self.params.fftshiftSwitch:
             raise ValueError("ASP propagatorType works only with fftshiftSwitch = False")
+        rec = self.reconstruction
+        if self.params.backgroundModeSwitch:  # BaseEngine.py:361-364
+            rec.background = 1e-1 * np.ones((rec.Np, rec.Np))
+        if self.params.intensityConstraint == "fluctuation":  # BaseEngine.py:367-369
+            self.intensityScaling = np.ones(self.experimentalData.numFrames)
+
+    def _projection_switches_on(self):
+        p = self.params
+        return (p.intensityConstraint != "standard" or p.adaptiveDenoisingSwitch or p.backgroundModeSwitch
+                or p.FourierMaskSwitch or bool(getattr(p, "intensityMask", False)))
 
     def _checkFFT(self):
         """Shift the data once so the uncentred transform applies (BaseEngine.py:405-450)."""
         d = self.experimentalData
+        W = getattr(d, "W", None)
         if self.params.fftshiftSwitch:
             if self.params.fftshiftFlag == 0:
                 d.ptychogram = np.fft.ifftshift(d.ptychogram, axes=(-1, -2))
+                if W is not None:
+                    d.W = np.fft.ifftshift(W, axes=(-1, -2))
                 self.params.fftshiftFlag = 1
         else:
             if self.params.fftshiftFlag == 1:
                 d.ptychogram = np.fft.fftshift(d.ptychogram, axes=(-1, -2))
+                if W is not None:
+                    d.W = np.fft.fftshift(W, axes=(-1, -2))
                 self.params.fftshiftFlag = 0
 
     def _initialProbePowerCorrection(self):
@@ -207,6 +236,7 @@ class BaseEngine(object):
         _native.check(lib.ptyg_plan_create(C.byref(geom), C.byref(plan)), "ptyg_plan_create")
         self._plan = plan
         self._set_tables()
+        self._set_projection()
         self._device_extras()
         self._bind()
         self.params.gpuFlag = 1
@@ -227,6 +257,34 @@ class BaseEngine(object):
         self._tables_keepalive = (q, h, sh)
         ptr = lambda a: a.ctypes.data if a is not None else None  # noqa: E731
         _native.check(lib.ptyg_plan_set_tables(self._plan, ptr(q), ptr(h), ptr(sh)), "ptyg_plan_set_tables")
+
+    def _set_projection(self):
+        """The projection switches and their tables (BaseEngine.py:870-1012)."""
+        if not self._projection_switches_on():
+            return
+        torch = _torch()
+        p, rec, d = self.params, self.reconstruction, self.experimentalData
+        lib = self._dev["lib"]
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        mask_on = bool(getattr(p, "intensityMask", False))
+        pr = _native.Projection(
+            intensity_constraint=_native.INTENSITY_CONSTRAINTS[p.intensityConstraint],
+            adaptive_denoising=int(bool(p.adaptiveDenoisingSwitch)), background_mode=int(bool(p.backgroundModeSwitch)),
+            fourier_mask=int(bool(p.FourierMaskSwitch)), intensity_mask=int(mask_on),
+        )
+        tab = lambda a: self._to_device(np.broadcast_to(np.asarray(a, dtype=np.float32), (rec.Np, rec.Np)), torch.float32)  # noqa: E731
+        W = tab(d.W) if p.FourierMaskSwitch else None
+        M = tab(_host(rec.intensity_mask)) if mask_on else None
+        self._dev["W"], self._dev["intensity_mask"] = W, M
+        _native.check(
+            lib.ptyg_plan_set_projection(self._plan, C.byref(pr), W.data_ptr() if W is not None else None,
+                                         M.data_ptr() if M is not None else None, stream),
+            "ptyg_plan_set_projection",
+        )
+        if p.backgroundModeSwitch:
+            bg = tab(rec.background)
+            self._dev["background"] = bg
+            _native.check(lib.ptyg_plan_set_background(self._plan, 0, bg.data_ptr(), stream), "ptyg_plan_set_background")
 
     def _slice_table(self):
         return None
@@ -436,12 +494,32 @@ class BaseEngine(object):
         self._check_status()
         if detector_error and not self.params.saveMemory:
             rec.detectorError = self._detector_error_host()
+        if self._projection_switches_on():
+            self._projection_state_to_host()
         for name in self._state_fields():
             v = getattr(rec, name)
             if isinstance(v, torch.Tensor):
                 setattr(rec, name, v.cpu().numpy())
         self._release_plan()
         self.params.gpuFlag = 0
+
+    def _projection_state_to_host(self):
+        """reconstruction.background (float64, as the reference keeps it) and
+        params.intensityScaling, written in place like the reference does."""
+        torch = _torch()
+        p, rec = self.params, self.reconstruction
+        lib = self._dev["lib"]
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        if p.backgroundModeSwitch:
+            bg = self._dev["background"]
+            _native.check(lib.ptyg_plan_get_background(self._plan, 0, bg.data_ptr(), stream), "ptyg_plan_get_background")
+            rec.background = bg.cpu().numpy().astype(np.float64)
+        if p.intensityConstraint == "fluctuation":
+            nf = self.experimentalData.numFrames
+            out = np.empty(nf, dtype=np.float64)
+            _native.check(lib.ptyg_plan_intensity_scaling(self._plan, 0, out.ctypes.data, stream),
+                          "ptyg_plan_intensity_scaling")
+            p.intensityScaling[...] = out
 
     def changeExperimentalData(self, experimentalData):
         if experimentalData is not None:

@@ -26,6 +26,7 @@ PTYG_ERR_DEVICE = -6
 
 ENGINES = {"ePIE": 0, "mPIE": 1, "qNewton": 2, "e3PIE": 3, "mqNewton": 4}
 MOMENTUM_METHODS = {"momentum": 0, "ADAM": 1, "NADAM": 2}
+INTENSITY_CONSTRAINTS = {"standard": 0, "poission": 1, "exponential": 2, "fluctuation": 3}
 PROPAGATORS = {"fraunhofer": 0, "fresnel": 1, "asp": 2}
 
 _EXC = {
@@ -75,6 +76,16 @@ class UpdateParams(C.Structure):
         ("beta2_scale", C.c_float),
         ("beta_object_m", C.c_float),
         ("beta_probe_m", C.c_float),
+    ]
+
+
+class Projection(C.Structure):
+    _fields_ = [
+        ("intensity_constraint", C.c_int32),
+        ("adaptive_denoising", C.c_int32),
+        ("background_mode", C.c_int32),
+        ("fourier_mask", C.c_int32),
+        ("intensity_mask", C.c_int32),
     ]
 
 
@@ -128,6 +139,10 @@ _SIGNATURES = {
     "ptyg_plan_frame_errors": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_detector_error": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_status": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p],
+    "ptyg_plan_set_projection": [C.c_void_p, C.POINTER(Projection), C.c_void_p, C.c_void_p, C.c_void_p],
+    "ptyg_plan_set_background": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_plan_get_background": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_plan_intensity_scaling": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_multislice_workspace_bytes": [C.POINTER(Multislice)],
     "ptyg_multislice_forward": [
         C.POINTER(Multislice), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,

@@ -203,6 +203,8 @@ struct ScanOwned {
   double* err = nullptr;
   float* detErr = nullptr;
   float* tileMax = nullptr;
+  float* background = nullptr;  // data layout
+  double* iscale = nullptr;
   unsigned* red = nullptr;
   int* status = nullptr;
   bool bound = false;
@@ -220,6 +222,9 @@ struct ptyg_plan {
   float2* fresnelQ = nullptr;
   float2* aspH = nullptr;
   float2* sliceH = nullptr;
+  ptyg_projection proj = {};
+  float* W = nullptr;         // data layout
+  float* imask = nullptr;     // data layout
   std::vector<ScanOwned> scans;
   ScanDev* dScans = nullptr;
   std::vector<ScanDev> hScans;
@@ -230,7 +235,11 @@ static void plan_free(ptyg_plan* p) {
   cudaFree(p->fresnelQ);
   cudaFree(p->aspH);
   cudaFree(p->sliceH);
+  cudaFree(p->W);
+  cudaFree(p->imask);
   for (auto& s : p->scans) {
+    cudaFree(s.background);
+    cudaFree(s.iscale);
     cudaFree(s.data);
     cudaFree(s.work);
     cudaFree(s.esw);
@@ -457,6 +466,8 @@ extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffe
   d.tileMax = o.tileMax;
   d.moment2 = b->second_moment;
   d.vec4 = p->g.No % 2 == 0 && ((uintptr_t)b->object % 16) == 0 && ((uintptr_t)b->object_momentum % 16) == 0;
+  d.background = o.background;
+  d.iscale = o.iscale;
   o.bound = true;
   o.orderLen = p->g.num_frames;
   PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &d, sizeof(ScanDev), cudaMemcpyHostToDevice, st), "scan upload");
@@ -540,6 +551,14 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
     a.betaOm = u->beta_object_m;
     a.betaPm = u->beta_probe_m;
   }
+  a.iconstraint = p->proj.intensity_constraint;
+  a.denoise = p->proj.adaptive_denoising;
+  a.bgMode = p->proj.background_mode;
+  a.fmask = p->proj.fourier_mask;
+  a.imask = p->proj.intensity_mask;
+  a.invFrames = 1.f / (float)g.num_frames;
+  a.W = p->W;
+  a.imaskTab = p->imask;
   if (g.engine == PTYG_E3PIE && !p->sliceH) return fail(PTYG_ERR_INVALID, "e3PIE slice transfer function not set");
   cudaError_t e = g.engine == PTYG_E3PIE ? ptyg::launch_e3pie(a, g.num_scans, p->threads, p->smem, st)
                                          : ptyg::launch_engine(a, g.num_scans, p->threads, p->smem, st);
@@ -601,6 +620,107 @@ extern "C" int ptyg_plan_detector_error(ptyg_plan* p, int scan, float* out, void
   } else {
     PTYG_CUDA(ptyg::from_fourier_layout(o.detErr, out, p->g.num_frames, p->g.Np, st), "layout");
   }
+  return PTYG_OK;
+}
+
+// a device Np x Np float table in the ptychogram's layout -> the data layout
+static int to_data_layout(const ptyg_plan* p, const float* in, float* out, cudaStream_t st) {
+  const int Np = p->g.Np;
+  if (p->g.propagator == PTYG_ASP) {
+    PTYG_CUDA(cudaMemcpyAsync(out, in, (size_t)Np * Np * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+  } else {
+    PTYG_CUDA(ptyg::to_fourier_layout(in, out, 1, Np, st), "layout");
+  }
+  return PTYG_OK;
+}
+
+static int from_data_layout(const ptyg_plan* p, const float* in, float* out, cudaStream_t st) {
+  const int Np = p->g.Np;
+  if (p->g.propagator == PTYG_ASP) {
+    PTYG_CUDA(cudaMemcpyAsync(out, in, (size_t)Np * Np * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+  } else {
+    PTYG_CUDA(ptyg::from_fourier_layout(in, out, 1, Np, st), "layout");
+  }
+  return PTYG_OK;
+}
+
+static __global__ void fill_kernel(float* x, size_t n, float v) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+static __global__ void fill_kernel_d(double* x, size_t n, double v) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
+extern "C" int ptyg_plan_set_projection(ptyg_plan* p, const ptyg_projection* pr, const float* W,
+                                        const float* intensity_mask, void* stream) {
+  if (!p || !pr) return fail(PTYG_ERR_INVALID, "null argument");
+  const ptyg_projection& q = *pr;
+  if (q.intensity_constraint < PTYG_STANDARD || q.intensity_constraint > PTYG_FLUCTUATION)
+    return fail(PTYG_ERR_INVALID, "intensity_constraint=%d", q.intensity_constraint);
+  const bool any = q.intensity_constraint || q.adaptive_denoising || q.background_mode || q.fourier_mask ||
+                   q.intensity_mask;
+  if (p->g.engine == PTYG_E3PIE && any)
+    return fail(PTYG_ERR_UNSUPPORTED, "e3PIE runs the standard projection only");
+  if (q.fourier_mask && !W) return fail(PTYG_ERR_INVALID, "FourierMaskSwitch needs W");
+  if (q.intensity_mask && !intensity_mask) return fail(PTYG_ERR_INVALID, "intensityMask needs intensity_mask");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n2 = (size_t)p->g.Np * p->g.Np;
+  int r;
+  if (q.fourier_mask) {
+    if (!p->W) PTYG_CUDA(cudaMalloc(&p->W, n2 * sizeof(float)), "allocation");
+    if ((r = to_data_layout(p, W, p->W, st))) return r;
+  }
+  if (q.intensity_mask) {
+    if (!p->imask) PTYG_CUDA(cudaMalloc(&p->imask, n2 * sizeof(float)), "allocation");
+    if ((r = to_data_layout(p, intensity_mask, p->imask, st))) return r;
+  }
+  for (int s = 0; s < p->g.num_scans; ++s) {
+    ScanOwned& o = p->scans[s];
+    if (q.background_mode && !o.background) {
+      PTYG_CUDA(cudaMalloc(&o.background, n2 * sizeof(float)), "allocation");
+      fill_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(o.background, n2, 0.1f);
+      PTYG_CUDA(cudaGetLastError(), "fill");
+    }
+    if (q.intensity_constraint == PTYG_FLUCTUATION && !o.iscale) {
+      const size_t nf = (size_t)p->g.num_frames;
+      PTYG_CUDA(cudaMalloc(&o.iscale, nf * sizeof(double)), "allocation");
+      fill_kernel_d<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(o.iscale, nf, 1.0);
+      PTYG_CUDA(cudaGetLastError(), "fill");
+    }
+    p->hScans[s].background = o.background;
+    p->hScans[s].iscale = o.iscale;
+    PTYG_CUDA(cudaMemcpyAsync(p->dScans + s, &p->hScans[s], sizeof(ScanDev), cudaMemcpyHostToDevice, st),
+              "scan upload");
+  }
+  p->proj = q;
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_set_background(ptyg_plan* p, int scan, const float* background, void* stream) {
+  if (!p || !background) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  if (!p->scans[scan].background) return fail(PTYG_ERR_INVALID, "background mode is off (ptyg_plan_set_projection)");
+  return to_data_layout(p, background, p->scans[scan].background, (cudaStream_t)stream);
+}
+
+extern "C" int ptyg_plan_get_background(ptyg_plan* p, int scan, float* background, void* stream) {
+  if (!p || !background) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  if (!p->scans[scan].background) return fail(PTYG_ERR_INVALID, "background mode is off (ptyg_plan_set_projection)");
+  return from_data_layout(p, p->scans[scan].background, background, (cudaStream_t)stream);
+}
+
+extern "C" int ptyg_plan_intensity_scaling(ptyg_plan* p, int scan, double* host_out, void* stream) {
+  if (!p || !host_out) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  if (!p->scans[scan].iscale) return fail(PTYG_ERR_INVALID, "the fluctuation constraint is off");
+  cudaStream_t st = (cudaStream_t)stream;
+  PTYG_CUDA(cudaMemcpyAsync(host_out, p->scans[scan].iscale, (size_t)p->g.num_frames * sizeof(double),
+                            cudaMemcpyDeviceToHost, st),
+            "copy");
+  PTYG_CUDA(cudaStreamSynchronize(st), "copy");
   return PTYG_OK;
 }
 

@@ -8,6 +8,8 @@ namespace ptyg {
 
 enum Engine { ENG_EPIE = 0, ENG_MPIE = 1, ENG_QNEWTON = 2, ENG_E3PIE = 3, ENG_MQNEWTON = 4 };
 enum Momentum { MOM_PLAIN = 0, MOM_ADAM = 1, MOM_NADAM = 2 };
+// params.intensityConstraint (BaseEngine.py:913-961)
+enum IntensityConstraint { IC_STANDARD = 0, IC_POISSON = 1, IC_EXPONENTIAL = 2, IC_FLUCTUATION = 3 };
 
 // Object modes the pixel-update loop carries in registers.
 constexpr int MAX_OBJECT_MODES = 4;
@@ -47,6 +49,8 @@ struct ScanDev {
   float* tileMax;          // qNewton/mqNewton: max of sum_o |O_o| per TILE x TILE object tile
   float* moment2;          // mqNewton ADAM/NADAM: {v_object, v_probe}
   int vec4;                // No even and object / objectMomentum 16-byte aligned: 16-byte accesses
+  float* background;       // backgroundModeSwitch: Np x Np, data layout (plan-owned)
+  double* iscale;          // 'fluctuation': per-frame intensity scaling aleph (plan-owned)
 };
 
 // Side of the object tiles whose maxima qNewton keeps up to date.
@@ -69,6 +73,13 @@ struct EngineArgs {
   // mqNewton: method, float32 beta1, 1-beta1, beta2, 1-beta2, 1-beta^itr, step sizes
   int momentum;
   float b1, omb1, b2, omb2, b1s, b2s, betaOm, betaPm;
+  // intensity projection switches (BaseEngine.py:870-1012): constraint,
+  // adaptive denoising, background mode, Fourier-mask error weights,
+  // intensity mask; tables in the data layout (Np x Np)
+  int iconstraint, denoise, bgMode, fmask, imask;
+  float invFrames;         // 1 / numFrames (background update)
+  const float* W;          // experimentalData.W
+  const float* imaskTab;   // reconstruction.intensity_mask
 };
 
 }  // namespace ptyg

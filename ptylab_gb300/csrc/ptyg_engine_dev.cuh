@@ -90,6 +90,31 @@ PTYG_DEV void block_sum_n(double (&v)[NV], double* scratch) {
   }
 }
 
+// Sum NV values over the whole cluster: CTA totals go to rank 0's `part`
+// ([value][CTA], NV * C doubles), one cluster barrier, then every thread of
+// every CTA adds the C totals in the same order (an xor butterfly over C
+// lanes), so all CTAs hold bitwise the same sums.  scratch: NV * 32 doubles.
+template <int NV, int C>
+PTYG_DEV void cluster_sum_n(double (&v)[NV], double* part, double* scratch, int crank) {
+  __syncthreads();  // scratch may still be read by an earlier block reduction
+  block_sum_n<NV>(v, scratch);
+  if (threadIdx.x == 0) {
+    double* dst = dsmem(part, 0);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) dst[k * C + crank] = v[k];
+  }
+  cluster_sync(C);
+  const int lane = threadIdx.x & 31;
+  const double* src = dsmem(part, 0);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double t = lane < C ? src[k * C + lane] : 0.0;
+#pragma unroll
+    for (int off = 1; off < C; off <<= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    v[k] = __shfl_sync(0xffffffffu, t, 0);
+  }
+}
+
 // Sum over the CTA; thread 0 receives the result.
 PTYG_DEV double block_sum(double v, double* scratch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;

@@ -471,6 +471,88 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
     cp_async_wait_prev();  // this position's intensities
     cluster_sync(C);
 
+    // The intensity projection of this CTA's LN detector pixels
+    // (BaseEngine.py:881-1009): getRMSD on the estimate (plus the background),
+    // adaptive denoising (:1805-1822, a frame mean: one cluster sum), the
+    // standard / poission / exponential / fluctuation constraint (fluctuation:
+    // two more frame sums), the intensity mask, the background update.  Iest(i)
+    // is the estimate of pixel i; the factor goes to sm.fr[i] times outScale.
+    // Tables and the background are in the data layout, this CTA's block at
+    // blk0 * NP.  Returns this thread's (FourierMask-weighted) error sum.
+    auto project = [&](auto Iest, float outScale) -> double {
+      const bool det = a.writeDetErr && s.detErr;
+      const size_t tb = (size_t)blk0 * NP;
+      float* bg = a.bgMode ? s.background + tb : nullptr;
+      const float* Wt = a.fmask ? a.W + tb : nullptr;
+      const float* Mt = a.imask ? a.imaskTab + tb : nullptr;
+      float e = 0.f, noise = 0.f, aleph = 0.f;
+      auto denoised = [&](float im) {
+        if (!a.denoise) return im;
+        const float am = fmaxf(sqrtf(im) - noise, 0.f);
+        return am * am;
+      };
+      auto finish = [&](int i, float ie, float im, float d) {
+        const float q = denoised(im) / (ie + 1e-10f);
+        float frac;
+        if (a.iconstraint == IC_POISSON) {
+          frac = q;
+        } else if (a.iconstraint == IC_EXPONENTIAL) {
+          const float w = expf(-0.05f * (d / (ie + 1e-10f)));
+          frac = w * sqrtf(q) + (1.f - w);
+        } else if (a.iconstraint == IC_FLUCTUATION) {
+          frac = (1.f + aleph) * 0.5f * q;
+        } else {
+          frac = sqrtf(q);
+        }
+        sm.fr[i] = (Mt ? frac * Mt[i] + (Mt[i] - 1.f) : frac) * outScale;
+        if (bg) {
+          const float u = 1.f + a.invFrames * (sqrtf(frac) - 1.f);
+          float b = bg[i] * (u * u);
+          if (Wt) b *= Wt[i];
+          bg[i] = b;
+        }
+      };
+      const bool twoPass = a.denoise || a.iconstraint == IC_FLUCTUATION;
+      double dn = 0.0;
+      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+        float ie = Iest(i);
+        if (bg) ie += bg[i];
+        const float im = dat[i];
+        const float d = fabsf(im - ie);
+        e += Wt ? d * Wt[i] : d;
+        if (det) s.detErr[((size_t)frame * NP + blk0) * NP + i] = d;
+        if (twoPass) {
+          sm.fr[i] = ie;  // kept for the second pass (same thread)
+          if (a.denoise) dn += (double)(sqrtf(im) - sqrtf(fabsf(ie)));
+        } else {
+          finish(i, ie, im, d);
+        }
+      }
+      if (twoPass) {
+        if (a.denoise) {
+          double v[1] = {dn};
+          cluster_sum_n<1, C>(v, sm.part, sm.redD, crank);
+          noise = fabsf((float)(v[0] / (double)(NP * NP)));
+        }
+        if (a.iconstraint == IC_FLUCTUATION) {
+          double v[2] = {0.0, 0.0};
+          for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+            const float ie = sm.fr[i], imd = denoised(dat[i]), w = Wt ? Wt[i] : 1.f;
+            v[0] += (double)(imd * ie * w);
+            v[1] += (double)(imd * imd * w);
+          }
+          cluster_sum_n<2, C>(v, sm.part + 32, sm.redD, crank);
+          aleph = (float)(v[0] / v[1]);
+          if (crank == 0 && threadIdx.x == 0 && s.iscale) s.iscale[frame] = (double)aleph;
+        }
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          const float ie = sm.fr[i], im = dat[i];
+          finish(i, ie, im, fabsf(im - ie));
+        }
+      }
+      return (double)e;
+    };
+
     double err = 0.0;
     if (!asp) {
       // ---------------- B: Fourier-plane intensity projection (BaseEngine.py:870-1012)
@@ -487,22 +569,14 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
             for (int r = 0; r < E; ++r) sm.tile[(k * NP + 32 * r + lane) * ld + c] = v[r];
           });
       __syncthreads();
-      {
-        float e = 0.f;
-        const bool det = a.writeDetErr && s.detErr;
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-          const int c = i / NP, sy = i - (i / NP) * NP;
-          float ie = 0.f;
-          for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[(k * NP + sy) * ld + c]);
-          ie *= inv2;
-          const float im = dat[i];
-          const float d = fabsf(im - ie);
-          e += d;
-          if (det) s.detErr[((size_t)frame * NP + sx0) * NP + i] = d;
-          sm.fr[i] = sqrtf(im / (ie + 1e-10f)) * inv2;
-        }
-        err = (double)e;
-      }
+      err = project(
+          [&](int i) {
+            const int c = i / NP, sy = i - (i / NP) * NP;
+            float ie = 0.f;
+            for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[(k * NP + sy) * ld + c]);
+            return ie * inv2;
+          },
+          inv2);
       __syncthreads();
       fft_tasks<E, true>(
           F, K * L,
@@ -530,20 +604,13 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
             for (int j = 0; j < E; ++j) row[lane + 32 * j] = v[j];
           });
       __syncthreads();
-      {
-        float e = 0.f;
-        const bool det = a.writeDetErr && s.detErr;
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-          float ie = 0.f;
-          for (int k = 0; k < K; ++k) ie += cabs2(sm.rows[k * LN + i]);
-          const float im = dat[i];
-          const float d = fabsf(im - ie);
-          e += d;
-          if (det) s.detErr[((size_t)frame * NP + line0) * NP + i] = d;
-          sm.fr[i] = sqrtf(im / (ie + 1e-10f));
-        }
-        err = (double)e;
-      }
+      err = project(
+          [&](int i) {
+            float ie = 0.f;
+            for (int k = 0; k < K; ++k) ie += cabs2(sm.rows[k * LN + i]);
+            return ie;
+          },
+          1.f);
       __syncthreads();
       fft_tasks<E, false>(
           F, K * L,
@@ -560,6 +627,7 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
       column_filter<E, L>(sm.tile, sm.rows, F, a.aspH, true, crank, K);
     }
     {
+      __syncthreads();  // sm.redD may still be read by the projection's cluster sums
       const double t = block_sum(err, sm.redD);
       if (threadIdx.x == 0) s.errPart[(size_t)frame * C + crank] = t;
     }

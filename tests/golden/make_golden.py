@@ -188,6 +188,18 @@ def run_case(ref, d, case):
     params.fftshiftSwitch = case.get("fftshift", False)
     for k, v in case.get("params", {}).items():
         setattr(params, k, v)
+    extra_inputs = {}
+    if case.get("W"):
+        # experimentalData.W for FourierMaskSwitch: a detector-plane disc
+        n = d["ptychogram"].shape[-1]
+        yy, xx = np.mgrid[:n, :n] - n / 2
+        data.W = (np.hypot(yy, xx) < 0.4 * n).astype(np.float32)
+        extra_inputs["W"] = data.W.copy()
+    if case.get("intensityScaling"):
+        # the fluctuation constraint writes params.intensityScaling, which
+        # Params never creates (BaseEngine.py:931): the caller provides it
+        params.intensityScaling = np.ones(d["ptychogram"].shape[0])
+        extra_inputs["intensityScaling"] = params.intensityScaling.copy()
     if "No" in d:
         # the reconstruction derives No from the scan unless it is set first
         Reconstruction = ref["Reconstruction"]
@@ -203,6 +215,15 @@ def run_case(ref, d, case):
         rec.refrIndex = 1.0
     np_.random.seed(SEED)
     rec.initializeObjectProbe()
+    if case.get("intensity_mask"):
+        # reconstruction.intensity_mask for params.intensityMask: 1 inside, 0.5 on a ring, 0 in one corner
+        n = rec.Np
+        yy, xx = np.mgrid[:n, :n] - n / 2
+        r = np.hypot(yy, xx)
+        m = np.where(r < 0.35 * n, 1.0, 0.5).astype(np.float32)
+        m[: n // 8, : n // 8] = 0.0
+        rec.intensity_mask = m
+        extra_inputs["intensity_mask"] = m.copy()
     init_object = rec.object.copy()
     init_probe = rec.probe.copy()
     engine = getattr(ref["Engines"], case["engine"])(rec, data, params, ref["DummyMonitor"]())
@@ -241,6 +262,7 @@ def run_case(ref, d, case):
         entrancePupilDiameter=np.float64(data.entrancePupilDiameter),
         energyAtPos=np.asarray(data.energyAtPos),
         orders=np.stack(orders),
+        **extra_inputs,
     )
     if nsl > 1:
         inputs["dz"] = np.float64(rec.dz)
@@ -261,6 +283,10 @@ def run_case(ref, d, case):
             outputs["probeMomentum_v"] = np.asarray(rec.probeMomentum_v)
     if case.get("keep_detector_error", False):
         outputs["detectorError"] = np.asarray(rec.detectorError, dtype=np.float64)
+    if getattr(params, "backgroundModeSwitch", False):
+        outputs["background"] = np.asarray(rec.background)
+    if case.get("intensityScaling"):
+        outputs["intensityScaling"] = np.asarray(params.intensityScaling)
     return inputs, outputs
 
 
@@ -336,6 +362,30 @@ SCAN_CONFIGS = {
         params=dict(orthogonalizationSwitch=True, orthogonalizationFrequency=2),
     ),
     "mqnewton_momentum": dict(engine="mqNewton", iters=3, engine_attrs=dict(momentum_method="momentum")),
+    # intensity-projection switches (BaseEngine.py:870-1012, 1805-1822)
+    # the unsquared constraints need an initial probe of the data's power
+    "epie_poission": dict(
+        engine="ePIE", order="random", iters=3,
+        params=dict(intensityConstraint="poission", probePowerCorrectionSwitch=True),
+    ),
+    "mpie_exponential_denoise": dict(
+        engine="mPIE", iters=3, params=dict(intensityConstraint="exponential", adaptiveDenoisingSwitch=True)
+    ),
+    "epie_background_fmask": dict(
+        engine="ePIE", order="random", iters=3, W=True, keep_detector_error=True,
+        params=dict(backgroundModeSwitch=True, FourierMaskSwitch=True),
+    ),
+    "epie_fluctuation": dict(
+        engine="ePIE", iters=3, intensityScaling=True,
+        params=dict(intensityConstraint="fluctuation", probePowerCorrectionSwitch=True),
+    ),
+    "epie_intensity_mask": dict(engine="ePIE", iters=3, intensity_mask=True, params=dict(intensityMask=True)),
+    "epie_asp_denoise_background": dict(
+        engine="ePIE", propagator="ASP", iters=3, params=dict(adaptiveDenoisingSwitch=True, backgroundModeSwitch=True)
+    ),
+    "qnewton_savememory_background": dict(
+        engine="qNewton", iters=3, W=True, params=dict(saveMemory=True, backgroundModeSwitch=True, FourierMaskSwitch=True)
+    ),
 }
 
 FPM_CONFIGS = {
@@ -345,6 +395,11 @@ FPM_CONFIGS = {
     "mqnewton_nadam_fpm": dict(
         engine="mqNewton", order="NA", iters=3, engine_attrs=dict(momentum_method="NADAM"),
         params=dict(probeBoundary=True),
+    ),
+    # ... with the example's adaptive denoising (exampleReconstructionFPM.py:54-60)
+    "mqnewton_nadam_fpm_denoise": dict(
+        engine="mqNewton", order="NA", iters=3, engine_attrs=dict(momentum_method="NADAM"),
+        params=dict(probeBoundary=True, adaptiveDenoisingSwitch=True),
     ),
 }
 
@@ -450,6 +505,13 @@ def _meta(case, d):
         magnification=d.get("magnification", 0.0),
         NA=d.get("NA", 0.0),
         momentum_method=case.get("engine_attrs", {}).get("momentum_method", "ADAM"),
+        intensityConstraint=params.get("intensityConstraint", "standard"),
+        adaptiveDenoisingSwitch=bool(params.get("adaptiveDenoisingSwitch", False)),
+        backgroundModeSwitch=bool(params.get("backgroundModeSwitch", False)),
+        FourierMaskSwitch=bool(params.get("FourierMaskSwitch", False)),
+        intensityMask=bool(params.get("intensityMask", False)),
+        saveMemory=bool(params.get("saveMemory", False)),
+        probePowerCorrectionSwitch=bool(params.get("probePowerCorrectionSwitch", False)),
     )
 
 

@@ -42,6 +42,7 @@ def run_fixture_gpu(fx, engine_name=None, iters=None):
         eng.momentum_method = str(m["momentum_method"])
     np.random.seed(int(m["seed"]))
     eng.reconstruct()
+    run_fixture_gpu.params = p
     return rec, eng
 
 
@@ -51,7 +52,8 @@ def reference_spread(fx):
     from oracle import ptyoracle as O
 
     st = O.run_fixture(fx, dtype=np.complex128)
-    return {k: rel_err(fx[f"out_{k}"], getattr(st, k)) for k in ("object", "probe", "error", "errorAtPos")}
+    keys = ("object", "probe", "error", "errorAtPos", "background", "intensityScaling")
+    return {k: rel_err(fx[f"out_{k}"], getattr(st, k)) for k in keys if f"out_{k}" in fx}
 
 
 @pytest.mark.parametrize("name", IN_SCOPE)
@@ -82,6 +84,10 @@ def test_engine_matches_reference_fixture(torch_cuda, name):
     if "objectMomentum" in target:
         assert rel_err(rec.objectMomentum, target["objectMomentum"]) < max(1e-2, 3 * floor["object"])
         assert rel_err(rec.probeMomentum, target["probeMomentum"]) < max(1e-2, 3 * floor["probe"])
+    for key in ("background", "intensityScaling"):
+        if f"out_{key}" in fx and platform_reproduces_order(fx):
+            got = rec.background if key == "background" else run_fixture_gpu.params.intensityScaling
+            assert rel_err(got, fx[f"out_{key}"]) < max(TOL_FIXTURE, 3 * floor[key]), (key, rel_err(got, fx[f"out_{key}"]), floor[key])
     if str(fx["meta_engine"]) == "mqNewton":
         # the object buffer equals the final object; the probe buffer is the
         # probe before the last iteration's constraints; the second moments
@@ -129,10 +135,13 @@ def test_unsupported_switch_raises(torch_cuda):
     fx = load_fixture("reg_epie_fraunhofer")
     m, i, d, p, rec = containers(fx)
     rec.object, rec.probe = i["init_object"].copy(), i["init_probe"].copy()
-    p.intensityConstraint = "poission"
+    p.intensityConstraint = "interferometric"
     eng = Engines.ePIE(rec, d, p, DummyMonitor())
     with pytest.raises(NotImplementedError):
         eng.reconstruct()
+    p.intensityConstraint = "sigmoid"  # not a constraint PtyLab knows (BaseEngine.py:963-964)
+    with pytest.raises(ValueError):
+        Engines.ePIE(rec, d, p, DummyMonitor()).reconstruct()
 
 
 def test_asp_with_fftshift_raises_value_error(torch_cuda):
@@ -271,17 +280,19 @@ def test_config3_fpm_qnewton_precision_vs_complex128(torch_cuda):
         assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 5e-4, msg
 
 
-def test_config3_fpm_mqnewton_nadam_precision_vs_complex128(torch_cuda):
+@pytest.mark.parametrize("denoise", [False, True])
+def test_config3_fpm_mqnewton_nadam_precision_vs_complex128(torch_cuda, denoise):
     """The FPM example's engine (mqNewton, NADAM, beta1 = beta2 = 0.5,
-    exampleReconstructionFPM.py:66-75) at the LED-array configuration, 3
-    iterations: every position adds a momentum step over the whole 512 x 512
-    spectrum.  The GB300 result is as close to a complex128 oracle run as the
-    reference's complex64 path."""
+    exampleReconstructionFPM.py:54-75, with and without its adaptive
+    denoising) at the LED-array configuration, 3 iterations: every position
+    adds a momentum step over the whole 512 x 512 spectrum.  The GB300 result
+    is as close to a complex128 oracle run as the reference's complex64 path."""
     from oracle import ptyoracle as O
     from ptylab_gb300 import DummyMonitor, Engines
     from ptylab_gb300.simulate import FPMSpec, fpm_problem
 
     d, p, rec, _, _ = fpm_problem(FPMSpec())
+    p.adaptiveDenoisingSwitch = denoise
     obj0, prb0 = rec.object.copy(), rec.probe.copy()
     positions = rec.positions.copy()
     eng = Engines.mqNewton(rec, d, p, DummyMonitor())
@@ -290,7 +301,8 @@ def test_config3_fpm_mqnewton_nadam_precision_vs_complex128(torch_cuda):
     eng.reconstruct()
     g = O.Geometry(Np=128, No=512, dxp=rec.dxp, wavelength=rec.wavelength, zo=rec.zo)
     s = O.Settings(engine="mqNewton", momentum_method="NADAM", order="NA", operationMode="FPM",
-                   probeBoundary=True, entrancePupilDiameter=d.entrancePupilDiameter)
+                   probeBoundary=True, entrancePupilDiameter=d.entrancePupilDiameter,
+                   adaptiveDenoisingSwitch=denoise)
 
     def oracle(cdt, fdt):
         st = O.State(object=obj0.astype(cdt), probe=prb0.astype(cdt))

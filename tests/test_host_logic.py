@@ -33,12 +33,27 @@ def containers(fx):
     p.probeBoundary = bool(m["probeBoundary"])
     p.orthogonalizationSwitch = bool(m["orthogonalizationSwitch"])
     p.orthogonalizationFrequency = int(m["orthogonalizationFrequency"])
+    # intensity-projection switches and their tables (absent from older fixtures)
+    p.intensityConstraint = str(m.get("intensityConstraint", "standard"))
+    p.adaptiveDenoisingSwitch = bool(m.get("adaptiveDenoisingSwitch", False))
+    p.backgroundModeSwitch = bool(m.get("backgroundModeSwitch", False))
+    p.FourierMaskSwitch = bool(m.get("FourierMaskSwitch", False))
+    p.saveMemory = bool(m.get("saveMemory", False))
+    p.probePowerCorrectionSwitch = bool(m.get("probePowerCorrectionSwitch", False))
+    if bool(m.get("intensityMask", False)):
+        p.intensityMask = True
+    if "W" in i:
+        d.W = np.array(i["W"], copy=True)
+    if "intensityScaling" in i:
+        p.intensityScaling = np.array(i["intensityScaling"], copy=True)
     rec = Reconstruction(d, p, No=int(i["No"]) if mode == "FPM" else None)
     nl, nos, nps, nsl = (int(v) for v in m["modes"])
     rec.nlambda, rec.nosm, rec.npsm, rec.nslice = nl, nos, nps, nsl
     if nsl > 1:
         rec.dz = float(i["dz"])
         rec.refrIndex = 1.0
+    if "intensity_mask" in i:
+        rec.intensity_mask = np.array(i["intensity_mask"], copy=True)
     return m, i, d, p, rec
 
 

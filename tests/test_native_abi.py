@@ -87,7 +87,7 @@ def declared_structs():
 @pytest.mark.parametrize(
     "cname,pyname",
     [("ptyg_geometry", "Geometry"), ("ptyg_update_params", "UpdateParams"), ("ptyg_scan_buffers", "ScanBuffers"),
-     ("ptyg_multislice", "Multislice")],
+     ("ptyg_multislice", "Multislice"), ("ptyg_projection", "Projection")],
 )
 def test_ctypes_structs_match_the_header(cname, pyname):
     """Field names, order and types of the ctypes mirrors equal the C structs."""
