@@ -283,6 +283,48 @@ PTYG_API int ptyg_gram(const void* p, int modes, int64_t n, void* gram, void* st
 /* out[a][i] = sum_b V[a][b] * p[b][i]; V is device complex64 modes x modes. */
 PTYG_API int ptyg_mix_modes(const void* V, const void* p, void* out, int modes, int64_t n, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Learned warm start: kernels of a small convolutional encoder-decoder
+ * (BF16 operands on the tcgen05 tensor cores, FP32 accumulation).  No
+ * counterpart in PtyLab.  Activations are NHWC bf16; weights [Co][3][3][Ci]
+ * bf16; every pointer is device memory.  `status` (may be NULL) is set to 1
+ * if a tensor-core wait gave up (the results are then invalid).
+ */
+
+/* C = A . B^T: A [M][K], B [N][K] bf16, K a multiple of 8.  Either out != NULL:
+ * bf16 [M][N] = relu?(C + bias); or C: float [splits][M][N] partial sums over
+ * `splits` slices of K (reduce them with ptyg_nn_reduce_splits; bias only
+ * with splits = 1). */
+PTYG_API int ptyg_nn_gemm(const void* A, const void* B, int M, int N, int K, int splits, float* C, void* out,
+                          const float* bias, int relu, int* status, void* stream);
+
+/* 3x3 'same' convolution of X [Bn][H][W][C0] (channel-concatenated with
+ * X1 [Bn][H][W][C1] when C1 > 0; C0, C1 multiples of 8) with weights
+ * Wt [Co][9 (C0 + C1)]: into out (bf16, + bias, optional ReLU) or C (float). */
+PTYG_API int ptyg_nn_conv3(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, const void* Wt, int Co,
+                           float* C, void* out, const float* bias, int relu, int* status, void* stream);
+
+PTYG_API int ptyg_nn_reduce_splits(const float* part, float* out, int64_t n, int splits, void* stream);
+/* colT [Kpad][Bn H W]: the transposed 3x3 patch matrix (rows >= 9 (C0 + C1) zero) */
+PTYG_API int ptyg_nn_im2col_t(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, int Kpad,
+                              void* colT, void* stream);
+/* col [Bn H W][Kpad]: the patch matrix of a one-channel image (the first layer) */
+PTYG_API int ptyg_nn_im2col1(const void* X, int Bn, int H, int W, int Kpad, void* col, void* stream);
+PTYG_API int ptyg_nn_transpose(const void* in, void* out, int R, int C, void* stream);
+/* W [Co][9][Ci] -> Wf [Ci][9][Co] with the taps flipped (backward-data weights) */
+PTYG_API int ptyg_nn_flip_weights(const void* w, void* wf, int Co, int Ci, void* stream);
+PTYG_API int ptyg_nn_relu_bwd(const float* dy, const void* y, void* dpre, float* dpre_f32, int64_t n, void* stream);
+PTYG_API int ptyg_nn_col_sum(const float* d, float* out, int M, int N, void* stream);
+PTYG_API int ptyg_nn_pool2(const void* x, void* y, int Bn, int H, int W, int C, void* stream);
+PTYG_API int ptyg_nn_pool2_bwd(const float* dy, float* dx, int Bn, int H, int W, int C, void* stream);
+PTYG_API int ptyg_nn_up2(const void* x, void* y, int Bn, int H, int W, int C, void* stream);
+PTYG_API int ptyg_nn_up2_bwd(const float* dy, float* dx, int Bn, int H, int W, int C, int ldy, int coff, void* stream);
+PTYG_API int ptyg_nn_slice_add(const float* src, int ldsrc, int coff, float* dst, int C, int64_t M, int accumulate,
+                               void* stream);
+PTYG_API int ptyg_nn_cast_bf16(const float* x, void* y, int64_t n, void* stream);
+PTYG_API int ptyg_nn_adam(float* p, const float* g, float* m, float* v, void* p16, int64_t n, float lr, float b1,
+                          float b2, float eps, int step, float weight_decay, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -152,6 +152,26 @@ _SIGNATURES = {
         C.POINTER(Multislice), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
         C.c_void_p, C.c_size_t, C.c_void_p,
     ],
+    "ptyg_nn_gemm": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                     C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_nn_conv3": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_nn_reduce_splits": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p],
+    "ptyg_nn_im2col_t": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                         C.c_void_p],
+    "ptyg_nn_im2col1": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_nn_transpose": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_flip_weights": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_relu_bwd": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p],
+    "ptyg_nn_col_sum": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_pool2": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_pool2_bwd": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_up2": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_up2_bwd": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_slice_add": [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int64, C.c_int, C.c_void_p],
+    "ptyg_nn_cast_bf16": [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p],
+    "ptyg_nn_adam": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_float,
+                     C.c_float, C.c_float, C.c_int, C.c_float, C.c_void_p],
     "ptyg_mul_window": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p],
     "ptyg_gram": [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p],
     "ptyg_mix_modes": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.c_void_p],

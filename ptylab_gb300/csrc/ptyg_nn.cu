@@ -1,0 +1,586 @@
+// Kernels of the learned warm start: a small convolutional encoder-decoder
+// trained and evaluated on the GPU.  No counterpart in PtyLab.
+//
+// Convolutions are implicit GEMMs on the 5th-generation tensor cores:
+// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor memory),
+// issued by one thread per CTA, operands staged in shared memory in the
+// canonical K-major layout without swizzle (8-row x 16-byte core matrices),
+// two pipeline stages so the next tile loads while the tensor core works on
+// the current one.  The A-operand loader either reads a dense K-major matrix
+// or gathers 3x3 'same' convolution patches straight from NHWC activations
+// (optionally the channel concatenation of two tensors, the decoder's skip
+// connections), 8 channels (16 bytes) per load.
+//
+//   forward            Y[m, co]  = sum_k Xpatch[m, k] W[co, k]         (conv A-loader)
+//   backward, data     dX[m, ci] = sum_k dYpatch[m, k] W'[ci, k]       (conv A-loader on dY,
+//                      W' = W with the taps flipped and in/out channels swapped)
+//   backward, weights  dW^T[k, co] = sum_m XcolT[k, m] dYT[co, m]      (dense, split over m)
+//
+// Every wait on a tensor-core completion is bounded: after the limit the
+// kernel records an error and skips its remaining MMAs, so a fault can never
+// hang the device.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+
+#include "ptyg.h"
+#include "ptyg_ops.cuh"
+
+namespace ptyg {
+namespace nn {
+
+typedef __nv_bfloat16 bf16;
+
+#define NN_DEV __device__ __forceinline__
+
+NN_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory matrix descriptor: start >> 4 in [0,14), leading
+// (K-direction) byte offset >> 4 in [16,30), stride (M/N-direction) byte
+// offset >> 4 in [32,46), descriptor version 1 in [46,48), no swizzle.
+NN_DEV uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor, kind::f16: FP32 D (bits 4-5 = 1), BF16 A and B
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 in bits 17-22, M >> 4 in 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+constexpr int BM = 128, BK = 64, STAGES = 2;
+constexpr long WAIT_LIMIT = 1L << 26;  // try_wait polls before an MMA wait is declared lost
+
+enum AMode { A_DENSE = 0, A_CONV3 = 1 };
+enum Epilogue { EPI_F32 = 0, EPI_BF16 = 1 };
+
+struct GemmArgs {
+  // A: dense [M, K] bf16 (lda = K), or NHWC activations for the 3x3 gather
+  const bf16* A;
+  const bf16* A1;    // conv: second input of a channel concatenation (or null)
+  int C0, C1;        // conv: channels of A and A1 (both multiples of 8)
+  int H, W;          // conv: image size (M = batch * H * W)
+  const bf16* B;     // [N, K] bf16
+  int M, N, K;       // K: a multiple of 8
+  int kSplit;        // K range per blockIdx.z (multiple of BK); gridDim.z partials
+  int epi;           // EPI_F32: C[z][M][N] f32 partials; EPI_BF16: out bf16 [M, N]
+  float* C;
+  bf16* out;
+  const float* bias; // + bias[n] (single K split only)
+  int relu;          // EPI_BF16: max(0, .)
+  int* status;       // set to 1 when a wait gives up
+};
+
+// 16 bytes of the A tile: row m (pixel), K chunk k8 (8 consecutive k)
+template <int AMODE>
+NN_DEV uint4 load_a_chunk(const GemmArgs& g, int m, int k) {
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (m >= g.M || k >= g.K) return v;
+  if (AMODE == A_DENSE) return *reinterpret_cast<const uint4*>(g.A + (size_t)m * g.K + k);
+  const int Ct = g.C0 + g.C1;
+  const int tap = k / Ct, c = k - tap * Ct;
+  const int hw = g.H * g.W;
+  const int b = m / hw, rem = m - b * hw, y = rem / g.W, x = rem - (rem / g.W) * g.W;
+  const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+  if (yy < 0 || yy >= g.H || xx < 0 || xx >= g.W) return v;
+  const size_t pix = ((size_t)b * g.H + yy) * g.W + xx;
+  if (c < g.C0) return *reinterpret_cast<const uint4*>(g.A + pix * g.C0 + c);
+  return *reinterpret_cast<const uint4*>(g.A1 + pix * g.C1 + (c - g.C0));
+}
+
+NN_DEV bool mbar_wait(uint32_t bar, uint32_t phase) {
+  uint32_t done = 0;
+  for (long i = 0; i < WAIT_LIMIT && !done; ++i) {
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+  }
+  return done != 0;
+}
+
+template <int BN, int AMODE>
+__global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // stage s: A tile (BM x BK) then B tile (BN x BK), K-major no-swizzle core matrices
+  constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + STAGES * STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + STAGES);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int kBegin = blockIdx.z * g.kSplit;
+  const int kEnd = min(g.K, kBegin + g.kSplit);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar + s)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  const uint32_t tmem = *tmem_slot;
+  constexpr uint32_t idesc = idesc_bf16(BM, BN);
+  bool ok = true;
+  int kb = 0;
+  for (int k0 = kBegin; k0 < kEnd; k0 += BK, ++kb) {
+    const int s = kb % STAGES;
+    uint8_t* sA = smem_raw + s * STAGE_BYTES;
+    uint8_t* sB = sA + A_BYTES;
+    if (kb >= STAGES) {  // the MMAs that last read this stage must be done
+      if (!mbar_wait(smem_u32(mbar + s), (uint32_t)((kb / STAGES - 1) & 1))) ok = false;
+    }
+    if (!__syncthreads_and(ok)) break;
+    for (int e = tid; e < BM * BK / 8; e += 128) {
+      const int r = e / (BK / 8), kc = e % (BK / 8);
+      const uint4 v = load_a_chunk<AMODE>(g, m0 + r, k0 + kc * 8);
+      *reinterpret_cast<uint4*>(sA + ((r >> 3) * (BK / 8) + kc) * 128 + (r & 7) * 16) = v;
+    }
+    for (int e = tid; e < BN * BK / 8; e += 128) {
+      const int r = e / (BK / 8), kc = e % (BK / 8);
+      const int gn = n0 + r, gk = k0 + kc * 8;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (gn < g.N && gk < kEnd) v = *reinterpret_cast<const uint4*>(g.B + (size_t)gn * g.K + gk);
+      *reinterpret_cast<uint4*>(sB + ((r >> 3) * (BK / 8) + kc) * 128 + (r & 7) * 16) = v;
+    }
+    // generic-proxy stores -> visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n");
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        // K = 16 per MMA: two core-matrix columns, 128 bytes apart
+        const uint64_t ad = smem_desc(smem_u32(sA) + kk * 256, 128, (BK / 8) * 128);
+        const uint64_t bd = smem_desc(smem_u32(sB) + kk * 256, 128, (BK / 8) * 128);
+        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+          smem_u32(mbar + s)));
+    }
+  }
+  // drain: the last MMAs of each stage
+  if (ok) {
+    for (int j = max(0, kb - STAGES); j < kb; ++j)
+      if (!mbar_wait(smem_u32(mbar + (j % STAGES)), (uint32_t)((j / STAGES) & 1))) ok = false;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  ok = __syncthreads_and(ok);
+  if (!ok) {
+    if (tid == 0 && g.status) atomicExch(g.status, 1);
+  } else if (kb > 0) {
+    // accumulator: TMEM lane = tile row (warp w owns lanes 32w..32w+31), column = n
+    const int gm = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t r[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (gm < g.M) {
+        if (g.epi == EPI_F32) {
+          float* crow = g.C + ((size_t)blockIdx.z * g.M + gm) * g.N;
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (n0 + c0 + j < g.N) crow[n0 + c0 + j] = __uint_as_float(r[j]) + (g.bias ? g.bias[n0 + c0 + j] : 0.f);
+        } else {
+          bf16* orow = g.out + (size_t)gm * g.N;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c0 + j;
+            if (n < g.N) {
+              float v = __uint_as_float(r[j]) + (g.bias ? g.bias[n] : 0.f);
+              if (g.relu) v = fmaxf(v, 0.f);
+              orow[n] = __float2bfloat16(v);
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
+}
+
+template <int BN, int AMODE>
+static cudaError_t launch_gemm_t(const GemmArgs& g, int splits, cudaStream_t st) {
+  const size_t smem = (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + STAGES * 8 + 16;
+  cudaError_t e = cudaFuncSetAttribute(gemm_kernel<BN, AMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((g.M + BM - 1) / BM, (g.N + BN - 1) / BN, splits);
+  gemm_kernel<BN, AMODE><<<grid, 128, smem, st>>>(g);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_gemm(const GemmArgs& g, int amode, int splits, cudaStream_t st) {
+  const int bn = g.N <= 32 ? 32 : g.N <= 64 ? 64 : g.N <= 128 ? 128 : 256;
+#define NN_CASE(b)                                                                         \
+  if (bn == b) return amode == A_CONV3 ? launch_gemm_t<b, A_CONV3>(g, splits, st)         \
+                                       : launch_gemm_t<b, A_DENSE>(g, splits, st);
+  NN_CASE(32)
+  NN_CASE(64)
+  NN_CASE(128)
+  NN_CASE(256)
+#undef NN_CASE
+  return cudaErrorInvalidValue;
+}
+
+// ------------------------------------------------------------------ helpers
+// partials [splits][M][N] -> out[M][N] (fixed order)
+__global__ void reduce_splits_kernel(const float* part, float* out, size_t n, int splits) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int z = 0; z < splits; ++z) s += part[(size_t)z * n + i];
+  out[i] = s;
+}
+
+// im2col of a 3x3 'same' patch, transposed: colT[k][m], k = tap * Ct + c
+// (channels of X then X1), m = pixel; rows k >= 9 Ct (padding to Kpad) are zero
+__global__ void im2col_t_kernel(const bf16* X, const bf16* X1, int C0, int C1, int Bn, int H, int W, int Kpad,
+                                bf16* colT) {
+  const size_t M = (size_t)Bn * H * W;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M * Kpad) return;
+  const int k = (int)(i / M);
+  const size_t m = i - (size_t)k * M;
+  const int Ct = C0 + C1;
+  bf16 v = __float2bfloat16(0.f);
+  if (k < 9 * Ct) {
+    const int tap = k / Ct, c = k - tap * Ct;
+    const int hw = H * W;
+    const int b = (int)(m / hw), rem = (int)(m - (size_t)b * hw), y = rem / W, x = rem % W;
+    const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+    if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
+      const size_t pix = ((size_t)b * H + yy) * W + xx;
+      v = c < C0 ? X[pix * C0 + c] : X1[pix * C1 + (c - C0)];
+    }
+  }
+  colT[i] = v;
+}
+
+// im2col of a one-channel image into a dense [M][Kpad] matrix (the first layer)
+__global__ void im2col1_kernel(const bf16* X, int Bn, int H, int W, int Kpad, bf16* col) {
+  const size_t M = (size_t)Bn * H * W;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M * Kpad) return;
+  const size_t m = i / Kpad;
+  const int k = (int)(i - m * Kpad);
+  bf16 v = __float2bfloat16(0.f);
+  if (k < 9) {
+    const int hw = H * W;
+    const int b = (int)(m / hw), rem = (int)(m - (size_t)b * hw), y = rem / W, x = rem % W;
+    const int yy = y + k / 3 - 1, xx = x + k % 3 - 1;
+    if (yy >= 0 && yy < H && xx >= 0 && xx < W) v = X[((size_t)b * H + yy) * W + xx];
+  }
+  col[i] = v;
+}
+
+__global__ void transpose_kernel(const bf16* in, bf16* out, int R, int Cc) {
+  __shared__ bf16 t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = r0 + j, c = c0 + threadIdx.x;
+    if (r < R && c < Cc) t[j][threadIdx.x] = in[(size_t)r * Cc + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int c = c0 + j, r = r0 + threadIdx.x;
+    if (c < Cc && r < R) out[(size_t)c * R + r] = t[threadIdx.x][j];
+  }
+}
+
+// W [Co][9][Ci] -> W' [Ci][9][Co] with the taps flipped: the weights of the
+// backward-data convolution
+__global__ void flip_weights_kernel(const bf16* w, bf16* wf, int Co, int Ci) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Co * 9 * Ci) return;
+  const int co = i / (9 * Ci), rem = i - co * 9 * Ci, tap = rem / Ci, ci = rem - (rem / Ci) * Ci;
+  wf[((size_t)ci * 9 + (8 - tap)) * Co + co] = w[i];
+}
+
+// dPre = dY * (Y > 0) (ReLU backward, Y the bf16 forward output), cast to bf16
+__global__ void relu_bwd_kernel(const float* dy, const bf16* y, bf16* dpre, float* dpre_f32, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = __bfloat162float(y[i]) > 0.f ? dy[i] : 0.f;
+  dpre[i] = __float2bfloat16(g);
+  if (dpre_f32) dpre_f32[i] = g;
+}
+
+// db[n] = sum_m d[m][n]: one block per column group, fixed order
+__global__ void col_sum_kernel(const float* d, float* out, int M, int N) {
+  const int n = blockIdx.x;
+  double s = 0.0;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) s += (double)d[(size_t)m * N + n];
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = (float)red[0];
+}
+
+// 2x2 average pooling, NHWC
+__global__ void pool2_kernel(const bf16* x, bf16* y, int Bn, int H, int W, int C) {
+  const size_t n = (size_t)Bn * (H / 2) * (W / 2) * C;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = (int)(i % C);
+  size_t p = i / C;
+  const int xo = (int)(p % (W / 2));
+  p /= (W / 2);
+  const int yo = (int)(p % (H / 2));
+  const int b = (int)(p / (H / 2));
+  float s = 0.f;
+  for (int dy = 0; dy < 2; ++dy)
+    for (int dx = 0; dx < 2; ++dx) s += __bfloat162float(x[(((size_t)b * H + 2 * yo + dy) * W + 2 * xo + dx) * C + c]);
+  y[i] = __float2bfloat16(0.25f * s);
+}
+
+__global__ void pool2_bwd_kernel(const float* dy, float* dx, int Bn, int H, int W, int C) {
+  const size_t n = (size_t)Bn * H * W * C;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = (int)(i % C);
+  size_t p = i / C;
+  const int x = (int)(p % W);
+  p /= W;
+  const int y = (int)(p % H);
+  const int b = (int)(p / H);
+  dx[i] += 0.25f * dy[(((size_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c];
+}
+
+// nearest 2x upsampling, NHWC (H, W: the input size)
+__global__ void up2_kernel(const bf16* in, bf16* out, int Bn, int H, int W, int C) {
+  const size_t n = (size_t)Bn * 2 * H * 2 * W * C;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = (int)(i % C);
+  size_t p = i / C;
+  const int x = (int)(p % (2 * W));
+  p /= (2 * W);
+  const int y = (int)(p % (2 * H));
+  const int b = (int)(p / (2 * H));
+  out[i] = in[(((size_t)b * H + y / 2) * W + x / 2) * C + c];
+}
+
+__global__ void up2_bwd_kernel(const float* dy, float* dx, int Bn, int H, int W, int C, int ldy, int coff) {
+  // dy: [Bn, 2H, 2W, ldy] with this tensor's channels at [coff, coff + C)
+  const size_t n = (size_t)Bn * H * W * C;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = (int)(i % C);
+  size_t p = i / C;
+  const int x = (int)(p % W);
+  p /= W;
+  const int y = (int)(p % H);
+  const int b = (int)(p / H);
+  float s = 0.f;
+  for (int dyy = 0; dyy < 2; ++dyy)
+    for (int dxx = 0; dxx < 2; ++dxx)
+      s += dy[(((size_t)b * 2 * H + 2 * y + dyy) * 2 * W + 2 * x + dxx) * ldy + coff + c];
+  dx[i] = s;
+}
+
+// dst[m][c] (+)= src[m][coff + c], c < C: a channel slice of a concatenation's gradient
+__global__ void slice_add_kernel(const float* src, int ldsrc, int coff, float* dst, int C, size_t M, int accumulate) {
+  const size_t n = M * C;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const size_t m = i / C;
+  const int c = (int)(i - m * C);
+  const float v = src[m * ldsrc + coff + c];
+  dst[i] = accumulate ? dst[i] + v : v;
+}
+
+__global__ void cast_kernel(const float* x, bf16* y, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = __float2bfloat16(x[i]);
+}
+
+// Adam on FP32 master weights, BF16 copy for the tensor cores
+__global__ void adam_kernel(float* p, const float* g, float* m, float* v, bf16* p16, size_t n, float lr, float b1,
+                            float b2, float eps, float c1, float c2, float wd) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i] + wd * p[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  p[i] = pi;
+  if (p16) p16[i] = __float2bfloat16(pi);
+}
+
+static unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace nn
+}  // namespace ptyg
+
+using namespace ptyg::nn;
+
+static int nn_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return PTYG_OK;
+  char msg[256];
+  snprintf(msg, sizeof msg, "%s: %s", what, cudaGetErrorString(e));
+  return ptyg::set_last_error(PTYG_ERR_CUDA, msg);
+}
+
+extern "C" int ptyg_nn_gemm(const void* A, const void* B, int M, int N, int K, int splits, float* C, void* out,
+                            const float* bias, int relu, int* status, void* stream) {
+  if (!A || !B || M < 1 || N < 1 || K < 1 || (K % 8) || splits < 1 || (!C && !out))
+    return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_gemm: bad arguments (K must be a multiple of 8)");
+  if (((uintptr_t)A | (uintptr_t)B) % 16) return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_gemm: A, B not 16-byte aligned");
+  GemmArgs g = {};
+  g.A = (const bf16*)A;
+  g.B = (const bf16*)B;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  const int kb = (K + BK - 1) / BK;
+  if (splits > kb) splits = kb;
+  g.kSplit = ((kb + splits - 1) / splits) * BK;
+  splits = (K + g.kSplit - 1) / g.kSplit;
+  g.epi = out ? EPI_BF16 : EPI_F32;
+  if ((out || bias) && splits > 1)
+    return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_gemm: bf16 output and bias need splits = 1");
+  g.C = C;
+  g.out = (bf16*)out;
+  g.bias = bias;
+  g.relu = relu;
+  g.status = status;
+  return nn_check(launch_gemm(g, A_DENSE, splits, (cudaStream_t)stream), "ptyg_nn_gemm");
+}
+
+extern "C" int ptyg_nn_conv3(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, const void* Wt,
+                             int Co, float* C, void* out, const float* bias, int relu, int* status, void* stream) {
+  if (!X || !Wt || C0 < 8 || (C0 % 8) || (C1 % 8) || (C1 && !X1) || Bn < 1 || H < 1 || W < 1 || Co < 1 ||
+      (!C && !out))
+    return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_conv3: bad arguments (channels: multiples of 8)");
+  GemmArgs g = {};
+  g.A = (const bf16*)X;
+  g.A1 = (const bf16*)X1;
+  g.C0 = C0;
+  g.C1 = C1;
+  g.H = H;
+  g.W = W;
+  g.B = (const bf16*)Wt;
+  g.M = Bn * H * W;
+  g.N = Co;
+  g.K = 9 * (C0 + C1);
+  g.kSplit = ((g.K + BK - 1) / BK) * BK;
+  g.epi = out ? EPI_BF16 : EPI_F32;
+  g.C = C;
+  g.out = (bf16*)out;
+  g.bias = bias;
+  g.relu = relu;
+  g.status = status;
+  return nn_check(launch_gemm(g, A_CONV3, 1, (cudaStream_t)stream), "ptyg_nn_conv3");
+}
+
+extern "C" int ptyg_nn_reduce_splits(const float* part, float* out, int64_t n, int splits, void* stream) {
+  reduce_splits_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>(part, out, (size_t)n, splits);
+  return nn_check(cudaGetLastError(), "ptyg_nn_reduce_splits");
+}
+
+extern "C" int ptyg_nn_im2col_t(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, int Kpad,
+                                void* colT, void* stream) {
+  const size_t n = (size_t)Bn * H * W * Kpad;
+  im2col_t_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)X, (const bf16*)X1, C0, C1, Bn, H, W,
+                                                               Kpad, (bf16*)colT);
+  return nn_check(cudaGetLastError(), "ptyg_nn_im2col_t");
+}
+
+extern "C" int ptyg_nn_im2col1(const void* X, int Bn, int H, int W, int Kpad, void* col, void* stream) {
+  const size_t n = (size_t)Bn * H * W * Kpad;
+  im2col1_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)X, Bn, H, W, Kpad, (bf16*)col);
+  return nn_check(cudaGetLastError(), "ptyg_nn_im2col1");
+}
+
+extern "C" int ptyg_nn_transpose(const void* in, void* out, int R, int Cc, void* stream) {
+  dim3 grid((Cc + 31) / 32, (R + 31) / 32), block(32, 8);
+  transpose_kernel<<<grid, block, 0, (cudaStream_t)stream>>>((const bf16*)in, (bf16*)out, R, Cc);
+  return nn_check(cudaGetLastError(), "ptyg_nn_transpose");
+}
+
+extern "C" int ptyg_nn_flip_weights(const void* w, void* wf, int Co, int Ci, void* stream) {
+  flip_weights_kernel<<<blocks((size_t)Co * 9 * Ci), 256, 0, (cudaStream_t)stream>>>((const bf16*)w, (bf16*)wf, Co, Ci);
+  return nn_check(cudaGetLastError(), "ptyg_nn_flip_weights");
+}
+
+extern "C" int ptyg_nn_relu_bwd(const float* dy, const void* y, void* dpre, float* dpre_f32, int64_t n, void* stream) {
+  relu_bwd_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>(dy, (const bf16*)y, (bf16*)dpre, dpre_f32, (size_t)n);
+  return nn_check(cudaGetLastError(), "ptyg_nn_relu_bwd");
+}
+
+extern "C" int ptyg_nn_col_sum(const float* d, float* out, int M, int N, void* stream) {
+  col_sum_kernel<<<N, 256, 0, (cudaStream_t)stream>>>(d, out, M, N);
+  return nn_check(cudaGetLastError(), "ptyg_nn_col_sum");
+}
+
+extern "C" int ptyg_nn_pool2(const void* x, void* y, int Bn, int H, int W, int C, void* stream) {
+  pool2_kernel<<<blocks((size_t)Bn * H * W * C / 4), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)y, Bn, H,
+                                                                                     W, C);
+  return nn_check(cudaGetLastError(), "ptyg_nn_pool2");
+}
+
+extern "C" int ptyg_nn_pool2_bwd(const float* dy, float* dx, int Bn, int H, int W, int C, void* stream) {
+  pool2_bwd_kernel<<<blocks((size_t)Bn * H * W * C), 256, 0, (cudaStream_t)stream>>>(dy, dx, Bn, H, W, C);
+  return nn_check(cudaGetLastError(), "ptyg_nn_pool2_bwd");
+}
+
+extern "C" int ptyg_nn_up2(const void* x, void* y, int Bn, int H, int W, int C, void* stream) {
+  up2_kernel<<<blocks((size_t)Bn * H * W * C * 4), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)y, Bn, H, W,
+                                                                                   C);
+  return nn_check(cudaGetLastError(), "ptyg_nn_up2");
+}
+
+extern "C" int ptyg_nn_up2_bwd(const float* dy, float* dx, int Bn, int H, int W, int C, int ldy, int coff,
+                               void* stream) {
+  up2_bwd_kernel<<<blocks((size_t)Bn * H * W * C), 256, 0, (cudaStream_t)stream>>>(dy, dx, Bn, H, W, C, ldy, coff);
+  return nn_check(cudaGetLastError(), "ptyg_nn_up2_bwd");
+}
+
+extern "C" int ptyg_nn_slice_add(const float* src, int ldsrc, int coff, float* dst, int C, int64_t M, int accumulate,
+                                 void* stream) {
+  slice_add_kernel<<<blocks((size_t)M * C), 256, 0, (cudaStream_t)stream>>>(src, ldsrc, coff, dst, C, (size_t)M,
+                                                                            accumulate);
+  return nn_check(cudaGetLastError(), "ptyg_nn_slice_add");
+}
+
+extern "C" int ptyg_nn_cast_bf16(const float* x, void* y, int64_t n, void* stream) {
+  cast_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>(x, (bf16*)y, (size_t)n);
+  return nn_check(cudaGetLastError(), "ptyg_nn_cast_bf16");
+}
+
+extern "C" int ptyg_nn_adam(float* p, const float* g, float* m, float* v, void* p16, int64_t n, float lr, float b1,
+                            float b2, float eps, int step, float weight_decay, void* stream) {
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, (bf16*)p16, (size_t)n, lr, b1, b2, eps, c1, c2,
+                                                           weight_decay);
+  return nn_check(cudaGetLastError(), "ptyg_nn_adam");
+}
