@@ -74,7 +74,8 @@ class ScanSpec:
 
 
 def simulate_cpm(spec: ScanSpec):
-    """Return (ptychogram float32, encoder metres, true object, true probe, dxp)."""
+    """Return (ptychogram float32, encoder metres, true object, true probe, dxp);
+    the true probe is scaled to the photon count of the intensities."""
     rng = np.random.default_rng(spec.seed)
     Np, No = spec.Np, spec.No
     dxp = spec.wavelength * spec.zo / (Np * spec.dxd)
@@ -93,14 +94,18 @@ def simulate_cpm(spec: ScanSpec):
     if spec.npsm == 1:
         probe = ((r < R) * np.exp(1j * 2 * np.pi * (r / R) ** 2))[None]
     else:
+        # Hermite-Gauss modes whose fundamental falls to 1/e in amplitude at
+        # the pupil radius R, the footprint of the circular pupil guess
         powers = [1.0 / 2**m for m in range(spec.npsm)]
-        probe = hermite_gauss_modes(Np, R / 2, spec.npsm, powers) * np.exp(1j * 2 * np.pi * (r / R) ** 2)
+        probe = hermite_gauss_modes(Np, R / np.sqrt(2), spec.npsm, powers) * np.exp(1j * 2 * np.pi * (r / R) ** 2)
     rows_cols = np.round(encoder / dxp).astype(int) + No // 2 - Np // 2
     I = np.empty((spec.num_positions, Np, Np), np.float64)
     for j, (py, px) in enumerate(rows_cols):
         patch = obj[py : py + Np, px : px + Np]
         I[j] = np.sum(np.abs(fft2c(patch[None] * probe)) ** 2, axis=0)
-    I *= spec.photons / I.max()
+    scale = spec.photons / I.max()
+    I *= scale
+    probe = probe * np.sqrt(scale)  # the probe that generates these intensities
     I = rng.poisson(I).astype(np.float32)
     return I, encoder, obj, probe, dxp
 
