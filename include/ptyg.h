@@ -304,6 +304,15 @@ PTYG_API int ptyg_nn_gemm(const void* A, const void* B, int M, int N, int K, int
 PTYG_API int ptyg_nn_conv3(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, const void* Wt, int Co,
                            float* C, void* out, const float* bias, int relu, int* status, void* stream);
 
+/* Weight gradients of a 3x3 convolution: C[z][Co][9 (C0 + C1)] = partial sums
+ * over `splits` pixel ranges of dY[p][co] times the patches of X (+ X1) at
+ * pixel p; H and W powers of two.  No transposes: both operands are read
+ * in NHWC order. */
+PTYG_API int ptyg_nn_conv3_wgrad(const void* dY, int Co, const void* X, const void* X1, int C0, int C1, int Bn, int H,
+                                 int W, int splits, float* C, void* status, void* stream);
+/* ... and of a dense layer: C[z][Co][K] = sum over pixel ranges of dY[p][co] X[p][k] */
+PTYG_API int ptyg_nn_dense_wgrad(const void* dY, int Co, const void* X, int K, int P, int splits, float* C,
+                                 void* status, void* stream);
 PTYG_API int ptyg_nn_reduce_splits(const float* part, float* out, int64_t n, int splits, void* stream);
 /* colT [Kpad][Bn H W]: the transposed 3x3 patch matrix (rows >= 9 (C0 + C1) zero) */
 PTYG_API int ptyg_nn_im2col_t(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, int Kpad,
@@ -314,7 +323,8 @@ PTYG_API int ptyg_nn_transpose(const void* in, void* out, int R, int C, void* st
 /* W [Co][9][Ci] -> Wf [Ci][9][Co] with the taps flipped (backward-data weights) */
 PTYG_API int ptyg_nn_flip_weights(const void* w, void* wf, int Co, int Ci, void* stream);
 PTYG_API int ptyg_nn_relu_bwd(const float* dy, const void* y, void* dpre, float* dpre_f32, int64_t n, void* stream);
-PTYG_API int ptyg_nn_col_sum(const float* d, float* out, int M, int N, void* stream);
+/* out[n] = sum_m d[m][n] (N divides 256); part: scratch of ceil(M / 1024) * N floats */
+PTYG_API int ptyg_nn_col_sum(const float* d, float* part, float* out, int M, int N, void* stream);
 PTYG_API int ptyg_nn_pool2(const void* x, void* y, int Bn, int H, int W, int C, void* stream);
 PTYG_API int ptyg_nn_pool2_bwd(const float* dy, float* dx, int Bn, int H, int W, int C, void* stream);
 PTYG_API int ptyg_nn_up2(const void* x, void* y, int Bn, int H, int W, int C, void* stream);

@@ -156,6 +156,10 @@ _SIGNATURES = {
                      C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_nn_conv3": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_nn_conv3_wgrad": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                            C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],
+    "ptyg_nn_dense_wgrad": [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                            C.c_void_p],
     "ptyg_nn_reduce_splits": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p],
     "ptyg_nn_im2col_t": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
                          C.c_void_p],
@@ -163,7 +167,7 @@ _SIGNATURES = {
     "ptyg_nn_transpose": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p],
     "ptyg_nn_flip_weights": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p],
     "ptyg_nn_relu_bwd": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p],
-    "ptyg_nn_col_sum": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p],
+    "ptyg_nn_col_sum": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p],
     "ptyg_nn_pool2": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p],
     "ptyg_nn_pool2_bwd": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p],
     "ptyg_nn_up2": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p],

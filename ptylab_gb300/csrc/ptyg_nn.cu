@@ -51,7 +51,7 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-constexpr int BM = 128, BK = 64, STAGES = 2;
+constexpr int BM = 128, BK = 64, STAGES = 4;
 constexpr long WAIT_LIMIT = 1L << 26;  // try_wait polls before an MMA wait is declared lost
 
 enum AMode { A_DENSE = 0, A_CONV3 = 1 };
@@ -74,23 +74,6 @@ struct GemmArgs {
   int* status;       // set to 1 when a wait gives up
 };
 
-// 16 bytes of the A tile: row m (pixel), K chunk k8 (8 consecutive k)
-template <int AMODE>
-NN_DEV uint4 load_a_chunk(const GemmArgs& g, int m, int k) {
-  uint4 v = make_uint4(0u, 0u, 0u, 0u);
-  if (m >= g.M || k >= g.K) return v;
-  if (AMODE == A_DENSE) return *reinterpret_cast<const uint4*>(g.A + (size_t)m * g.K + k);
-  const int Ct = g.C0 + g.C1;
-  const int tap = k / Ct, c = k - tap * Ct;
-  const int hw = g.H * g.W;
-  const int b = m / hw, rem = m - b * hw, y = rem / g.W, x = rem - (rem / g.W) * g.W;
-  const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-  if (yy < 0 || yy >= g.H || xx < 0 || xx >= g.W) return v;
-  const size_t pix = ((size_t)b * g.H + yy) * g.W + xx;
-  if (c < g.C0) return *reinterpret_cast<const uint4*>(g.A + pix * g.C0 + c);
-  return *reinterpret_cast<const uint4*>(g.A1 + pix * g.C1 + (c - g.C0));
-}
-
 NN_DEV bool mbar_wait(uint32_t bar, uint32_t phase) {
   uint32_t done = 0;
   for (long i = 0; i < WAIT_LIMIT && !done; ++i) {
@@ -101,6 +84,67 @@ NN_DEV bool mbar_wait(uint32_t bar, uint32_t phase) {
         : "memory");
   }
   return done != 0;
+}
+
+// 16-byte asynchronous copy global -> shared; src_bytes = 0 writes zeros
+NN_DEV void cp16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+NN_DEV void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+NN_DEV void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Thread t of the 128 stages, for every K block, the 16-byte chunks of tile
+// rows t/8 + 16 i (A: i < 8; B: i < BN/16), K chunk t % 8.  The pixel
+// coordinates of its A rows are fixed for the whole tile, so the conv gather
+// costs one division per K block, not per chunk.
+struct RowInfo {
+  int y[8], x[8];   // conv: pixel row/column (y = -1e6 for rows past M)
+  size_t base[8];   // conv: pixel index of (b, 0, 0); dense: row offset m * K
+};
+
+template <int BN, int AMODE>
+NN_DEV void load_stage(const GemmArgs& g, const RowInfo& ri, uint32_t sA, uint32_t sB, int k0, int kEnd, int n0,
+                       int tid) {
+  const int kc = tid & 7, rb = tid >> 3;
+  const int k = k0 + kc * 8;
+  const uint32_t coff = (uint32_t)(kc * 128);
+  if (AMODE == A_DENSE) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = rb + 16 * i;
+      const bool ok = ri.y[i] >= 0 && k < g.K;
+      const bf16* src = ok ? g.A + ri.base[i] + k : g.A;
+      cp16(sA + (uint32_t)((r >> 3) * (BK / 8) * 128) + coff + (uint32_t)((r & 7) * 16), src, ok ? 16u : 0u);
+    }
+  } else {
+    const int Ct = g.C0 + g.C1;
+    const int tap = k / Ct, c = k - tap * Ct;
+    const int dy = tap / 3 - 1, dx = tap - (tap / 3) * 3 - 1;
+    const bool kin = k < g.K;
+    const bool first = c < g.C0;
+    const bf16* X = first ? g.A : g.A1;
+    const int Cx = first ? g.C0 : g.C1;
+    const int cx = first ? c : c - g.C0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = rb + 16 * i;
+      const int yy = ri.y[i] + dy, xx = ri.x[i] + dx;
+      const bool ok = kin && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
+      const bf16* src = ok ? X + (ri.base[i] + (size_t)yy * g.W + xx) * Cx + cx : g.A;
+      cp16(sA + (uint32_t)((r >> 3) * (BK / 8) * 128) + coff + (uint32_t)((r & 7) * 16), src, ok ? 16u : 0u);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < BN / 16; ++i) {
+    const int r = rb + 16 * i;
+    const int gn = n0 + r;
+    const bool ok = gn < g.N && k < kEnd;
+    const bf16* src = ok ? g.B + (size_t)gn * g.K + k : g.B;
+    cp16(sB + (uint32_t)((r >> 3) * (BK / 8) * 128) + coff + (uint32_t)((r & 7) * 16), src, ok ? 16u : 0u);
+  }
 }
 
 template <int BN, int AMODE>
@@ -114,6 +158,29 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int kBegin = blockIdx.z * g.kSplit;
   const int kEnd = min(g.K, kBegin + g.kSplit);
+  const int nkb = (kEnd - kBegin + BK - 1) / BK;
+  const uint32_t smem0 = smem_u32(smem_raw);
+
+  RowInfo ri;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int m = m0 + (tid >> 3) + 16 * i;
+    if (m >= g.M) {
+      ri.y[i] = -(1 << 20);
+      ri.x[i] = 0;
+      ri.base[i] = 0;
+    } else if (AMODE == A_DENSE) {
+      ri.y[i] = 0;
+      ri.x[i] = 0;
+      ri.base[i] = (size_t)m * g.K;
+    } else {
+      const int hw = g.H * g.W;
+      const int b = m / hw, rem = m - b * hw;
+      ri.y[i] = rem / g.W;
+      ri.x[i] = rem - ri.y[i] * g.W;
+      ri.base[i] = (size_t)b * hw;
+    }
+  }
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
@@ -124,43 +191,47 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
     for (int s = 0; s < STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar + s)));
     asm volatile("fence.mbarrier_init.release.cluster;\n");
   }
+  // prologue: stages 0 .. STAGES-2 in flight
+#pragma unroll
+  for (int s = 0; s < STAGES - 1; ++s) {
+    if (s < nkb)
+      load_stage<BN, AMODE>(g, ri, smem0 + s * STAGE_BYTES, smem0 + s * STAGE_BYTES + A_BYTES, kBegin + s * BK, kEnd, n0,
+                            tid);
+    cp_commit();
+  }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n");
   const uint32_t tmem = *tmem_slot;
   constexpr uint32_t idesc = idesc_bf16(BM, BN);
   bool ok = true;
-  int kb = 0;
-  for (int k0 = kBegin; k0 < kEnd; k0 += BK, ++kb) {
+  for (int kb = 0; kb < nkb; ++kb) {
     const int s = kb % STAGES;
-    uint8_t* sA = smem_raw + s * STAGE_BYTES;
-    uint8_t* sB = sA + A_BYTES;
-    if (kb >= STAGES) {  // the MMAs that last read this stage must be done
-      if (!mbar_wait(smem_u32(mbar + s), (uint32_t)((kb / STAGES - 1) & 1))) ok = false;
+    // refill the stage the MMAs of kb - 1 read, once they are done
+    const int kn = kb + STAGES - 1;
+    if (kn < nkb) {
+      const int sn = kn % STAGES;
+      if (kb >= 1 && !mbar_wait(smem_u32(mbar + sn), (uint32_t)(((kb - 1) / STAGES) & 1))) ok = false;
+      if (ok)
+        load_stage<BN, AMODE>(g, ri, smem0 + sn * STAGE_BYTES, smem0 + sn * STAGE_BYTES + A_BYTES, kBegin + kn * BK,
+                              kEnd, n0, tid);
     }
-    if (!__syncthreads_and(ok)) break;
-    for (int e = tid; e < BM * BK / 8; e += 128) {
-      const int r = e / (BK / 8), kc = e % (BK / 8);
-      const uint4 v = load_a_chunk<AMODE>(g, m0 + r, k0 + kc * 8);
-      *reinterpret_cast<uint4*>(sA + ((r >> 3) * (BK / 8) + kc) * 128 + (r & 7) * 16) = v;
-    }
-    for (int e = tid; e < BN * BK / 8; e += 128) {
-      const int r = e / (BK / 8), kc = e % (BK / 8);
-      const int gn = n0 + r, gk = k0 + kc * 8;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (gn < g.N && gk < kEnd) v = *reinterpret_cast<const uint4*>(g.B + (size_t)gn * g.K + gk);
-      *reinterpret_cast<uint4*>(sB + ((r >> 3) * (BK / 8) + kc) * 128 + (r & 7) * 16) = v;
-    }
-    // generic-proxy stores -> visible to the tensor core (async proxy)
+    cp_commit();
+    cp_wait<STAGES - 1>();  // this thread's copies for stage s have landed
+    // generic-proxy writes -> visible to the tensor core (async proxy)
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n");
+      const uint32_t sA = smem0 + s * STAGE_BYTES, sB = sA + A_BYTES;
 #pragma unroll
       for (int kk = 0; kk < BK / 16; ++kk) {
         // K = 16 per MMA: two core-matrix columns, 128 bytes apart
-        const uint64_t ad = smem_desc(smem_u32(sA) + kk * 256, 128, (BK / 8) * 128);
-        const uint64_t bd = smem_desc(smem_u32(sB) + kk * 256, 128, (BK / 8) * 128);
+        const uint64_t ad = smem_desc(sA + kk * 256, 128, (BK / 8) * 128);
+        const uint64_t bd = smem_desc(sB + kk * 256, 128, (BK / 8) * 128);
         const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
         asm volatile(
             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -171,16 +242,18 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
           smem_u32(mbar + s)));
     }
   }
-  // drain: the last MMAs of each stage
+  cp_wait<0>();
+  // drain: the last MMAs (each stage's last commit not yet waited for)
   if (ok) {
-    for (int j = max(0, kb - STAGES); j < kb; ++j)
+    // the loop waited for commit j exactly when j + STAGES < nkb (before refilling its stage)
+    for (int j = max(0, nkb - STAGES); j < nkb; ++j)
       if (!mbar_wait(smem_u32(mbar + (j % STAGES)), (uint32_t)((j / STAGES) & 1))) ok = false;
   }
   asm volatile("tcgen05.fence::after_thread_sync;\n");
   ok = __syncthreads_and(ok);
   if (!ok) {
     if (tid == 0 && g.status) atomicExch(g.status, 1);
-  } else if (kb > 0) {
+  } else if (nkb > 0) {
     // accumulator: TMEM lane = tile row (warp w owns lanes 32w..32w+31), column = n
     const int gm = m0 + warp * 32 + lane;
 #pragma unroll 1
@@ -196,23 +269,40 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
             "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      if (gm < g.M) {
-        if (g.epi == EPI_F32) {
-          float* crow = g.C + ((size_t)blockIdx.z * g.M + gm) * g.N;
+      if (gm >= g.M) continue;
+      const int nb = n0 + c0;
+      float v[32];
 #pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (n0 + c0 + j < g.N) crow[n0 + c0 + j] = __uint_as_float(r[j]) + (g.bias ? g.bias[n0 + c0 + j] : 0.f);
+      for (int j = 0; j < 32; ++j) {
+        v[j] = __uint_as_float(r[j]);
+        if (g.bias && nb + j < g.N) v[j] += g.bias[nb + j];
+        if (g.epi == EPI_BF16 && g.relu) v[j] = fmaxf(v[j], 0.f);
+      }
+      const bool full = nb + 32 <= g.N && (g.N & 7) == 0;
+      if (g.epi == EPI_F32) {
+        float* crow = g.C + ((size_t)blockIdx.z * g.M + gm) * g.N + nb;
+        if (full) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(crow + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
         } else {
-          bf16* orow = g.out + (size_t)gm * g.N;
+          for (int j = 0; j < 32 && nb + j < g.N; ++j) crow[j] = v[j];
+        }
+      } else {
+        bf16* orow = g.out + (size_t)gm * g.N + nb;
+        if (full) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int n = n0 + c0 + j;
-            if (n < g.N) {
-              float v = __uint_as_float(r[j]) + (g.bias ? g.bias[n] : 0.f);
-              if (g.relu) v = fmaxf(v, 0.f);
-              orow[n] = __float2bfloat16(v);
-            }
+          for (int j = 0; j < 32; j += 8) {
+            uint4 q;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(v[j], v[j + 1]), h1 = __floats2bfloat162_rn(v[j + 2], v[j + 3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(v[j + 4], v[j + 5]), h3 = __floats2bfloat162_rn(v[j + 6], v[j + 7]);
+            q.x = *reinterpret_cast<uint32_t*>(&h0);
+            q.y = *reinterpret_cast<uint32_t*>(&h1);
+            q.z = *reinterpret_cast<uint32_t*>(&h2);
+            q.w = *reinterpret_cast<uint32_t*>(&h3);
+            *reinterpret_cast<uint4*>(orow + j) = q;
           }
+        } else {
+          for (int j = 0; j < 32 && nb + j < g.N; ++j) orow[j] = __float2bfloat16(v[j]);
         }
       }
     }
@@ -220,6 +310,242 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
+}
+
+// ------------------------------------------------------------------ weight gradients
+// dW[co][k] = sum_pixels dY[pixel][co] P[pixel][k], P the 3x3 patch matrix of X
+// (or a dense [pixels][K] matrix): a GEMM whose contraction runs over pixels,
+// with both operands staged MN-major (the 16 contiguous bytes run along co,
+// resp. k), so dY and X are read in their NHWC order with no transposes and no
+// materialised patch matrix.  MN-major no-swizzle core matrices: 8 K rows
+// (pixels) x 16 bytes (8 co, resp. 8 k); core (mn, kc) at (kc * R/8 + mn) * 128
+// bytes; the descriptor's leading offset is the K-direction stride (R/8 * 128),
+// the stride offset the MN-direction one (128 bytes).  Every MMA reads within
+// its stage: largest offset (2 kk + 1) * R/8 * 128 + (R/8 - 1) * 128 + 127 =
+// R * 128 - 1 at kk = 3, the size of an R x 64 tile.
+struct DwArgs {
+  const bf16* dY;    // [P][Co] (row stride Co)
+  int Co;
+  const bf16* X;     // conv: NHWC [P][C0] (+ X1 [P][C1]); dense: [P][K]
+  const bf16* X1;
+  int C0, C1;
+  int lgW, lgHW, H, W;  // conv: log2 of the width and of the image size (powers of two)
+  int K;             // columns of dW (9 (C0 + C1) for conv)
+  int P;             // pixels (the contraction)
+  int pSplit;        // pixels per blockIdx.z (multiple of BK)
+  float* C;          // [splits][Co][K]
+  int* status;
+};
+
+// The B-operand column a thread loads is the same for every pixel block
+// (its 8 k values at n0 + (t % (BN/8)) * 8): tap, channel and source tensor
+// are worked out once.
+struct DwCol {
+  bool kin;
+  int dy, dx, Cx, cx;
+  const bf16* X;
+};
+
+template <int BN, bool CONV>
+NN_DEV DwCol dw_column(const DwArgs& g, int k0, int tid) {
+  DwCol d;
+  const int k = k0 + (tid % (BN / 8)) * 8;
+  d.kin = k < g.K;
+  if (!CONV) {
+    d.dy = d.dx = 0;
+    d.Cx = g.K;
+    d.cx = k;
+    d.X = g.X;
+  } else {
+    const int Ct = g.C0 + g.C1;
+    const int tap = d.kin ? k / Ct : 0, c = d.kin ? k - tap * Ct : 0;
+    d.dy = tap / 3 - 1;
+    d.dx = tap - (tap / 3) * 3 - 1;
+    const bool first = c < g.C0;
+    d.X = first ? g.X : g.X1;
+    d.Cx = first ? g.C0 : g.C1;
+    d.cx = first ? c : c - g.C0;
+  }
+  return d;
+}
+
+template <int BN, bool CONV>
+NN_DEV void dw_load_stage(const DwArgs& g, const DwCol& col, uint32_t sA, uint32_t sB, int p0, int pEnd, int co0,
+                          int tid) {
+  // A: 64 pixels x 128 co, chunk (pixel p, co chunk mc): thread t -> mc = t % 16, p = t / 16 + 8 i
+  {
+    const int mc = tid & 15;
+    const int co = co0 + mc * 8;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int p = (tid >> 4) + 8 * i;
+      const int pix = p0 + p;
+      const bool ok = pix < pEnd && co < g.Co;
+      const bf16* src = ok ? g.dY + (size_t)pix * g.Co + co : g.dY;
+      cp16(sA + (uint32_t)(((p >> 3) * (BM / 8) + mc) * 128 + (p & 7) * 16), src, ok ? 16u : 0u);
+    }
+  }
+  // B: 64 pixels x BN k, chunk (pixel p, k chunk nc): thread t -> nc = t % (BN/8), p = t / (BN/8) + (128/(BN/8)) i
+  {
+    constexpr int NCH = BN / 8, PSTEP = 128 / NCH, NI = 64 / PSTEP;
+    const int nc = tid % NCH;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      const int p = tid / NCH + PSTEP * i;
+      const int pix = p0 + p;
+      bool ok = col.kin && pix < pEnd;
+      const bf16* src = g.X;
+      if (ok) {
+        if (!CONV) {
+          src = col.X + (size_t)pix * col.Cx + col.cx;
+        } else {
+          const int b = pix >> g.lgHW, rem = pix & ((1 << g.lgHW) - 1);
+          const int y = (rem >> g.lgW) + col.dy, x = (rem & ((1 << g.lgW) - 1)) + col.dx;
+          ok = y >= 0 && y < g.H && x >= 0 && x < g.W;
+          const size_t q = ((size_t)b << g.lgHW) + ((size_t)y << g.lgW) + x;
+          src = ok ? col.X + q * col.Cx + col.cx : g.X;
+        }
+      }
+      cp16(sB + (uint32_t)(((p >> 3) * NCH + nc) * 128 + (p & 7) * 16), src, ok ? 16u : 0u);
+    }
+  }
+}
+
+template <int BN, bool CONV>
+__global__ void __launch_bounds__(128, 1) dw_kernel(const DwArgs g) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + STAGES * STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + STAGES);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int co0 = blockIdx.x * BM, k0 = blockIdx.y * BN;
+  const int pBegin = blockIdx.z * g.pSplit;
+  const int pEnd = min(g.P, pBegin + g.pSplit);
+  const int nkb = (pEnd - pBegin + BK - 1) / BK;
+  const uint32_t smem0 = smem_u32(smem_raw);
+  const DwCol col = dw_column<BN, CONV>(g, k0, tid);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar + s)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n");
+  }
+#pragma unroll
+  for (int s = 0; s < STAGES - 1; ++s) {
+    if (s < nkb)
+      dw_load_stage<BN, CONV>(g, col, smem0 + s * STAGE_BYTES, smem0 + s * STAGE_BYTES + A_BYTES, pBegin + s * BK, pEnd,
+                              co0, tid);
+    cp_commit();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  const uint32_t tmem = *tmem_slot;
+  // MN-major A (bit 15) and B (bit 16)
+  constexpr uint32_t idesc = idesc_bf16(BM, BN) | (1u << 15) | (1u << 16);
+  constexpr uint32_t LBO_A = (BM / 8) * 128, LBO_B = (BN / 8) * 128;
+  bool ok = true;
+  for (int kb = 0; kb < nkb; ++kb) {
+    const int s = kb % STAGES;
+    const int kn = kb + STAGES - 1;
+    if (kn < nkb) {
+      const int sn = kn % STAGES;
+      if (kb >= 1 && !mbar_wait(smem_u32(mbar + sn), (uint32_t)(((kb - 1) / STAGES) & 1))) ok = false;
+      if (ok)
+        dw_load_stage<BN, CONV>(g, col, smem0 + sn * STAGE_BYTES, smem0 + sn * STAGE_BYTES + A_BYTES,
+                                pBegin + kn * BK, pEnd, co0, tid);
+    }
+    cp_commit();
+    cp_wait<STAGES - 1>();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n");
+      const uint32_t sA = smem0 + s * STAGE_BYTES, sB = sA + A_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        const uint64_t ad = smem_desc(sA + kk * 2 * LBO_A, LBO_A, 128);
+        const uint64_t bd = smem_desc(sB + kk * 2 * LBO_B, LBO_B, 128);
+        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+          smem_u32(mbar + s)));
+    }
+  }
+  cp_wait<0>();
+  if (ok) {
+    for (int j = max(0, nkb - STAGES); j < nkb; ++j)
+      if (!mbar_wait(smem_u32(mbar + (j % STAGES)), (uint32_t)((j / STAGES) & 1))) ok = false;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  ok = __syncthreads_and(ok);
+  if (!ok) {
+    if (tid == 0 && g.status) atomicExch(g.status, 1);
+  } else {
+    const int co = co0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t r[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (co < g.Co) {
+        float* crow = g.C + ((size_t)blockIdx.z * g.Co + co) * g.K + k0 + c0;
+        const bool full = k0 + c0 + 32 <= g.K && (g.K & 3) == 0;
+        if (full) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 4)
+            *reinterpret_cast<float4*>(crow + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
+                                                               __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]));
+        } else {
+          for (int j = 0; j < 32 && k0 + c0 + j < g.K; ++j) crow[j] = __uint_as_float(r[j]);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
+}
+
+template <int BN, bool CONV>
+static cudaError_t launch_dw_t(const DwArgs& g, int splits, cudaStream_t st) {
+  const size_t smem = (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + STAGES * 8 + 16;
+  cudaError_t e = cudaFuncSetAttribute(dw_kernel<BN, CONV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((g.Co + BM - 1) / BM, (g.K + BN - 1) / BN, splits);
+  dw_kernel<BN, CONV><<<grid, 128, smem, st>>>(g);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_dw(const DwArgs& g, bool conv, int splits, cudaStream_t st) {
+  const int bn = g.K <= 32 ? 32 : g.K <= 64 ? 64 : g.K <= 128 ? 128 : 256;
+#define NN_CASE(b)                                                                                          \
+  if (bn == b) return conv ? launch_dw_t<b, true>(g, splits, st) : launch_dw_t<b, false>(g, splits, st);
+  NN_CASE(32)
+  NN_CASE(64)
+  NN_CASE(128)
+  NN_CASE(256)
+#undef NN_CASE
+  return cudaErrorInvalidValue;
 }
 
 template <int BN, int AMODE>
@@ -328,19 +654,32 @@ __global__ void relu_bwd_kernel(const float* dy, const bf16* y, bf16* dpre, floa
   if (dpre_f32) dpre_f32[i] = g;
 }
 
-// db[n] = sum_m d[m][n]: one block per column group, fixed order
-__global__ void col_sum_kernel(const float* d, float* out, int M, int N) {
-  const int n = blockIdx.x;
-  double s = 0.0;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) s += (double)d[(size_t)m * N + n];
-  __shared__ double red[256];
+// db[n] = sum_m d[m][n] in two fixed-order passes: block b sums rows
+// [b R, (b+1) R) column-wise with coalesced reads (consecutive threads read
+// consecutive columns of a row; N divides 256), then one pass over the blocks.
+constexpr int COLSUM_ROWS = 1024;
+__global__ void col_sum_part_kernel(const float* d, float* part, int M, int N) {
+  __shared__ float red[256];
+  const int rpp = 256 / N;  // rows per pass
+  const int c = threadIdx.x % N, r0 = threadIdx.x / N;
+  const int m0 = blockIdx.x * COLSUM_ROWS, m1 = min(M, m0 + COLSUM_ROWS);
+  float s = 0.f;
+  for (int m = m0 + r0; m < m1; m += rpp) s += d[(size_t)m * N + c];
   red[threadIdx.x] = s;
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
+  if (threadIdx.x < N) {
+    float t = 0.f;
+    for (int j = 0; j < rpp; ++j) t += red[j * N + threadIdx.x];
+    part[(size_t)blockIdx.x * N + threadIdx.x] = t;
   }
-  if (threadIdx.x == 0) out[n] = (float)red[0];
+}
+
+__global__ void col_sum_final_kernel(const float* part, float* out, int nb, int N) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += (double)part[(size_t)b * N + n];
+  out[n] = (float)s;
 }
 
 // 2x2 average pooling, NHWC
@@ -537,8 +876,13 @@ extern "C" int ptyg_nn_relu_bwd(const float* dy, const void* y, void* dpre, floa
   return nn_check(cudaGetLastError(), "ptyg_nn_relu_bwd");
 }
 
-extern "C" int ptyg_nn_col_sum(const float* d, float* out, int M, int N, void* stream) {
-  col_sum_kernel<<<N, 256, 0, (cudaStream_t)stream>>>(d, out, M, N);
+extern "C" int ptyg_nn_col_sum(const float* d, float* part, float* out, int M, int N, void* stream) {
+  if (!d || !part || !out || N < 1 || N > 256 || (256 % N))
+    return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_col_sum: N must divide 256");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nb = (M + COLSUM_ROWS - 1) / COLSUM_ROWS;
+  col_sum_part_kernel<<<nb, 256, 0, st>>>(d, part, M, N);
+  col_sum_final_kernel<<<(N + 255) / 256, 256, 0, st>>>(part, out, nb, N);
   return nn_check(cudaGetLastError(), "ptyg_nn_col_sum");
 }
 
@@ -583,4 +927,58 @@ extern "C" int ptyg_nn_adam(float* p, const float* g, float* m, float* v, void* 
   adam_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, (bf16*)p16, (size_t)n, lr, b1, b2, eps, c1, c2,
                                                            weight_decay);
   return nn_check(cudaGetLastError(), "ptyg_nn_adam");
+}
+
+static int ilog2_exact(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return (1 << l) == v ? l : -1;
+}
+
+extern "C" int ptyg_nn_conv3_wgrad(const void* dY, int Co, const void* X, const void* X1, int C0, int C1, int Bn, int H,
+                                   int W, int splits, float* C, void* status, void* stream) {
+  const int lgW = ilog2_exact(W), lgHW = ilog2_exact(H * W);
+  if (!dY || !X || !C || Co < 8 || (Co % 8) || C0 < 8 || (C0 % 8) || (C1 % 8) || (C1 && !X1) || Bn < 1 || lgW < 0 ||
+      lgHW < 0 || splits < 1)
+    return ptyg::set_last_error(PTYG_ERR_INVALID,
+                                "ptyg_nn_conv3_wgrad: bad arguments (channels multiples of 8, H and W powers of two)");
+  DwArgs g = {};
+  g.dY = (const bf16*)dY;
+  g.Co = Co;
+  g.X = (const bf16*)X;
+  g.X1 = (const bf16*)X1;
+  g.C0 = C0;
+  g.C1 = C1;
+  g.lgW = lgW;
+  g.lgHW = lgHW;
+  g.H = H;
+  g.W = W;
+  g.K = 9 * (C0 + C1);
+  g.P = Bn * H * W;
+  const int pb = (g.P + BK - 1) / BK;
+  if (splits > pb) splits = pb;
+  g.pSplit = ((pb + splits - 1) / splits) * BK;
+  splits = (g.P + g.pSplit - 1) / g.pSplit;
+  g.C = C;
+  g.status = (int*)status;
+  return nn_check(launch_dw(g, true, splits, (cudaStream_t)stream), "ptyg_nn_conv3_wgrad");
+}
+
+extern "C" int ptyg_nn_dense_wgrad(const void* dY, int Co, const void* X, int K, int P, int splits, float* C,
+                                   void* status, void* stream) {
+  if (!dY || !X || !C || Co < 8 || (Co % 8) || K < 8 || (K % 8) || P < 1 || splits < 1)
+    return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_dense_wgrad: bad arguments (Co, K multiples of 8)");
+  DwArgs g = {};
+  g.dY = (const bf16*)dY;
+  g.Co = Co;
+  g.X = (const bf16*)X;
+  g.K = K;
+  g.P = P;
+  const int pb = (P + BK - 1) / BK;
+  if (splits > pb) splits = pb;
+  g.pSplit = ((pb + splits - 1) / splits) * BK;
+  splits = (P + g.pSplit - 1) / g.pSplit;
+  g.C = C;
+  g.status = (int*)status;
+  return nn_check(launch_dw(g, false, splits, (cudaStream_t)stream), "ptyg_nn_dense_wgrad");
 }

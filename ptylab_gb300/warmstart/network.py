@@ -158,6 +158,7 @@ class WarmStartNet:
         self.a, self.gbuf = a, g
         self.x16 = torch.empty(B * H * W, dtype=bf, device=dev)
         self.col1 = torch.empty(B * H * W, FIRST_K, dtype=bf, device=dev)
+        self.colsum = torch.empty(-(-(B * H * W) // 1024) * 256, dtype=f32, device=dev)  # column-sum partials
         self._shape = (B, H, W)
 
     # ---------------------------------------------------------------- forward
@@ -219,23 +220,19 @@ class WarmStartNet:
 
     # ---------------------------------------------------------------- backward
     def _splits(self, rows, cols, k):
+        """Pixel ranges for a weight-gradient GEMM: about four CTAs per SM in all."""
         tiles = max(1, -(-rows // 128)) * max(1, -(-cols // 256))
         return int(max(1, min(-(-k // 64), 600 // tiles)))
 
-    def _grad_w(self, name, dpre16, colT, k):
-        """dW [Co, k] = dpre^T . col over the batch (split over pixels, fixed-order reduction)."""
+    def _wgrad(self, name, launch, co, k, P):
+        """dW [co, k] of layer `name` from the split-over-pixels GEMM `launch(splits, partials)`."""
         torch = _torch()
-        M, co = dpre16.shape
-        dT = torch.empty(co, M, dtype=torch.bfloat16, device=self.device)
-        self._call("ptyg_nn_transpose", dpre16.data_ptr(), dT.data_ptr(), M, co)
-        s = self._splits(co, k, M)
-        # the split count ptyg_nn_gemm uses: K ranges of whole 64-blocks
-        kb = -(-M // 64)
-        s = min(s, kb)
-        used = -(-M // (-(-kb // s) * 64))
+        s = self._splits(co, k, P)
+        pb = -(-P // 64)
+        s = min(s, pb)
+        used = -(-P // (-(-pb // s) * 64))  # the split count the kernel uses (whole 64-pixel blocks)
         part = torch.empty(used, co, k, dtype=torch.float32, device=self.device)
-        self._call("ptyg_nn_gemm", dT.data_ptr(), colT.data_ptr(), co, k, M, s, part.data_ptr(), None, None, 0,
-                   self.status.data_ptr())
+        launch(s, part)
         self._call("ptyg_nn_reduce_splits", part.data_ptr(), self.W[name].g.data_ptr(), co * k, used)
 
     def _conv_bwd(self, name, srcs, lv, need_dx=True):
@@ -251,17 +248,15 @@ class WarmStartNet:
         dpre32 = torch.empty(M, co, dtype=torch.float32, device=self.device)
         self._call("ptyg_nn_relu_bwd", self.gbuf[name].data_ptr(), y.data_ptr(), dpre16.data_ptr(), dpre32.data_ptr(),
                    M * co)
-        self._call("ptyg_nn_col_sum", dpre32.data_ptr(), self.b[name].g.data_ptr(), M, co)
+        self._call("ptyg_nn_col_sum", dpre32.data_ptr(), self.colsum.data_ptr(), self.b[name].g.data_ptr(), M, co)
         x0 = self.a[srcs[0]]
         x1 = self.a[srcs[1]] if len(srcs) > 1 else None
         c0 = x0.shape[1]
         c1 = x1.shape[1] if x1 is not None else 0
         k = 9 * (c0 + c1)
-        colT = torch.empty(k, M, dtype=torch.bfloat16, device=self.device)
-        self._call("ptyg_nn_im2col_t", x0.data_ptr(), x1.data_ptr() if x1 is not None else None, c0, c1, B, h, w, k,
-                   colT.data_ptr())
-        self._grad_w(name, dpre16, colT, k)
-        del colT
+        self._wgrad(name, lambda s, part: self._call(
+            "ptyg_nn_conv3_wgrad", dpre16.data_ptr(), co, x0.data_ptr(), x1.data_ptr() if x1 is not None else None,
+            c0, c1, B, h, w, s, part.data_ptr(), self.status.data_ptr()), co, k, M)
         if not need_dx:
             return None
         wf = torch.empty(c0 + c1, 9 * co, dtype=torch.bfloat16, device=self.device)
@@ -284,10 +279,10 @@ class WarmStartNet:
         dh[:, :2] = dout.reshape(M, 2)
         dh16 = torch.empty(M, HEAD_PAD, dtype=torch.bfloat16, device=self.device)
         self._call("ptyg_nn_cast_bf16", dh.data_ptr(), dh16.data_ptr(), M * HEAD_PAD)
-        self._call("ptyg_nn_col_sum", dh.data_ptr(), self.b["head"].g.data_ptr(), M, HEAD_PAD)
-        actT = torch.empty(c1, M, dtype=torch.bfloat16, device=self.device)
-        self._call("ptyg_nn_transpose", self.a["d1b"].data_ptr(), actT.data_ptr(), M, c1)
-        self._grad_w("head", dh16, actT, c1)
+        self._call("ptyg_nn_col_sum", dh.data_ptr(), self.colsum.data_ptr(), self.b["head"].g.data_ptr(), M, HEAD_PAD)
+        self._wgrad("head", lambda s, part: self._call(
+            "ptyg_nn_dense_wgrad", dh16.data_ptr(), HEAD_PAD, self.a["d1b"].data_ptr(), c1, M, s, part.data_ptr(),
+            self.status.data_ptr()), HEAD_PAD, c1, M)
         wT = torch.empty(c1, HEAD_PAD, dtype=torch.bfloat16, device=self.device)
         self._call("ptyg_nn_transpose", self.W["head"].p16.data_ptr(), wT.data_ptr(), HEAD_PAD, c1)
         self._call("ptyg_nn_gemm", dh16.data_ptr(), wT.data_ptr(), M, c1, HEAD_PAD, 1, g["d1b"].data_ptr(), None,
@@ -347,10 +342,10 @@ class WarmStartNet:
         dpre32 = torch.empty(M, co, dtype=torch.float32, device=self.device)
         self._call("ptyg_nn_relu_bwd", self.gbuf["e1a"].data_ptr(), self.a["e1a"].data_ptr(), dpre16.data_ptr(),
                    dpre32.data_ptr(), M * co)
-        self._call("ptyg_nn_col_sum", dpre32.data_ptr(), self.b["e1a"].g.data_ptr(), M, co)
-        colT = torch.empty(FIRST_K, M, dtype=torch.bfloat16, device=self.device)
-        self._call("ptyg_nn_transpose", self.col1.data_ptr(), colT.data_ptr(), M, FIRST_K)
-        self._grad_w("e1a", dpre16, colT, FIRST_K)
+        self._call("ptyg_nn_col_sum", dpre32.data_ptr(), self.colsum.data_ptr(), self.b["e1a"].g.data_ptr(), M, co)
+        self._wgrad("e1a", lambda s, part: self._call(
+            "ptyg_nn_dense_wgrad", dpre16.data_ptr(), co, self.col1.data_ptr(), FIRST_K, M, s, part.data_ptr(),
+            self.status.data_ptr()), co, FIRST_K, M)
 
     # ---------------------------------------------------------------- training
     def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, weight_decay=0.0):
