@@ -28,6 +28,7 @@ rank 0 prints one JSON line.
 from __future__ import annotations
 
 import argparse
+import copy
 import ctypes as C
 import json
 import multiprocessing as mp
@@ -203,14 +204,14 @@ def run_gb300(args, rank, world, local_rank):
     G = args.scans if args.scans > 0 else max(1, maxc.value)
     iters = args.warmup + args.steps
 
-    def build_batch(nscans, seed0, throughput):
+    def build_batch(host_scans, seed0, throughput):
+        nscans = len(host_scans)
         keep, plan = [], C.c_void_p()
         _native.check(lib.ptyg_plan_create(C.byref(geometry(nscans, throughput)), C.byref(plan)))
-        mom_total = 0
         flag_counts = np.zeros(iters, dtype=np.int64)
         for s in range(nscans):
             seed = seed0 + s
-            d, p, rec = make_scan(seed)
+            d, p, rec = host_scans[s]
             t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)  # noqa: E731
             obj = t(rec.object, torch.complex64)
             prb = t(rec.probe, torch.complex64)
@@ -249,8 +250,11 @@ def run_gb300(args, rank, world, local_rank):
             torch.distributed.barrier()
         return e0.elapsed_time(e1) / 1e3
 
-    # batched, device-resident: the headline
-    plan, keep, flag_counts = build_batch(G, 1000 * rank + 1, 1)
+    # G scans of host data, used by the device-resident run and the end-to-end one
+    host_scans = [make_scan(1000 * rank + 1 + s) for s in range(G)]
+
+    # batched, device-resident: the kernel view
+    plan, keep, flag_counts = build_batch(host_scans, 1000 * rank + 1, 1)
     clocks = ClockSampler(local_rank)
     clocks.start()
     t = timed(plan, args.steps, args.warmup)
@@ -272,30 +276,50 @@ def run_gb300(args, rank, world, local_rank):
     out = {}
     if rank == 0:
         # one scan alone: latency view of the same kernel
-        plan1, keep1, _ = build_batch(1, 7, 0)
+        plan1, keep1, _ = build_batch([make_scan(7)], 7, 0)
         t1 = timed(plan1, min(args.steps, 50), args.warmup)
         lib.ptyg_plan_destroy(plan1)
         del keep1
         single = {"value": NPOS * min(args.steps, 50) / t1, "us_per_position": t1 / (min(args.steps, 50) * NPOS) * 1e6}
 
-        # end to end through the public API, host NumPy in and out
+        # end to end through the public API, host NumPy in and out: the same
+        # G scans as engines built the PtyLab way, reconstructed together
+        def engines_from(scans, n_it):
+            out = []
+            for d, p, rec in scans:
+                e = Engines.mPIE(copy.deepcopy(rec), d, copy.deepcopy(p), DummyMonitor())
+                e.alphaObject = e.alphaProbe = 0.25
+                e.numIterations = n_it
+                out.append(e)
+            return out
+
+        Engines.reconstruct_batch(engines_from(host_scans, args.warmup))
+        engs = engines_from(host_scans, args.steps)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        Engines.reconstruct_batch(engs)
+        torch.cuda.synchronize(dev)
+        te = time.perf_counter() - t0
+        d0, _, r0 = host_scans[0]
+        per_scan_h2d = d0.ptychogram.nbytes + 3 * r0.object.nbytes + 3 * r0.probe.nbytes + NPOS * 2 * 4
+        per_scan_d2h = 3 * r0.object.nbytes + 3 * r0.probe.nbytes + NPOS * NP * NP * 4
+        h2d = G * (per_scan_h2d + args.steps * NPOS * 5)
+        d2h = G * (per_scan_d2h + args.steps * NPOS * 8)
+        e2e = {"value": G * NPOS * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+               "d2h_bytes_per_step": int(d2h / args.steps), "scans": G,
+               "api": "ptylab_gb300.Engines.reconstruct_batch([Engines.mPIE(...) per scan]), NumPy in/out"}
+
+        # one scan through Engines.mPIE(...).reconstruct(): PtyLab's own call
+        n1 = min(args.steps, 50)
         d, p, rec = make_scan(99)
         eng = Engines.mPIE(rec, d, p, DummyMonitor())
-        eng.numIterations = args.warmup
-        eng.reconstruct()
-        d, p, rec = make_scan(99)
-        eng = Engines.mPIE(rec, d, p, DummyMonitor())
-        eng.numIterations = args.steps
+        eng.numIterations = n1
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         eng.reconstruct()
         torch.cuda.synchronize(dev)
-        te = time.perf_counter() - t0
-        h2d = d.ptychogram.nbytes + 3 * rec.object.nbytes + 3 * rec.probe.nbytes + NPOS * 2 * 4 + args.steps * NPOS * 5
-        d2h = 3 * rec.object.nbytes + 3 * rec.probe.nbytes + args.steps * NPOS * 8 + NPOS * NP * NP * 4
-        e2e = {"value": NPOS * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
-               "d2h_bytes_per_step": int(d2h / args.steps), "scans": 1,
-               "api": "ptylab_gb300.Engines.mPIE(...).reconstruct(), NumPy in/out"}
+        e2e_single = {"value": NPOS * n1 / (time.perf_counter() - t0), "unit": UNIT, "steps": n1,
+                      "api": "ptylab_gb300.Engines.mPIE(...).reconstruct(), NumPy in/out"}
 
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -324,6 +348,7 @@ def run_gb300(args, rank, world, local_rank):
             "clocks": clk,
             "single_scan": single,
             "e2e": e2e,
+            "e2e_single_scan": e2e_single,
         }
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args.cpu_iters)

@@ -75,6 +75,8 @@ class BaseEngine(object):
             pass
         self.logger = logging.getLogger(self.engine_name)
         self._plan = None
+        self._owns_plan = True
+        self._scan = 0  # this engine's scan in the (possibly shared) launch plan
         self._dev = {}
 
     # --------------------------------------------------------- validation
@@ -171,13 +173,17 @@ class BaseEngine(object):
             rec.error = []
 
     def _prepareReconstruction(self):
+        self._prepare_host()
+        self._checkGPU()
+
+    def _prepare_host(self):
+        """BaseEngine._prepareReconstruction (BaseEngine.py:96-111) up to the device move."""
         self._check_supported()
         self._checkMISC()
         self._checkFFT()
         self._initialProbePowerCorrection()
         self._probeWindow()
         self._initializeErrors()
-        self._checkGPU()
 
     # --------------------------------------------------------- device state
     def _engine_code(self):
@@ -195,6 +201,11 @@ class BaseEngine(object):
 
     def _checkGPU(self):
         """Move the state to the GPU and build the launch plan (BaseEngine.py:613-635)."""
+        self._device_state()
+        self._plan_and_bind()
+
+    def _device_state(self):
+        """The reconstruction state, data, positions and order buffers on the GPU."""
         torch = _torch()
         if not getattr(self.params, "gpuSwitch", True):
             self.logger.warning("params.gpuSwitch is False; the GB300 engines always run on the GPU")
@@ -225,17 +236,31 @@ class BaseEngine(object):
         self._dev["flags"] = torch.zeros(nf, dtype=torch.uint8, device=device)
         self._order_host = torch.zeros(nf, dtype=torch.int32).pin_memory()
         self._flags_host = torch.zeros(nf, dtype=torch.uint8).pin_memory()
-        geom = _native.Geometry(
-            Np=Np, No=No, nosm=nosm, npsm=npsm, nslice=nslice, num_frames=nf, num_scans=1,
-            engine=self._engine_code(), propagator=_native.PROPAGATORS[p.propagatorType.lower()],
-            fftshift=int(bool(p.fftshiftSwitch)), fpm=int(d.operationMode == "FPM"),
-            cluster=int(getattr(self, "cluster", 0) or 0),
+
+    def _geometry(self, num_scans=1, throughput=0):
+        rec, d, p = self.reconstruction, self.experimentalData, self.params
+        return _native.Geometry(
+            Np=int(rec.Np), No=int(rec.No), nosm=int(rec.nosm), npsm=int(rec.npsm), nslice=int(rec.nslice),
+            num_frames=int(d.numFrames), num_scans=num_scans, engine=self._engine_code(),
+            propagator=_native.PROPAGATORS[p.propagatorType.lower()], fftshift=int(bool(p.fftshiftSwitch)),
+            fpm=int(d.operationMode == "FPM"), cluster=int(getattr(self, "cluster", 0) or 0), throughput=throughput,
         )
+
+    def _plan_and_bind(self, plan=None, scan=0, num_scans=1, throughput=0):
+        """Create the launch plan (or join `plan` as scan `scan`) and bind this
+        engine's buffers to it."""
+        lib = self._dev["lib"]
         self._release_plan()
-        plan = C.c_void_p()
-        _native.check(lib.ptyg_plan_create(C.byref(geom), C.byref(plan)), "ptyg_plan_create")
-        self._plan = plan
-        self._set_tables()
+        if plan is None:
+            plan = C.c_void_p()
+            _native.check(lib.ptyg_plan_create(C.byref(self._geometry(num_scans, throughput)), C.byref(plan)),
+                          "ptyg_plan_create")
+            self._owns_plan = True
+            self._plan, self._scan = plan, scan
+            self._set_tables()
+        else:
+            self._owns_plan = False
+            self._plan, self._scan = plan, scan
         self._set_projection()
         self._device_extras()
         self._bind()
@@ -284,7 +309,7 @@ class BaseEngine(object):
         if p.backgroundModeSwitch:
             bg = tab(rec.background)
             self._dev["background"] = bg
-            _native.check(lib.ptyg_plan_set_background(self._plan, 0, bg.data_ptr(), stream), "ptyg_plan_set_background")
+            _native.check(lib.ptyg_plan_set_background(self._plan, self._scan, bg.data_ptr(), stream), "ptyg_plan_set_background")
 
     def _slice_table(self):
         return None
@@ -308,12 +333,12 @@ class BaseEngine(object):
         self._buffers = self._scan_buffers()
         stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
         _native.check(
-            lib.ptyg_plan_bind_scan(self._plan, 0, C.byref(self._buffers), self._dev["data"].data_ptr(), stream),
+            lib.ptyg_plan_bind_scan(self._plan, self._scan, C.byref(self._buffers), self._dev["data"].data_ptr(), stream),
             "ptyg_plan_bind_scan",
         )
 
     def _release_plan(self):
-        if self._plan is not None and self._plan.value:
+        if self._plan is not None and self._plan.value and self._owns_plan:
             _native.load_library().ptyg_plan_destroy(self._plan)
         self._plan = None
 
@@ -355,6 +380,39 @@ class BaseEngine(object):
             "ptyg_plan_run",
         )
 
+    # ------------------------------------------------------ the iteration loop
+    # reconstruct() = prepare; _loop_begin; per iteration: _loop_order, one
+    # launch over every position, _loop_end; _finish.  reconstruct_batch()
+    # runs the same hooks for many engines sharing one launch.
+    def _pre_prepare(self):
+        """Engine set-up that PtyLab does before _prepareReconstruction."""
+
+    def _loop_begin(self):
+        """After the device move, before the first iteration."""
+
+    def _loop_order(self, loop):
+        self.setPositionOrder()
+        self._upload_order()
+
+    def _loop_end(self, loop):
+        self.getErrorMetrics()
+        self.applyConstraints(loop)
+        self.showReconstruction(loop)
+
+    def _finish(self):
+        self._move_data_to_cpu(detector_error=self.numIterations > 0)
+
+    def _run_loop(self):
+        self._pre_prepare()
+        self._prepareReconstruction()
+        self._loop_begin()
+        nf = self.experimentalData.numFrames
+        for loop in range(self.numIterations):
+            self._loop_order(loop)
+            self._run_positions(0, nf, record_detector_error=(loop == self.numIterations - 1))
+            self._loop_end(loop)
+        self._finish()
+
     # ------------------------------------------------------ host control
     def setPositionOrder(self):
         """BaseEngine.py:637-665 (same NumPy calls, same global RNG)."""
@@ -382,7 +440,7 @@ class BaseEngine(object):
         err = np.empty(nf, dtype=np.float64)
         stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
         _native.check(
-            self._dev["lib"].ptyg_plan_frame_errors(self._plan, 0, err.ctypes.data, stream), "ptyg_plan_frame_errors"
+            self._dev["lib"].ptyg_plan_frame_errors(self._plan, self._scan, err.ctypes.data, stream), "ptyg_plan_frame_errors"
         )
         energy = np.asarray(self.experimentalData.energyAtPos)
         if self.params.saveMemory:
@@ -474,7 +532,7 @@ class BaseEngine(object):
         out = torch.empty((int(d.numFrames), Np, Np), dtype=torch.float32, device=self._dev["device"])
         stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
         _native.check(
-            self._dev["lib"].ptyg_plan_detector_error(self._plan, 0, out.data_ptr(), stream), "ptyg_plan_detector_error"
+            self._dev["lib"].ptyg_plan_detector_error(self._plan, self._scan, out.data_ptr(), stream), "ptyg_plan_detector_error"
         )
         return out.cpu().numpy().astype(np.float64)
 
@@ -482,7 +540,7 @@ class BaseEngine(object):
         st = C.c_int(0)
         torch = _torch()
         stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
-        _native.check(self._dev["lib"].ptyg_plan_status(self._plan, 0, C.byref(st), stream), "ptyg_plan_status")
+        _native.check(self._dev["lib"].ptyg_plan_status(self._plan, self._scan, C.byref(st), stream), "ptyg_plan_status")
         if st.value != 0:
             raise RuntimeError(f"device status {st.value}: a scan position fell outside the object")
 
@@ -512,12 +570,12 @@ class BaseEngine(object):
         stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
         if p.backgroundModeSwitch:
             bg = self._dev["background"]
-            _native.check(lib.ptyg_plan_get_background(self._plan, 0, bg.data_ptr(), stream), "ptyg_plan_get_background")
+            _native.check(lib.ptyg_plan_get_background(self._plan, self._scan, bg.data_ptr(), stream), "ptyg_plan_get_background")
             rec.background = bg.cpu().numpy().astype(np.float64)
         if p.intensityConstraint == "fluctuation":
             nf = self.experimentalData.numFrames
             out = np.empty(nf, dtype=np.float64)
-            _native.check(lib.ptyg_plan_intensity_scaling(self._plan, 0, out.ctypes.data, stream),
+            _native.check(lib.ptyg_plan_intensity_scaling(self._plan, self._scan, out.ctypes.data, stream),
                           "ptyg_plan_intensity_scaling")
             p.intensityScaling[...] = out
 

@@ -1,0 +1,91 @@
+"""Many independent scans reconstructed side by side in one launch per iteration.
+
+PtyLab reconstructs one scan per engine; a GB300 runs the position loop of
+one scan on one thread-block cluster, so a single scan leaves most of the
+GPU idle.  ``reconstruct_batch(engines)`` takes engines built the usual way
+(``Engines.mPIE(reconstruction, experimentalData, params, monitor)`` ...),
+one per scan, and runs them together: one launch plan with a cluster per
+scan, one kernel launch per iteration for all of them.  Each engine keeps its
+own state, position order, momentum draws, error curve and constraints, and
+ends with its reconstruction back in NumPy exactly as ``reconstruct()``
+leaves it.
+
+The engines must be of one class and share the launch geometry (Np, No, mode
+counts, slices, frames, propagator, fftshift, operation mode), the update
+scalars, the propagator tables and the projection switches.  The global
+NumPy RNG is consumed engine by engine within each iteration (order shuffle,
+then mPIE's momentum draws), so a batched scan sees different draws than the
+same engine run alone unless its order is deterministic.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+def _same(a, b):
+    if isinstance(a, np.ndarray) or isinstance(b, np.ndarray):
+        return np.array_equal(np.asarray(a), np.asarray(b))
+    return a == b
+
+
+def _check_compatible(engines):
+    e0 = engines[0]
+    if any(type(e) is not type(e0) for e in engines):
+        raise ValueError("reconstruct_batch: all engines must be of one class")
+    if len({id(e.reconstruction) for e in engines}) != len(engines):
+        raise ValueError("reconstruct_batch: every engine needs its own reconstruction")
+    geo = [f for f, _ in e0._geometry()._fields_ if f not in ("num_scans", "throughput")]
+    g0 = e0._geometry()
+    upd = [f for f, _ in e0._update_params()._fields_]
+    u0 = e0._update_params()
+    r0, p0 = e0.reconstruction, e0.params
+    for e in engines[1:]:
+        g = e._geometry()
+        bad = [f for f in geo if getattr(g, f) != getattr(g0, f)]
+        if bad:
+            raise ValueError(f"reconstruct_batch: launch geometry differs ({', '.join(bad)})")
+        u = e._update_params()
+        bad = [f for f in upd if getattr(u, f) != getattr(u0, f)]
+        if bad:
+            raise ValueError(f"reconstruct_batch: update parameters differ ({', '.join(bad)})")
+        for name in ("zo", "wavelength", "dxp"):
+            if p0.propagatorType.lower() != "fraunhofer" and not _same(getattr(e.reconstruction, name),
+                                                                       getattr(r0, name)):
+                raise ValueError(f"reconstruct_batch: reconstruction.{name} differs (propagator tables)")
+        for name in ("intensityConstraint", "adaptiveDenoisingSwitch", "backgroundModeSwitch", "FourierMaskSwitch"):
+            if getattr(e.params, name) != getattr(p0, name):
+                raise ValueError(f"reconstruct_batch: params.{name} differs")
+        if e.numIterations != e0.numIterations:
+            raise ValueError("reconstruct_batch: numIterations differs")
+
+
+def reconstruct_batch(engines):
+    """Run ``engine.reconstruct()`` for every engine, all scans in one launch per iteration."""
+    engines = list(engines)
+    if not engines:
+        return
+    for e in engines:
+        e._pre_prepare()
+    _check_compatible(engines)
+    for e in engines:
+        e._prepare_host()
+    for e in engines:
+        e._device_state()
+    e0 = engines[0]
+    e0._plan_and_bind(num_scans=len(engines), throughput=1)
+    for i, e in enumerate(engines[1:], 1):
+        e._plan_and_bind(plan=e0._plan, scan=i)
+    for e in engines:
+        e._loop_begin()
+    nf = e0.experimentalData.numFrames
+    n = e0.numIterations
+    for loop in range(n):
+        for e in engines:
+            e._loop_order(loop)
+        e0._run_positions(0, nf, record_detector_error=(loop == n - 1))  # every bound scan
+        for e in engines:
+            e._loop_end(loop)
+    for e in engines[1:]:
+        e._finish()
+    e0._finish()  # the plan's owner last: it destroys the plan

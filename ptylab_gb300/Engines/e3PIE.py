@@ -43,15 +43,9 @@ class e3PIE(BaseEngine):
     def reconstruct(self):
         """e3PIE.py:71-330: one kernel launch per iteration walks every position
         through the slices, the detector projection and back."""
-        self._prepareReconstruction()
-        nf = self.experimentalData.numFrames
-        for loop in range(self.numIterations):
-            self.setPositionOrder()
-            self._upload_order()
-            self._run_positions(0, nf, record_detector_error=(loop == self.numIterations - 1))
-            self.getErrorMetrics()
-            self.applyConstraints(loop)
-            self.showReconstruction(loop)
-        self._move_data_to_cpu(detector_error=self.numIterations > 0)
+        self._run_loop()
+
+    def _finish(self):
+        super()._finish()
         # product of all object slices (e3PIE.py:316)
         self.reconstruction.objectProd = np.prod(self.reconstruction.object, 3)

@@ -23,15 +23,7 @@ class ePIE(BaseEngine):
         if experimentalData is not None:
             self.reconstruction.data = experimentalData
             self.experimentalData = experimentalData
-        self._prepareReconstruction()
-        nf = self.experimentalData.numFrames
-        for loop in range(self.numIterations):
-            self.setPositionOrder()
-            self._upload_order()
-            self._run_positions(0, nf, record_detector_error=(loop == self.numIterations - 1))
-            self.getErrorMetrics()
-            self.applyConstraints(loop)
-        self._move_data_to_cpu(detector_error=self.numIterations > 0)
+        self._run_loop()
 
     def reconstruct_stepwise(self, experimentalData=None):
         """Generator variant (ePIE.py:53-126): yields ``(iteration, positionLoop)``

@@ -61,20 +61,22 @@ class mPIE(BaseEngine):
     def reconstruct(self, experimentalData=None, reconstruction=None, vis_after_each_iteration=None):
         self.changeExperimentalData(experimentalData)
         self.changeOptimizable(reconstruction)
-        rec = self.reconstruction
+        self._vis = vis_after_each_iteration
+        self._run_loop()
+
+    def _loop_begin(self):
         # buffers follow the object/probe as they stand after preparation (mPIE.py:103-105)
-        self._prepareReconstruction()
+        rec = self.reconstruction
         rec.objectBuffer.copy_(rec.object)
         rec.probeBuffer.copy_(rec.probe)
-        nf = self.experimentalData.numFrames
-        for loop in range(self.numIterations):
-            self.setPositionOrder()
-            draws = np.random.rand(nf)
-            self._upload_order(momentum=draws > 0.95)
-            self._run_positions(0, nf, record_detector_error=(loop == self.numIterations - 1))
-            self.getErrorMetrics()
-            self.applyConstraints(loop)
-            self.showReconstruction(loop)
-            if callable(vis_after_each_iteration):
-                vis_after_each_iteration(loop, rec)
-        self._move_data_to_cpu(detector_error=self.numIterations > 0)
+
+    def _loop_order(self, loop):
+        self.setPositionOrder()
+        draws = np.random.rand(self.experimentalData.numFrames)
+        self._upload_order(momentum=draws > 0.95)
+
+    def _loop_end(self, loop):
+        super()._loop_end(loop)
+        vis = getattr(self, "_vis", None)
+        if callable(vis):
+            vis(loop, self.reconstruction)

@@ -119,6 +119,9 @@ class mqNewton(BaseEngine):
         if experimentalData is not None:
             self.reconstruction.data = experimentalData
             self.experimentalData = experimentalData
+        self._run_loop()
+
+    def _pre_prepare(self):
         self.initializeAdaptiveMomentum()
         rec = self.reconstruction
         if not np.array_equal(_host_copy(rec.objectBuffer), _host_copy(rec.object)):
@@ -127,21 +130,18 @@ class mqNewton(BaseEngine):
                 "changed after the engine was built; build the engine again)"
             )
         self._loop = 0
-        self._prepareReconstruction()
-        nf = self.experimentalData.numFrames
-        for loop in range(self.numIterations):
-            self._loop = loop
-            self.setPositionOrder()
-            self._upload_order()
-            self._run_positions(0, nf, record_detector_error=(loop == self.numIterations - 1))
-            self.getErrorMetrics()
-            self.applyConstraints(loop)
-            self.showReconstruction(loop)
+
+    def _loop_order(self, loop):
+        self._loop = loop
+        super()._loop_order(loop)
+
+    def _finish(self):
+        rec = self.reconstruction
         # the buffers equal the object and probe after the last step
         # (mqNewton.py:203, 224); the kernel keeps only the probe buffer
         rec.objectBuffer.copy_(rec.object)
         vO, vP = (float(x) for x in self._dev["moment2"].cpu())
-        self._move_data_to_cpu(detector_error=self.numIterations > 0)
+        super()._finish()
         if self.momentum_method in ("ADAM", "NADAM"):
             rec.objectMomentum_v = np.full(rec.objectMomentum.shape, np.complex64(vO))
             rec.probeMomentum_v = np.full(rec.probeMomentum.shape, np.complex64(vP))

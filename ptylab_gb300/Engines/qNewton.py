@@ -24,13 +24,4 @@ class qNewton(BaseEngine):
         if experimentalData is not None:
             self.reconstruction.data = experimentalData
             self.experimentalData = experimentalData
-        self._prepareReconstruction()
-        nf = self.experimentalData.numFrames
-        for loop in range(self.numIterations):
-            self.setPositionOrder()
-            self._upload_order()
-            self._run_positions(0, nf, record_detector_error=(loop == self.numIterations - 1))
-            self.getErrorMetrics()
-            self.applyConstraints(loop)
-            self.showReconstruction(loop)
-        self._move_data_to_cpu(detector_error=self.numIterations > 0)
+        self._run_loop()

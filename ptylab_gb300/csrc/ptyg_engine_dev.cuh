@@ -50,6 +50,29 @@ PTYG_DEV double warp_sum(double v) {
   return v;
 }
 
+// Sum over the warp as the balanced binary tree over lane order (pairs of
+// neighbouring lanes first); every lane receives the same bits.
+PTYG_DEV double warp_tree_sum(double v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of v[0, n), n a power of two of at most 128, as the balanced binary tree
+// over index order, on every lane.  The tree is fixed by n alone, so n values
+// split across CTAs in power-of-two blocks and summed block by block, then
+// over the blocks in the same tree, round exactly as one sum over all values.
+PTYG_DEV double tree_sum(const double* v, int n, unsigned lane) {
+  double s;
+  if (n <= 32)
+    s = (int)lane < n ? v[lane] : 0.0;  // the zero leaves add exactly
+  else if (n == 64)
+    s = v[2 * lane] + v[2 * lane + 1];
+  else
+    s = (v[4 * lane] + v[4 * lane + 1]) + (v[4 * lane + 2] + v[4 * lane + 3]);
+  return warp_tree_sum(s);
+}
+
 // Max-reduce NV values over the CTA and fold them into the cluster slots (rank
 // 0's shared memory) with one cluster-scope atomicMax per value per CTA
 // (non-negative floats order like their bits).

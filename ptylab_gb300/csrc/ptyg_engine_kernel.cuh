@@ -661,10 +661,17 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
 
     // ---------------- C: object and probe steps, pixel by pixel
     float omaxPatch = 0.f;  // qNewton: max over the new patch of sum_o |O_o|
-    // mqNewton partial sums: |objectBuffer - object|^2, and with
+    // mqNewton sums over the patch: |objectBuffer - object|^2, and with
     // d = probeBuffer - probe and the probe numerator U: |d|^2, Re(conj(d) U),
-    // |U|^2, from which |probeBuffer - (probe + U/Omax)|^2 follows once Omax is known
-    float gsqO = 0.f, pdd = 0.f, pdu = 0.f, puu = 0.f;
+    // |U|^2, from which |probeBuffer - (probe + U/Omax)|^2 follows once Omax is
+    // known.  A pixel's terms are exact double products summed over the modes;
+    // a warp sums its 32-pixel row segment in a fixed tree, and the segments
+    // (in sm.tile, free in this pass) are summed in the balanced tree over
+    // segment order, per CTA here and over the cluster in pass M: the same
+    // tree for every CTA shape, so a batched launch gives a single-scan
+    // launch's bits.
+    const int nseg = LN / 32;
+    double* segSum = reinterpret_cast<double*>(sm.tile);  // [4][nseg]
     {
       const float pmax2 = slot_value(red, RED_PMAX2);
       const float omax2 = slot_value(red, RED_OMAX2);
@@ -674,6 +681,7 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
       for (int i = threadIdx.x; i < LN; i += blockDim.x) {
         float2 O[MAX_OBJECT_MODES], accO[MAX_OBJECT_MODES];
         float gP[MAX_OBJECT_MODES];
+        double tgO = 0.0, tdd = 0.0, tdu = 0.0, tuu = 0.0;
 #pragma unroll
         for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
           if (o < nosm) {
@@ -715,9 +723,9 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
             sm.probe[p * pst + i] = cadd(P, cscale(accP, stepP));
           if (mq) {
             const float2 d = csub(s.probeBuffer[(size_t)p * NP * NP + (size_t)line0 * NP + i], P);
-            pdd += d.x * d.x + d.y * d.y;
-            pdu += d.x * accP.x + d.y * accP.y;
-            puu += accP.x * accP.x + accP.y * accP.y;
+            tdd += (double)d.x * d.x + (double)d.y * d.y;
+            tdu += (double)d.x * accP.x + (double)d.y * accP.y;
+            tuu += (double)accP.x * accP.x + (double)accP.y * accP.y;
           }
         }
         const int l = i / NP, x = i - (i / NP) * NP;
@@ -735,9 +743,17 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
               // it is the patch as it was before this step; kept for pass M
               const float2 g = csub(O[o], On);
               sm.obj[o * LN + i] = g;
-              gsqO += g.x * g.x + g.y * g.y;
+              tgO += (double)g.x * g.x + (double)g.y * g.y;
             }
           }
+        }
+        if (mq) {
+          // warp-uniform: LN and blockDim are multiples of 32
+          tgO = warp_tree_sum(tgO);
+          tdd = warp_tree_sum(tdd);
+          tdu = warp_tree_sum(tdu);
+          tuu = warp_tree_sum(tuu);
+          if (lane < 4) segSum[lane * nseg + (i >> 5)] = lane == 0 ? tgO : lane == 1 ? tdd : lane == 2 ? tdu : tuu;
         }
         if (qn) {
           omaxPatch = fmaxf(omaxPatch, onew);
@@ -758,13 +774,10 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
         block_max_to_slots<1>(m, sm.redF, red, idx);
       }
       if (mq) {
-        double v[4] = {gsqO, pdd, pdu, puu};
         __syncthreads();
-        block_sum_n<4>(v, sm.redD);
-        if (threadIdx.x == 0) {
-          double* dst = dsmem(sm.part, 0);
-#pragma unroll
-          for (int k = 0; k < 4; ++k) dst[k * C + crank] = v[k];
+        if (warp < 4) {
+          const double v = tree_sum(segSum + warp * nseg, nseg, lane);
+          if (lane == 0) dsmem(sm.part, 0)[warp * C + crank] = v;
         }
       }
     }
@@ -785,8 +798,8 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
         double t0, t1;
         {
           // lanes [0,2C) read [|gO|^2 | |d|^2] and then [Re conj(d)U | |U|^2]
-          // partials; the xor butterfly sums each group of C lanes in the same
-          // order in every warp and CTA
+          // partials; the xor butterfly from offset 1 up sums each group of C
+          // lanes in the balanced tree over CTA order, in every warp and CTA
           const double* src = dsmem(sm.part, 0);
           t0 = (int)lane < 2 * C ? src[lane] : 0.0;
           t1 = (int)lane < 2 * C ? src[2 * C + lane] : 0.0;

@@ -166,6 +166,41 @@ def test_position_outside_object_raises(torch_cuda):
         Engines.ePIE(rec, d, p, DummyMonitor()).reconstruct()
 
 
+@pytest.mark.parametrize("engine", ["ePIE", "qNewton", "mqNewton"])
+def test_reconstruct_batch_equals_single_engines(torch_cuda, engine):
+    """Engines.reconstruct_batch (one launch per iteration for all scans)
+    gives every scan what its own reconstruct() gives (sequential order: no
+    RNG between the engines).  The batch runs the many-scan kernel shape
+    (fewer, wider CTAs per scan); every sum that feeds the updates is formed
+    in a tree fixed by the patch size, so object, probe and detector error
+    are bit-identical, and only the error metric (per-CTA partials summed on
+    the host) can differ in its last bits."""
+    from ptylab_gb300 import DummyMonitor, Engines
+    from ptylab_gb300.simulate import ScanSpec, cpm_problem
+
+    def engines():
+        out = []
+        for g in range(3):
+            d, p, rec, _, _ = cpm_problem(ScanSpec(Np=64, No=192, num_positions=30, seed=300 + g), engine_seed=g)
+            e = getattr(Engines, engine)(rec, d, p, DummyMonitor())
+            e.numIterations = 3
+            out.append(e)
+        return out
+
+    single = engines()
+    for e in single:
+        e.reconstruct()
+    batch = engines()
+    Engines.reconstruct_batch(batch)
+    for a, b in zip(single, batch):
+        ra, rb = a.reconstruction, b.reconstruction
+        assert isinstance(rb.object, np.ndarray) and rb.object.dtype == np.complex64
+        np.testing.assert_array_equal(rb.object, ra.object)
+        np.testing.assert_array_equal(rb.probe, ra.probe)
+        np.testing.assert_array_equal(rb.detectorError, ra.detectorError)
+        assert rel_err(np.asarray(rb.error), np.asarray(ra.error)) < 1e-9
+
+
 def test_batched_scans_equal_single_runs(torch_cuda):
     """G independent scans in one launch (one cluster each) reproduce G single-scan launches bitwise."""
     torch = torch_cuda

@@ -148,3 +148,28 @@ def test_mqnewton_host_logic():
     eng.momentum_method = "Adagrad"
     with pytest.raises(AttributeError):
         eng.initializeAdaptiveMomentum()
+
+
+def test_reconstruct_batch_rejects_mismatched_engines():
+    """Engines that cannot share one launch are refused before any device work."""
+    from ptylab_gb300 import DummyMonitor, Engines
+
+    def make(name, **over):
+        fx = load_fixture(name)
+        m, i, d, p, rec = containers(fx)
+        rec.object, rec.probe = i["init_object"].copy(), i["init_probe"].copy()
+        rec.initialGuessObject, rec.initialGuessProbe = rec.object.copy(), rec.probe.copy()
+        eng = Engines.ePIE(rec, d, p, DummyMonitor())
+        for k, v in over.items():
+            setattr(eng, k, v)
+        return eng
+
+    with pytest.raises(ValueError, match="update parameters"):
+        Engines.reconstruct_batch([make("scan_epie_random"), make("scan_epie_random", betaObject=0.5)])
+    with pytest.raises(ValueError, match="geometry"):
+        Engines.reconstruct_batch([make("scan_epie_random"), make("reg_epie_fraunhofer")])
+    with pytest.raises(ValueError, match="one class"):
+        fx = load_fixture("scan_epie_random")
+        m, i, d, p, rec = containers(fx)
+        rec.object, rec.probe = i["init_object"].copy(), i["init_probe"].copy()
+        Engines.reconstruct_batch([make("scan_epie_random"), Engines.qNewton(rec, d, p, DummyMonitor())])
