@@ -50,7 +50,17 @@ enum ptyg_engine { PTYG_EPIE = 0, PTYG_MPIE = 1, PTYG_QNEWTON = 2, PTYG_E3PIE = 
 enum ptyg_momentum { PTYG_MOMENTUM = 0, PTYG_ADAM = 1, PTYG_NADAM = 2 };
 /* params.intensityConstraint (PtyLab/Engines/BaseEngine.py:913-961) */
 enum ptyg_intensity_constraint { PTYG_STANDARD = 0, PTYG_POISSION = 1, PTYG_EXPONENTIAL = 2, PTYG_FLUCTUATION = 3 };
-enum ptyg_propagator { PTYG_FRAUNHOFER = 0, PTYG_FRESNEL = 1, PTYG_ASP = 2 };
+enum ptyg_propagator {
+  PTYG_FRAUNHOFER = 0,
+  PTYG_FRESNEL = 1,
+  PTYG_ASP = 2,
+  /* ptyg_propagate_sets only: */
+  PTYG_POLYCHROME_ASP = 3,
+  PTYG_SCALED_ASP = 4,
+  PTYG_SCALED_POLYCHROME_ASP = 5,
+  PTYG_TWO_STEP_POLYCHROME = 6,
+  PTYG_IDENTITY = 7
+};
 enum ptyg_direction { PTYG_FORWARD = 0, PTYG_INVERSE = 1 };
 
 /* Library version (PTYG_VERSION of the build). */
@@ -95,6 +105,27 @@ PTYG_API int ptyg_propagate(int propagator, int direction, int fftshift, int Np,
  * `scratch`. */
 PTYG_API int ptyg_propagate_noalloc(int propagator, int direction, int fftshift, int Np, int batch, const void* in,
                                     void* out, const void* table, void* stream);
+
+/* The scaled and multi-wavelength propagators (centred transforms only; the
+ * reference rejects fftshiftSwitch for all of them) on `batch` fields of
+ * Np x Np.  `nsets` table sets (one per wavelength); the fields are
+ * wavelength-major, so field f uses set f / (batch / nsets) and batch must be
+ * a multiple of nsets.  Each table is nsets consecutive Np x Np complex64
+ * arrays in natural (centred-grid) order, except where noted.
+ *   POLYCHROME_ASP         ifft2c(fft2c(x)*A) (conj A inverse)      Operators.py:458-505, 536-558
+ *                          A: the angular-spectrum transfer function per wavelength
+ *   SCALED_ASP,            ifft2c(fft2c(x*A)*B);                    Operators.py:313-375
+ *   SCALED_POLYCHROME_ASP  inverse ifft2c(fft2c(x)*conj B)*conj A   Operators.py:378-455
+ *                          A = Q1, B = Q2 (SCALED_ASP: nsets = 1)
+ *   TWO_STEP_POLYCHROME    fft2c(ifft2c(fft2c(x)*A)*B);             Operators.py:233-282
+ *                          inverse ifft2c(fft2c(x*conj B)*conj A)
+ *                          A: transfer function over zo*(1 - l0/l) per wavelength l,
+ *                          B: ONE Np x Np Fresnel chirp of the first wavelength
+ *   IDENTITY               out = in                                 Operators.py:508-533
+ * `scratch`: batch*Np*Np complex64, or NULL to let the call allocate it.
+ * in == out is allowed.  Np must be 32, 64, 128 or 256. */
+PTYG_API int ptyg_propagate_sets(int propagator, int direction, int Np, int batch, int nsets, const void* in,
+                                 void* out, const void* table_a, const void* table_b, void* scratch, void* stream);
 
 /* ------------------------------------------------------------------------
  * Engine plans: the drop-in for the position loop of ePIE.reconstruct_stepwise

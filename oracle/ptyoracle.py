@@ -82,6 +82,57 @@ def aspw_transfer_function(z, wavelength, N, L, bandlimit=True):
     return H * W
 
 
+def scaled_asp_tables(z, wavelength, N, dx, dq):
+    """Q1 (source-plane chirp) and Q2 (Fourier-plane chirp) of the scaled
+    angular spectrum with its band limits (PtyLab/Operators/Operators.py:706-760,
+    bandlimit=True), rounded to complex64 as the propagator stores them
+    (Operators.py:954-988).  The expressions keep the reference's operation
+    order so the float64 values, and hence their complex64 rounding, agree."""
+    k = 2 * np.pi / wavelength
+    x1 = np.arange(-N // 2, N // 2) * dx
+    X1, Y1 = np.meshgrid(x1, x1)
+    r1sq = X1**2 + Y1**2
+    f = np.arange(-N // 2, N // 2) / (N * dx)
+    FX, FY = np.meshgrid(f, f)
+    fsq = FX**2 + FY**2
+    m = dq / dx
+    Q1 = np.exp(1.0j * k / 2 * (1 - m) / z * r1sq)
+    Q2 = np.exp(-1.0j * np.pi**2 * 2 * z / m / k * fsq)
+    if m != 1:
+        r1sq_max = wavelength * z / (2 * dx * (1 - m))
+        Q1 = Q1 * np.array(circ(X1, Y1, 2 * r1sq_max))
+    fsq_max = m / (2 * z * wavelength * (1 / (N * dx)))
+    Q2 = Q2 * np.array(circ(FX, FY, 2 * fsq_max))
+    return Q1.astype(np.complex64), Q2.astype(np.complex64)
+
+
+def _per_wavelength(tables):
+    """Stack per-wavelength Np x Np tables as (nlambda, 1, 1, 1, Np, Np): they
+    broadcast over modes and slices as the reference's (nlambda, nosm, npsm,
+    1, Np, Np) copies do."""
+    return np.stack(tables)[:, None, None, None]
+
+
+def polychrome_asp_tf(g):
+    """(Operators.py:909-951): one centred transfer function per wavelength of
+    spectralDensity, complex128 on the CPU path (no dtype given there)."""
+    return _per_wavelength([aspw_transfer_function(g.zo, lam, g.Np, g.Lp) for lam in g.spectralDensity])
+
+
+def scaled_polychrome_asp_tables(g):
+    """(Operators.py:990-1030): scaledASP's Q1, Q2 per wavelength, complex64."""
+    q = [scaled_asp_tables(g.zo, lam, g.Np, g.dxo, g.dxd) for lam in g.spectralDensity]
+    return _per_wavelength([a for a, _ in q]), _per_wavelength([b for _, b in q])
+
+
+def two_step_polychrome_tables(g):
+    """(Operators.py:1033-1077): transfer functions over zo*(1 - l0/l) at each
+    wavelength l (complex128) and the Fresnel chirp of the first wavelength."""
+    sd = g.spectralDensity
+    tf = _per_wavelength([aspw_transfer_function(g.zo * (1 - sd[0] / lam), lam, g.Np, g.Lp) for lam in sd])
+    return tf, quad_phase(g.zo, sd[0], g.Np, g.dxp)
+
+
 def asp_transfer_function(nosm, npsm, Np, zo, wavelength, Lp):
     """ASP detector transfer function as the engines use it: complex64, shape
     (1, nosm, npsm, 1, Np, Np) (PtyLab/Operators/Operators.py:861-893)."""
@@ -102,10 +153,16 @@ class Geometry:
     nslice: int = 1
     dz: float = 0.0
     refrIndex: float = 1.0
+    dxd: float = 0.0
+    spectralDensity: tuple = ()
 
     @property
     def Lp(self):
         return self.Np * self.dxp
+
+    @property
+    def dxo(self):
+        return self.dxp
 
     @property
     def xp(self):
@@ -132,6 +189,21 @@ def object2detector(fields, propagator, fftshift, g: Geometry):
             raise ValueError("ASP propagator only works with fftshiftswitch == False")
         tf = np.fft.ifftshift(asp_transfer_function(g.nosm, g.npsm, g.Np, g.zo, g.wavelength, g.Lp), axes=(-2, -1))
         return ifft2c(fft2c(fields, True) * tf, True)
+    if p in ("polychromeasp", "scaledasp", "scaledpolychromeasp", "twosteppolychrome") and fftshift:
+        raise ValueError(f"{propagator} propagatorType works only with fftshiftSwitch = False")
+    if p == "polychromeasp":  # Operators.py:458-505
+        return ifft2c(fft2c(fields) * polychrome_asp_tf(g))
+    if p == "scaledasp":  # Operators.py:313-350
+        Q1, Q2 = scaled_asp_tables(g.zo, g.wavelength, g.Np, g.dxo, g.dxd)
+        return ifft2c(fft2c(fields * Q1) * Q2)
+    if p == "scaledpolychromeasp":  # Operators.py:378-423
+        Q1, Q2 = scaled_polychrome_asp_tables(g)
+        return ifft2c(fft2c(fields * Q1) * Q2)
+    if p == "twosteppolychrome":  # Operators.py:233-282
+        tf, qp = two_step_polychrome_tables(g)
+        return fft2c(ifft2c(fft2c(fields) * tf) * qp)
+    if p == "identity":  # Operators.py:508-533: multiplication by complex128 ones
+        return fields * (quad_phase(1e-3, 532e-9, g.Np, g.dxp) * 0 + 1)
     raise NotImplementedError(propagator)
 
 
@@ -147,6 +219,21 @@ def detector2object(fields, propagator, fftshift, g: Geometry):
             raise ValueError("ASP propagator only works with fftshiftswitch == False")
         tf = np.fft.ifftshift(asp_transfer_function(g.nosm, g.npsm, g.Np, g.zo, g.wavelength, g.Lp), axes=(-2, -1))
         return ifft2c(fft2c(fields, True) * tf.conj(), True)
+    if p in ("polychromeasp", "scaledasp", "scaledpolychromeasp", "twosteppolychrome") and fftshift:
+        raise ValueError(f"{propagator} propagatorType works only with fftshiftSwitch = False")
+    if p == "polychromeasp":  # Operators.py:536-558
+        return ifft2c(fft2c(fields) * polychrome_asp_tf(g).conj())
+    if p == "scaledasp":  # Operators.py:346-375
+        Q1, Q2 = scaled_asp_tables(g.zo, g.wavelength, g.Np, g.dxo, g.dxd)
+        return ifft2c(fft2c(fields) * Q2.conj()) * Q1.conj()
+    if p == "scaledpolychromeasp":  # Operators.py:419-455
+        Q1, Q2 = scaled_polychrome_asp_tables(g)
+        return ifft2c(fft2c(fields) * Q2.conj()) * Q1.conj()
+    if p == "twosteppolychrome":  # Operators.py:270-275 (the field part of the pair returned at :285-310)
+        tf, qp = two_step_polychrome_tables(g)
+        return ifft2c(fft2c(fields * qp.conj()) * tf.conj())
+    if p == "identity":
+        return fields * (quad_phase(1e-3, 532e-9, g.Np, g.dxp) * 0 + 1)
     raise NotImplementedError(propagator)
 
 

@@ -28,6 +28,8 @@ ENGINES = {"ePIE": 0, "mPIE": 1, "qNewton": 2, "e3PIE": 3, "mqNewton": 4}
 MOMENTUM_METHODS = {"momentum": 0, "ADAM": 1, "NADAM": 2}
 INTENSITY_CONSTRAINTS = {"standard": 0, "poission": 1, "exponential": 2, "fluctuation": 3}
 PROPAGATORS = {"fraunhofer": 0, "fresnel": 1, "asp": 2}
+# ptyg_propagate_sets (include/ptyg.h enum ptyg_propagator)
+SET_PROPAGATORS = {"polychromeasp": 3, "scaledasp": 4, "scaledpolychromeasp": 5, "twosteppolychrome": 6, "identity": 7}
 
 _EXC = {
     PTYG_ERR_INVALID: ValueError,
@@ -126,6 +128,10 @@ _SIGNATURES = {
     ],
     "ptyg_propagate_noalloc": [
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+    ],
+    "ptyg_propagate_sets": [
+        C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
     ],
     "ptyg_plan_create": [C.POINTER(Geometry), C.POINTER(C.c_void_p)],
     "ptyg_plan_destroy": [C.c_void_p],

@@ -194,6 +194,118 @@ extern "C" int ptyg_propagate(int propagator, int direction, int fftshift, int N
   return PTYG_OK;
 }
 
+// With N = Np, F / I the unnormalised forward / inverse DFT and M the
+// checkerboard (-1)^(y+x): fft2c(x) = M F(M x) / N and ifft2c(X) = M I(M X) / N,
+// and M T M = T for any elementwise table T, so
+//   ifft2c(fft2c(x) * T) = M I(T F(M x)) / N^2:
+// a row pass (sign, forward), a column pass (forward, * T / N^2, inverse)
+// and a row pass (inverse, sign), the tables applied on the way in or out.
+extern "C" int ptyg_propagate_sets(int propagator, int direction, int Np, int batch, int nsets, const void* in,
+                                   void* out, const void* table_a, const void* table_b, void* scratch,
+                                   void* stream) {
+  if (!valid_np(Np)) return fail(PTYG_ERR_UNSUPPORTED, "Np=%d: supported sizes are 32, 64, 128, 256", Np);
+  if (batch < 0) return fail(PTYG_ERR_INVALID, "batch=%d", batch);
+  if (nsets < 1 || batch % nsets != 0)
+    return fail(PTYG_ERR_INVALID, "nsets=%d must be >= 1 and divide batch=%d", nsets, batch);
+  if (direction != PTYG_FORWARD && direction != PTYG_INVERSE) return fail(PTYG_ERR_INVALID, "direction=%d", direction);
+  if (propagator < PTYG_POLYCHROME_ASP || propagator > PTYG_IDENTITY)
+    return fail(PTYG_ERR_UNSUPPORTED, "propagator %d is not a ptyg_propagate_sets propagator", propagator);
+  if (propagator == PTYG_SCALED_ASP && nsets != 1) return fail(PTYG_ERR_INVALID, "SCALED_ASP takes one table set");
+  const bool needA = propagator != PTYG_IDENTITY;
+  const bool needB = propagator == PTYG_SCALED_ASP || propagator == PTYG_SCALED_POLYCHROME_ASP ||
+                     propagator == PTYG_TWO_STEP_POLYCHROME;
+  if ((needA && !table_a) || (needB && !table_b)) return fail(PTYG_ERR_INVALID, "propagator %d needs its tables", propagator);
+  if (batch == 0) return PTYG_OK;
+  if (!in || !out) return fail(PTYG_ERR_INVALID, "null field pointer");
+  int dev;
+  int r = ready_device(&dev);
+  if (r) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = (size_t)batch * Np * Np * sizeof(float2);
+  if (propagator == PTYG_IDENTITY) {
+    if (in != out) PTYG_CUDA(cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, st), "identity copy");
+    return PTYG_OK;
+  }
+  const float2* tw = twiddles(dev, Np);
+  float2* tmp = (float2*)scratch;
+  bool own = false;
+  if (!tmp) {
+    PTYG_CUDA(cudaMallocAsync((void**)&tmp, bytes, st), "propagate scratch");
+    own = true;
+  }
+  const bool inv = direction == PTYG_INVERSE;
+  const int div = batch / nsets;  // fields per table set
+  const float2* A = (const float2*)table_a;
+  const float2* B = (const float2*)table_b;
+  const float n2 = 1.f / (float)(Np * Np);
+
+  ptyg::RowOp r1 = {};  // sign, forward
+  r1.preSign = 1;
+  r1.scale = 1.f;
+  ptyg::ColOp co = {};  // forward, * T / N^2, inverse
+  co.filterScale = n2;
+  co.inverse2 = 1;
+  co.scale = 1.f;
+  co.filterDiv = div;
+  co.conjFilter = inv;
+  ptyg::RowOp r2 = {};  // inverse, sign
+  r2.inverse = 1;
+  r2.postSign = 1;
+  r2.scale = 1.f;
+  bool secondFft = false;
+  switch (propagator) {
+    case PTYG_POLYCHROME_ASP:
+      co.filter = A;
+      break;
+    case PTYG_SCALED_ASP:
+    case PTYG_SCALED_POLYCHROME_ASP:
+      co.filter = B;
+      if (!inv) {
+        r1.pre = A;
+        r1.preDiv = div;
+      } else {
+        r2.post = A;
+        r2.postDiv = div;
+        r2.conjPost = 1;
+      }
+      break;
+    case PTYG_TWO_STEP_POLYCHROME:
+      co.filter = A;
+      if (!inv) {
+        // fft2c(ifft2c(fft2c(x) A) B) = M F(B I(A F(M x))) / N^3: no sign
+        // between the halves (M M = 1), the chirp B after the inverse
+        r2.postSign = 0;
+        r2.post = B;
+        secondFft = true;
+      } else {
+        r1.pre = B;
+        r1.conjPre = 1;
+      }
+      break;
+  }
+  cudaError_t e = ptyg::prop_rows(Np, (const float2*)in, tmp, batch, r1, tw, st);
+  if (e == cudaSuccess) e = ptyg::prop_cols(Np, tmp, tmp, batch, co, tw, st);
+  if (!secondFft) {
+    if (e == cudaSuccess) e = ptyg::prop_rows(Np, tmp, (float2*)out, batch, r2, tw, st);
+  } else {
+    ptyg::RowOp r3 = {};  // forward rows
+    r3.scale = 1.f;
+    ptyg::ColOp c2 = {};  // forward columns, sign, 1/N
+    c2.postSign = 1;
+    c2.scale = 1.f / (float)Np;
+    // row passes never run in place (their pointers are __restrict__)
+    if (e == cudaSuccess) e = ptyg::prop_rows(Np, tmp, (float2*)out, batch, r2, tw, st);
+    if (e == cudaSuccess) e = ptyg::prop_rows(Np, (const float2*)out, tmp, batch, r3, tw, st);
+    if (e == cudaSuccess) e = ptyg::prop_cols(Np, tmp, (float2*)out, batch, c2, tw, st);
+  }
+  if (own) {
+    cudaError_t e2 = cudaFreeAsync(tmp, st);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "ptyg_propagate_sets");
+  return PTYG_OK;
+}
+
 // ------------------------------------------------------------------ plans
 struct ScanOwned {
   float* data = nullptr;      // converted ptychogram

@@ -55,14 +55,17 @@ __global__ void prop_row_kernel(const float2* __restrict__ in, float2* __restric
   const long long line = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
   if (line >= (long long)batch * NP) return;
   const int y = (int)(line % NP);
+  const long long field = line / NP;
   const float2* src = in + line * NP;
+  const float2* pre = op.pre ? op.pre + (op.preDiv > 0 ? (size_t)(field / op.preDiv) * NP * NP : 0) : nullptr;
+  const float2* post = op.post ? op.post + (op.postDiv > 0 ? (size_t)(field / op.postDiv) * NP * NP : 0) : nullptr;
   float2 v[E];
   const float sg = (op.preSign && ((y + lane) & 1)) ? -1.f : 1.f;
 #pragma unroll
   for (int j = 0; j < E; ++j) {
     float2 x = src[lane + 32 * j];
-    if (op.pre) {
-      float2 q = op.pre[y * NP + lane + 32 * j];
+    if (pre) {
+      float2 q = pre[y * NP + lane + 32 * j];
       if (op.conjPre) q.y = -q.y;
       x = cmul(x, q);
     }
@@ -75,8 +78,8 @@ __global__ void prop_row_kernel(const float2* __restrict__ in, float2* __restric
     const int x = lane + 32 * j;
     float2 u = cscale(v[j], op.scale);
     if (op.postSign && ((y + x) & 1)) u = cscale(u, -1.f);
-    if (op.post) {
-      float2 q = op.post[y * NP + x];
+    if (post) {
+      float2 q = post[y * NP + x];
       if (op.conjPost) q.y = -q.y;
       u = cmul(u, q);
     }
@@ -101,6 +104,9 @@ __global__ void prop_col_kernel(const float2* in, float2* out, int batch, ColOp 
   const int field = blockIdx.x / nblk;
   const int c0 = (blockIdx.x % nblk) * CB;
   if (field >= batch) return;
+  const float2* filter =
+      op.filter ? op.filter + (op.filterDiv > 0 ? (size_t)(field / op.filterDiv) * NP * NP : 0) : nullptr;
+  const float2* post = op.post ? op.post + (op.postDiv > 0 ? (size_t)(field / op.postDiv) * NP * NP : 0) : nullptr;
   for (int i = threadIdx.x; i < NP; i += blockDim.x) tw[i] = twiddle[i];
   const float2* src = in + (size_t)field * NP * NP;
   for (int i = threadIdx.x; i < NP * CB; i += blockDim.x) {
@@ -118,10 +124,10 @@ __global__ void prop_col_kernel(const float2* in, float2* out, int batch, ColOp 
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = tile[(lane + 32 * j) * LD + c];
     line_fft<E>(v, op.inverse1 != 0, F, wbuf + warp * NP, lane);
-    if (op.filter) {
+    if (filter) {
 #pragma unroll
       for (int j = 0; j < E; ++j) {
-        float2 h = op.filter[(size_t)(lane + 32 * j) * NP + x];
+        float2 h = filter[(size_t)(lane + 32 * j) * NP + x];
         if (op.conjFilter) h.y = -h.y;
         v[j] = cmul(v[j], cscale(h, op.filterScale));
       }
@@ -132,8 +138,8 @@ __global__ void prop_col_kernel(const float2* in, float2* out, int batch, ColOp 
       const int y = lane + 32 * j;
       float2 u = cscale(v[j], op.scale);
       if (op.postSign && ((y + x) & 1)) u = cscale(u, -1.f);
-      if (op.post) {
-        float2 q = op.post[(size_t)y * NP + x];
+      if (post) {
+        float2 q = post[(size_t)y * NP + x];
         if (op.conjPost) q.y = -q.y;
         u = cmul(u, q);
       }

@@ -10,6 +10,9 @@ namespace ptyg {
 // Row pass of a standalone propagation: per row, x * pre (or conj) * [sign]
 // -> 1D transform -> * scale * [sign] * post (or conj).  The 2D centring
 // modulation is one pre-sign in the first pass and one post-sign in the last.
+// Tables (pre, post, filter) are Np x Np complex64 in natural order; with
+// setDiv > 0 a table holds consecutive sets of Np x Np and field f reads set
+// f / setDiv (one set per wavelength), else every field reads the one table.
 struct RowOp {
   int inverse;
   int preSign;   // multiply the input by (-1)^(y+x)
@@ -19,6 +22,7 @@ struct RowOp {
   const float2* post;
   int conjPost;
   float scale;
+  int preDiv, postDiv;
 };
 
 // Column pass: transform (inverse1), optionally * filter*filterScale (or conj)
@@ -33,6 +37,7 @@ struct ColOp {
   const float2* post;
   int conjPost;
   float scale;
+  int filterDiv, postDiv;
 };
 
 cudaError_t prop_rows(int Np, const float2* in, float2* out, int batch, const RowOp& op, const float2* tw,

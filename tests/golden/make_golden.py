@@ -14,8 +14,9 @@ What it writes, all under ``tests/golden/``:
   relative Frobenius error is exactly 0, so these fixtures are the reference's
   goldens reproduced, with the inputs stored beside them.
 * ``prop_<name>.npz`` -- forward/back propagation of the seeded initial probe
-  for the in-scope propagators (``tests/regression/test_propagator_regression.py:58-82``),
-  likewise checked against ``propagator_<name>.npz``.
+  for all eight propagators, three wavelengths for the polychrome ones
+  (``tests/regression/test_propagator_regression.py:27-82``), likewise checked
+  against ``propagator_<name>.npz``.
 * ``scan_<name>.npz`` -- cases the regression dataset cannot exercise (its 16
   frames all round to one pixel position): a Fermat-spiral CPM scan with
   random position order, mPIE momentum, mqNewton (ADAM, NADAM, plain
@@ -290,13 +291,26 @@ def run_case(ref, d, case):
     return inputs, outputs
 
 
+# tests/regression/test_propagator_regression.py:27-36: wavelengths per propagator
+PROPAGATORS = {
+    "fraunhofer": 1, "fresnel": 1, "asp": 1, "scaledasp": 1, "identity": 1,
+    "polychromeasp": 3, "scaledpolychromeasp": 3, "twosteppolychrome": 3,
+}
+
+
 def run_propagator(ref, d, prop):
+    """tests/regression/test_propagator_regression.py:39-82."""
+    nlambda = PROPAGATORS[prop]
     data = _experimental_data(ref, d)
     params = ref["Params"]()
     params.gpuSwitch = False
     params.propagatorType = prop
     params.fftshiftSwitch = False
     rec = ref["Reconstruction"](data, params)
+    rec.nlambda = nlambda
+    if nlambda > 1:
+        base = float(np.atleast_1d(rec.wavelength)[0])
+        rec.spectralDensity = base * np.linspace(0.98, 1.02, nlambda)
     np.random.seed(SEED)
     rec.initializeObjectProbe()
     Operators = ref["Operators"]
@@ -312,6 +326,9 @@ def run_propagator(ref, d, prop):
         wavelength=np.float64(rec.wavelength),
         zo=np.float64(rec.zo),
         Lp=np.float64(rec.Lp),
+        dxd=np.float64(rec.dxd),
+        spectralDensity=np.atleast_1d(np.asarray(rec.spectralDensity, dtype=np.float64)),
+        nlambda=np.int64(nlambda),
     )
     outputs = dict(
         forward=np.asarray(fwd),
@@ -456,14 +473,16 @@ def main():
         save(out / f"reg_{name}.npz", _meta(case, d), inputs, outputs)
         print(f"reg_{name}: matches {gold.name}/{name}.npz exactly")
 
-    for prop in ("fraunhofer", "fresnel", "asp"):
+    for prop in PROPAGATORS:
         if not wanted(f"prop_{prop}"):
             continue
         inputs, outputs = run_propagator(ref, d, prop)
         g = np.load(gold / f"propagator_{prop}.npz")
         for key in g.files:
             e = rel(outputs[key], g[key])
-            if e != 0.0:
+            # the fields must be bit-identical; the stored norms may differ in
+            # the last bit (np.linalg.norm's BLAS sums in its own order)
+            if e > (2.3e-16 if key == "error" else 0.0):
                 raise SystemExit(f"propagator {prop}: {key} differs by {e:.3e}")
         save(out / f"prop_{prop}.npz", dict(propagator=prop), inputs, outputs)
         print(f"prop_{prop}: matches propagator_{prop}.npz exactly")

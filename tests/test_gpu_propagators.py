@@ -25,8 +25,10 @@ def torch_cuda():
     return torch
 
 
-def _rec(Np, dxp, wavelength, zo):
-    return SimpleNamespace(Np=Np, dxp=dxp, wavelength=wavelength, zo=zo, nlambda=1, esw=None)
+def _rec(Np, dxp, wavelength, zo, dxd=None, spectralDensity=None, nlambda=1, nosm=1, npsm=1):
+    sd = np.atleast_1d(wavelength if spectralDensity is None else spectralDensity)
+    return SimpleNamespace(Np=Np, dxp=dxp, wavelength=wavelength, zo=zo, nlambda=nlambda, nosm=nosm, npsm=npsm,
+                           dxd=dxp if dxd is None else dxd, spectralDensity=sd, esw=None, ESW=None)
 
 
 @pytest.mark.parametrize("name", fixture_names("prop_"))
@@ -37,10 +39,12 @@ def test_propagator_fixtures(torch_cuda, name):
     p = Params()
     p.propagatorType = str(fx["meta_propagator"])
     p.fftshiftSwitch = False
-    rec = _rec(int(fx["in_Np"]), float(fx["in_dxp"]), float(fx["in_wavelength"]), float(fx["in_zo"]))
+    rec = _rec(int(fx["in_Np"]), float(fx["in_dxp"]), float(fx["in_wavelength"]), float(fx["in_zo"]),
+               dxd=float(fx["in_dxd"]), spectralDensity=fx["in_spectralDensity"], nlambda=int(fx["in_nlambda"]))
     _, fwd = Operators.object2detector(fx["in_field"], p, rec)
     assert isinstance(fwd, np.ndarray) and fwd.shape == fx["out_forward"].shape
     assert rel_err(fwd, fx["out_forward"]) < TOL
+    rec.ESW = fx["out_forward"]  # twoStepPolychrome's inverse also propagates reconstruction.ESW
     _, back = Operators.detector2object(fx["out_forward"], p, rec)
     assert rel_err(back, fx["out_back"]) < TOL
     # device follows the data: a CUDA tensor comes back as a CUDA tensor
@@ -70,6 +74,40 @@ def test_propagators_match_oracle(torch_cuda, Np, prop, fftshift):
     assert rel_err(fwd, O.object2detector(x.astype(np.complex128), prop, fftshift, g)) < TOL
     _, back = Operators.detector2object(x, p, rec)
     assert rel_err(back, O.detector2object(x.astype(np.complex128), prop, fftshift, g)) < TOL
+
+
+@pytest.mark.parametrize("Np", [32, 64, 128, 256])
+@pytest.mark.parametrize("prop", ["polychromeASP", "scaledASP", "scaledPolychromeASP", "twoStepPolychrome", "identity"])
+def test_wavelength_set_propagators_match_oracle(torch_cuda, Np, prop):
+    """Three wavelengths (one for scaledASP), two object modes, three probe
+    modes: the (nlambda, 1, npsm, 1, Np, Np) probe-shaped input is broadcast
+    against the (nlambda, nosm, npsm, 1, Np, Np) tables as PtyLab broadcasts
+    it, and each wavelength block reads its own tables."""
+    from ptylab_gb300 import Operators, Params
+
+    nl = 1 if prop == "scaledASP" else 3
+    rng = np.random.default_rng(Np + nl)
+    shape = (nl, 1, 3, 1, Np, Np)
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    dxp, dxd, lam, zo = 4e-6, 6e-6, 632.8e-9, 2e-3
+    sd = lam * np.linspace(0.98, 1.02, nl)
+    p = Params()
+    p.propagatorType = prop
+    rec = _rec(Np, dxp, lam, zo, dxd=dxd, spectralDensity=sd, nlambda=nl, nosm=2, npsm=3)
+    g = O.Geometry(Np=Np, No=Np, dxp=dxp, wavelength=lam, zo=zo, dxd=dxd, nlambda=nl, nosm=2, npsm=3,
+                   spectralDensity=tuple(sd))
+    want_shape = shape if prop == "identity" else (nl, 2, 3, 1, Np, Np)
+    xb = np.broadcast_to(x, want_shape).astype(np.complex128)
+    _, fwd = Operators.object2detector(x, p, rec)
+    assert fwd.shape == want_shape
+    assert rel_err(fwd, O.object2detector(xb, prop, False, g)) < TOL
+    rec.ESW = fwd
+    _, back = Operators.detector2object(fwd, p, rec)
+    assert rel_err(back, O.detector2object(fwd.astype(np.complex128), prop, False, g)) < TOL
+    if prop != "identity":
+        p.fftshiftSwitch = True
+        with pytest.raises(ValueError):
+            Operators.object2detector(x, p, rec)
 
 
 def test_fraunhofer_round_trip_is_identity(torch_cuda):
