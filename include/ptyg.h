@@ -151,6 +151,13 @@ typedef struct ptyg_geometry {
   int32_t throughput;  /* 0: shortest time per position (8 rows per CTA);
                           1: most positions per second over many scans (16
                           rows per CTA: fewer CTAs per scan, more scans at once) */
+  int32_t nlambda;     /* wavelengths (reconstruction.nlambda; 0 reads as 1).  Above
+                          1: ePIE only, object (nlambda, nosm, ...) and probe
+                          (nlambda, npsm, ...) wavelength-major, exit waves
+                          O_(l,o) P_(l,p) of each wavelength l, the ASP table
+                          one per wavelength (polychromeASP, Operators.py:458-505),
+                          and the object and probe steps summed over the
+                          wavelengths (ePIE.py:128-160) */
 } ptyg_geometry;
 
 /* Engine scalars (ePIE.py:35-42, mPIE.py:233-245, qNewton.py:43-52,
@@ -207,7 +214,8 @@ PTYG_API int ptyg_plan_destroy(ptyg_plan* plan);
 /* Host complex64 tables, Np*Np each, centred (DC at Np/2), built in double
  * and rounded as PtyLab builds them; NULL where the configuration needs none:
  *   fresnel_q  __make_quad_phase      (Operators/_propagation_kernels.py:16-36)
- *   asp_h      __aspw_transfer_function at zo (Operators.py:631-684, 861-893)
+ *   asp_h      __aspw_transfer_function at zo (Operators.py:631-684, 861-893);
+ *              nlambda consecutive tables, one per wavelength (Operators.py:909-951)
  *   slice_h    aspw at dz, wavelength/refrIndex (e3PIE.py:62-69) */
 PTYG_API int ptyg_plan_set_tables(ptyg_plan* plan, const void* fresnel_q, const void* asp_h, const void* slice_h);
 

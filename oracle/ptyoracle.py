@@ -746,6 +746,8 @@ def run_fixture(fx, iters=None, dtype=None):
         npsm=nps,
         nslice=nsl,
         dz=float(i.get("dz", 0.0)),
+        dxd=float(m.get("dxd", 0.0)),
+        spectralDensity=tuple(np.atleast_1d(i["spectralDensity"])) if "spectralDensity" in i else (float(i["wavelength"]),),
     )
     s = Settings(
         momentum_method=str(m.get("momentum_method", "ADAM")),

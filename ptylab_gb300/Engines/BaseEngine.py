@@ -102,10 +102,18 @@ class BaseEngine(object):
                 raise NotImplementedError(f"params.{name} is not supported by the GB300 engines")
         if getattr(p, "comStabilizationSwitch", None) not in (None, False):
             raise NotImplementedError("params.comStabilizationSwitch is not supported by the GB300 engines")
-        if getattr(rec, "nlambda", 1) != 1:
-            raise NotImplementedError("nlambda > 1 (polychromatic propagators) is not on this path")
-        if p.propagatorType.lower() not in ("fraunhofer", "fresnel", "asp"):
+        nl = int(getattr(rec, "nlambda", 1))
+        if nl != 1 and self.engine_name != "ePIE":
+            raise NotImplementedError(f"nlambda = {nl}: several wavelengths run with the GB300 ePIE only")
+        if nl != 1 and getattr(p, "orthogonalizationSwitch", False):
+            raise NotImplementedError("orthogonalizationSwitch with several wavelengths is not on this path")
+        kind = p.propagatorType.lower()
+        if kind not in ("fraunhofer", "fresnel", "asp", "polychromeasp"):
             raise NotImplementedError(f"propagatorType {p.propagatorType!r} is not on this path")
+        if kind == "asp" and nl > 1:  # Operators.py:866-869
+            raise ValueError("For multi-wavelength, polychromeASP needs to be used instead of ASP")
+        if kind == "polychromeasp" and np.atleast_1d(rec.spectralDensity).size < nl:
+            raise ValueError(f"reconstruction.spectralDensity holds fewer than nlambda = {nl} wavelengths")
 
     def _checkMISC(self):
         """BaseEngine.py:376-403."""
@@ -113,7 +121,7 @@ class BaseEngine(object):
             raise ValueError(
                 "probePowerCorrectionSwitch and modulusEnforcedProbeSwitch can not simultaneously be switched on!"
             )
-        if self.params.propagatorType == "ASP" and self.params.fftshiftSwitch:
+        if self.params.propagatorType.lower() in ("asp", "polychromeasp") and self.params.fftshiftSwitch:
             raise ValueError("ASP propagatorType works only with fftshiftSwitch = False")
         rec = self.reconstruction
         if self.params.backgroundModeSwitch:  # BaseEngine.py:361-364
@@ -219,10 +227,11 @@ class BaseEngine(object):
             setattr(rec, name, self._to_device(getattr(rec, name), torch.complex64))
         Np, No = int(rec.Np), int(rec.No)
         nosm, npsm, nslice = int(rec.nosm), int(rec.npsm), int(rec.nslice)
-        if tuple(rec.object.shape) != (1, nosm, 1, nslice, No, No):
-            raise ValueError(f"object shape {tuple(rec.object.shape)} != {(1, nosm, 1, nslice, No, No)}")
-        if tuple(rec.probe.shape) != (1, 1, npsm, nslice, Np, Np):
-            raise ValueError(f"probe shape {tuple(rec.probe.shape)} != {(1, 1, npsm, nslice, Np, Np)}")
+        nl = int(getattr(rec, "nlambda", 1))
+        if tuple(rec.object.shape) != (nl, nosm, 1, nslice, No, No):
+            raise ValueError(f"object shape {tuple(rec.object.shape)} != {(nl, nosm, 1, nslice, No, No)}")
+        if tuple(rec.probe.shape) != (nl, 1, npsm, nslice, Np, Np):
+            raise ValueError(f"probe shape {tuple(rec.probe.shape)} != {(nl, 1, npsm, nslice, Np, Np)}")
         nf = int(d.numFrames)
         positions = np.asarray(rec.positions).astype(np.int64)
         if positions.shape != (nf, 2):
@@ -244,6 +253,7 @@ class BaseEngine(object):
             num_frames=int(d.numFrames), num_scans=num_scans, engine=self._engine_code(),
             propagator=_native.PROPAGATORS[p.propagatorType.lower()], fftshift=int(bool(p.fftshiftSwitch)),
             fpm=int(d.operationMode == "FPM"), cluster=int(getattr(self, "cluster", 0) or 0), throughput=throughput,
+            nlambda=int(getattr(rec, "nlambda", 1)),
         )
 
     def _plan_and_bind(self, plan=None, scan=0, num_scans=1, throughput=0):
@@ -278,6 +288,10 @@ class BaseEngine(object):
             )
         elif kind == "asp":
             h = np.ascontiguousarray(_tables.asp_detector_tf(float(rec.zo), float(rec.wavelength), Np, Np * float(rec.dxp)))
+        elif kind == "polychromeasp":
+            # one transfer function per wavelength of spectralDensity (Operators.py:909-951)
+            wl = tuple(float(w) for w in np.atleast_1d(rec.spectralDensity)[: int(rec.nlambda)])
+            h = np.ascontiguousarray(_tables.polychrome_asp_tf(float(rec.zo), wl, Np, Np * float(rec.dxp)))
         sh = self._slice_table()
         self._tables_keepalive = (q, h, sh)
         ptr = lambda a: a.ctypes.data if a is not None else None  # noqa: E731

@@ -49,6 +49,10 @@ def _check_compatible(engines):
         bad = [f for f in upd if getattr(u, f) != getattr(u0, f)]
         if bad:
             raise ValueError(f"reconstruct_batch: update parameters differ ({', '.join(bad)})")
+        if p0.propagatorType.lower() == "polychromeasp" and not _same(
+            np.atleast_1d(e.reconstruction.spectralDensity), np.atleast_1d(r0.spectralDensity)
+        ):
+            raise ValueError("reconstruct_batch: reconstruction.spectralDensity differs (propagator tables)")
         for name in ("zo", "wavelength", "dxp"):
             if p0.propagatorType.lower() != "fraunhofer" and not _same(getattr(e.reconstruction, name),
                                                                        getattr(r0, name)):

@@ -27,7 +27,8 @@ PTYG_ERR_DEVICE = -6
 ENGINES = {"ePIE": 0, "mPIE": 1, "qNewton": 2, "e3PIE": 3, "mqNewton": 4}
 MOMENTUM_METHODS = {"momentum": 0, "ADAM": 1, "NADAM": 2}
 INTENSITY_CONSTRAINTS = {"standard": 0, "poission": 1, "exponential": 2, "fluctuation": 3}
-PROPAGATORS = {"fraunhofer": 0, "fresnel": 1, "asp": 2}
+# the engines' propagators: polychromeASP is the ASP kernel with one table per wavelength
+PROPAGATORS = {"fraunhofer": 0, "fresnel": 1, "asp": 2, "polychromeasp": 2}
 # ptyg_propagate_sets (include/ptyg.h enum ptyg_propagator)
 SET_PROPAGATORS = {"polychromeasp": 3, "scaledasp": 4, "scaledpolychromeasp": 5, "twosteppolychrome": 6, "identity": 7}
 
@@ -56,6 +57,7 @@ class Geometry(C.Structure):
         ("fpm", C.c_int32),
         ("cluster", C.c_int32),
         ("throughput", C.c_int32),
+        ("nlambda", C.c_int32),
     ]
 
 

@@ -369,7 +369,7 @@ static void plan_free(ptyg_plan* p) {
 // One warp per 1D-transform task of a pass (K modes x L lines), 4..16 warps
 // (mqNewton: 8, the bound its kernel is compiled for).
 static int engine_threads(const ptyg_geometry& g, int C) {
-  const int tasks = g.nosm * g.npsm * (g.Np / C);
+  const int tasks = g.nlambda * g.nosm * g.npsm * (g.Np / C);
   const int wmax = g.engine == PTYG_MQNEWTON ? 8 : 16;
   const int w = tasks < 4 ? 4 : (tasks > wmax ? wmax : tasks);
   return 32 * w;
@@ -392,7 +392,11 @@ static std::vector<int> cluster_candidates(const ptyg_geometry& g) {
 extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan) {
   if (!geometry || !plan) return fail(PTYG_ERR_INVALID, "null argument");
   *plan = nullptr;
-  const ptyg_geometry& g = *geometry;
+  ptyg_geometry g = *geometry;
+  if (g.nlambda == 0) g.nlambda = 1;
+  if (g.nlambda < 1) return fail(PTYG_ERR_INVALID, "nlambda=%d", g.nlambda);
+  if (g.nlambda > 1 && g.engine != PTYG_EPIE)
+    return fail(PTYG_ERR_UNSUPPORTED, "nlambda=%d: several wavelengths run with the ePIE engine only", g.nlambda);
   if (!valid_np(g.Np)) return fail(PTYG_ERR_UNSUPPORTED, "Np=%d: supported sizes are 32, 64, 128, 256", g.Np);
   if (g.No < g.Np) return fail(PTYG_ERR_INVALID, "No=%d smaller than Np=%d", g.No, g.Np);
   if (g.nosm < 1 || g.npsm < 1 || g.nslice < 1 || g.num_frames < 1 || g.num_scans < 1)
@@ -408,8 +412,9 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   } else if (g.nslice != 1) {
     return fail(PTYG_ERR_UNSUPPORTED, "nslice=%d needs the e3PIE engine", g.nslice);
   }
-  if (!ptyg::engine_modes_supported(g.Np, g.nosm, g.npsm))
-    return fail(PTYG_ERR_UNSUPPORTED, "nosm=%d npsm=%d at Np=%d is not instantiated", g.nosm, g.npsm, g.Np);
+  if (!ptyg::engine_modes_supported(g.Np, g.nlambda * g.nosm, g.nlambda * g.npsm))
+    return fail(PTYG_ERR_UNSUPPORTED, "nlambda=%d nosm=%d npsm=%d at Np=%d is not instantiated", g.nlambda, g.nosm,
+                g.npsm, g.Np);
   int dev;
   int r = ready_device(&dev);
   if (r) return r;
@@ -430,11 +435,11 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
       const bool e3 = g.engine == PTYG_E3PIE;
       if (e3 && psm) continue;  // e3PIE keeps its probe slices in global memory
       p->smem = e3 ? ptyg::e3pie_smem_bytes(g.Np, c, g.npsm)
-                   : ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.engine, psm);
+                   : ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.nlambda, g.engine, psm);
       if ((int)p->smem > maxSmem) continue;
       int nclusters = 0;
       cudaError_t e = e3 ? ptyg::e3pie_max_clusters(g.Np, c, p->threads, p->smem, &nclusters)
-                         : ptyg::engine_max_clusters(g.Np, g.engine, c, p->threads, p->smem, &nclusters);
+                         : ptyg::engine_max_clusters(g.Np, g.engine, g.nlambda, c, p->threads, p->smem, &nclusters);
       if (e != cudaSuccess) {
         cudaGetLastError();
         continue;
@@ -452,7 +457,7 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
                 g.Np, g.nosm, g.npsm, p->smem, maxSmem);
   }
   const size_t np2 = (size_t)g.Np * g.Np;
-  const int K = g.nosm * g.npsm;
+  const int K = g.nlambda * g.nosm * g.npsm;
   p->scans.resize(g.num_scans);
   p->hScans.resize(g.num_scans);
   for (int s = 0; s < g.num_scans; ++s) {
@@ -523,8 +528,14 @@ extern "C" int ptyg_plan_set_tables(ptyg_plan* p, const void* fresnel_q, const v
   int r;
   if (fresnel_q && (r = upload(&p->fresnelQ, fresnel_q, n))) return r;
   if (asp_h) {
-    auto t = to_fourier_layout_host((const float2*)asp_h, Np);
-    if ((r = upload(&p->aspH, t.data(), n))) return r;
+    const int sets = p->g.nlambda;  // one table per wavelength
+    std::vector<float2> all;
+    all.reserve(sets * n);
+    for (int w = 0; w < sets; ++w) {
+      auto t = to_fourier_layout_host((const float2*)asp_h + w * n, Np);
+      all.insert(all.end(), t.begin(), t.end());
+    }
+    if ((r = upload(&p->aspH, all.data(), sets * n))) return r;
   }
   if (slice_h) {
     auto t = to_fourier_layout_host((const float2*)slice_h, Np);
@@ -625,6 +636,7 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
   a.No = g.No;
   a.nosm = g.nosm;
   a.npsm = g.npsm;
+  a.nlambda = g.nlambda;
   a.nslice = g.nslice;
   a.numFrames = g.num_frames;
   a.engine = g.engine;
@@ -701,7 +713,7 @@ extern "C" int ptyg_plan_info(ptyg_plan* p, int* cluster, int* threads, int* sme
   if (smem_bytes) *smem_bytes = (int)p->smem;
   if (max_active_clusters) {
     int n = 0;
-    cudaError_t e = ptyg::engine_max_clusters(p->g.Np, p->g.engine, p->C, p->threads, p->smem, &n);
+    cudaError_t e = ptyg::engine_max_clusters(p->g.Np, p->g.engine, p->g.nlambda, p->C, p->threads, p->smem, &n);
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveClusters");
     *max_active_clusters = n;
   }

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
 
     // ---------------- forward through the slices
     for (int sl = 1; sl < S; ++sl) {
-      column_filter<E, L>(tile, rows, F, a.sliceH, false, crank, K);
+      column_filter<E, L>(tile, rows, F, a.sliceH, false, crank, K, K);
       cluster_sync(C);
       // P_s rows (natural order) into the row buffer and the probe's slice sl
       fft_tasks<E, true>(
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           },
           [&](int t, float2(&v)[E]) { scatter_column<E, L>(rows, v, t / L, sx0 + t % L); });
     } else {
-      column_filter<E, L>(tile, rows, F, a.aspH, false, crank, K);
+      column_filter<E, L>(tile, rows, F, a.aspH, false, crank, K, K);
       cluster_sync(C);
       fft_tasks<E, true>(
           F, K * L,
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           },
           [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
       cluster_sync(C);
-      column_filter<E, L>(tile, rows, F, a.aspH, true, crank, K);
+      column_filter<E, L>(tile, rows, F, a.aspH, true, crank, K, K);
     }
     {
       const double t = block_sum(err, redD);
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
             },
             [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
         cluster_sync(C);
-        column_filter<E, L>(tile, rows, F, a.sliceH, true, crank, K);
+        column_filter<E, L>(tile, rows, F, a.sliceH, true, crank, K, K);
         cluster_sync(C);
       }
     }

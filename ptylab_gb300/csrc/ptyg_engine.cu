@@ -1,15 +1,17 @@
 // Instantiations of the position-loop kernel (ptyg_engine_kernel.cuh) for
-// ePIE / mPIE / qNewton, and the engine-independent launch queries.
+// ePIE / mPIE / qNewton at one wavelength, and the engine-independent launch
+// queries.
 #include "ptyg_engine_kernel.cuh"
 #include "ptyg_ops.cuh"
 
 namespace ptyg {
 
-size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine, bool probe_in_smem) {
+size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int nlambda, int engine, bool probe_in_smem) {
   const int L = Np / C;
   const size_t LN = (size_t)L * Np;
   const bool qn = engine == ENG_QNEWTON || engine == ENG_MQNEWTON;
-  const size_t n = smem_complex_elems(Np, L, nosm * npsm, nosm, npsm, qn, probe_in_smem);
+  const size_t n =
+      smem_complex_elems(Np, L, nlambda * nosm * npsm, nlambda * nosm, nlambda * npsm, qn, probe_in_smem);
   // + fr, dat (3 LN floats), slots, redD (4 x 32 doubles), redF (4 x 32
   // floats), part (4 x 16 doubles), alignment slack
   return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 4 * 32 * sizeof(double) +
@@ -25,14 +27,16 @@ bool engine_shape_supported(int Np, int cluster) {
   return false;
 }
 
-cudaError_t engine_max_clusters(int Np, int engine, int cluster, int threads, size_t smem, int* out) {
+cudaError_t engine_max_clusters(int Np, int engine, int nlambda, int cluster, int threads, size_t smem, int* out) {
   if (engine == ENG_MQNEWTON) return engine_max_clusters_mq(Np, cluster, threads, smem, out);
-  return engine_max_clusters_t<false>(Np, cluster, threads, smem, out);
+  if (nlambda > 1) return engine_max_clusters_poly(Np, cluster, threads, smem, out);
+  return engine_max_clusters_t<VAR_STD>(Np, cluster, threads, smem, out);
 }
 
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
   if (a.engine == ENG_MQNEWTON) return launch_engine_mq(a, nscans, threads, smem, st);
-  return launch_engine_t<false>(a, nscans, threads, smem, st);
+  if (a.nlambda > 1) return launch_engine_poly(a, nscans, threads, smem, st);
+  return launch_engine_t<VAR_STD>(a, nscans, threads, smem, st);
 }
 
 bool engine_modes_supported(int Np, int nosm, int npsm) {

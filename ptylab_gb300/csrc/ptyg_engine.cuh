@@ -60,9 +60,13 @@ struct EngineArgs {
   const ScanDev* scans;
   const float2* twiddle;   // W_Np^m, m = 0..Np-1
   const float2* fresnelQ;  // Fresnel chirp, natural [y][x]
-  const float2* aspH;      // ASP detector TF (ifftshifted), Fourier layout [sx][sy]
+  const float2* aspH;      // ASP detector TF (ifftshifted), Fourier layout [sx][sy]; one per wavelength
   const float2* sliceH;    // e3PIE slice TF (ifftshifted), Fourier layout [sx][sy]
   int Np, No, nosm, npsm, nslice, numFrames;
+  // wavelengths (ePIE only when > 1): object modes (l, o) and probe modes
+  // (l, p) lie wavelength-major in memory, the exit waves are the nlambda x
+  // nosm x npsm products O_(l,o) P_(l,p)
+  int nlambda;
   int engine, prop, centred, fpm;
   int start, count;
   int writeDetErr;

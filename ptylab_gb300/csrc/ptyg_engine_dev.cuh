@@ -186,9 +186,9 @@ PTYG_DEV void scatter_column(float2* rows, const float2 (&v)[E], int k, int sx) 
 // Column pass that multiplies the spectrum by H (or conj H) / Np^2 between a
 // forward and an inverse column transform (ASP, Operators.py:155-230); the
 // result goes to the row owners' row buffers.
-template <int E, int L>
+template <int E, int L, bool SETS = false>
 PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, const float2* H, bool conjH, int crank,
-                            int K) {
+                            int K, int kPerSet) {
   constexpr int NP = 32 * E;
   constexpr int ld = L + 1;
   const int lane = threadIdx.x & 31;
@@ -203,7 +203,8 @@ PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, con
       },
       [&](int t, float2(&v)[E]) {
         const int k = t / L, c = t % L;
-        const float2* h = H + (size_t)(sx0 + c) * NP;
+        // SETS: one table per wavelength, modes k of wavelength k / kPerSet
+        const float2* h = H + (SETS ? (size_t)(k / kPerSet) * NP * NP : 0) + (size_t)(sx0 + c) * NP;
 #pragma unroll
         for (int r = 0; r < E; ++r) {
           float2 hv = __ldg(h + r * 32 + lane);

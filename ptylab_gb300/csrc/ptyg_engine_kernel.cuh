@@ -317,9 +317,12 @@ __host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int n
 // ------------------------------------------------------------------ kernel
 // E: Np / 32 points per lane; L: rows (and Fourier columns) per CTA, so the
 // cluster has C = Np / L CTAs.  Both compile-time so index arithmetic is shifts.
-// MQ: the mqNewton instantiation (engine == ENG_MQNEWTON), else ePIE / mPIE / qNewton.
-template <int E, int L, bool MQ>
-__global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineArgs a) {
+// VAR: VAR_MQ is the mqNewton instantiation (engine == ENG_MQNEWTON), VAR_POLY
+// ePIE over several wavelengths, VAR_STD ePIE / mPIE / qNewton at one.
+enum { VAR_STD = 0, VAR_MQ = 1, VAR_POLY = 2 };
+template <int E, int L, int VAR>
+__global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(const EngineArgs a) {
+  constexpr bool MQ = VAR == VAR_MQ;
   // (512 threads x 128 registers: one CTA of 16 warps, or two of 8 warps, per
   // SM; mqNewton: at most 256 threads, so its momentum pass keeps all of a
   // tile's loads in registers)
@@ -331,7 +334,12 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
   const int line0 = crank * L, sx0 = crank * L;
   const unsigned lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int nosm = a.nosm, npsm = a.npsm, K = nosm * npsm, No = a.No;
+  // object and probe modes of every wavelength (wavelength-major); an exit
+  // wave k = (l * nosmW + o) * npsmW + p pairs object mode l * nosmW + o with
+  // probe mode l * npsmW + p of the same wavelength l
+  const int nl = VAR == VAR_POLY ? a.nlambda : 1;  // a compile-time 1 outside VAR_POLY
+  const int nosmW = a.nosm, npsmW = a.npsm;
+  const int nosm = nl * nosmW, npsm = nl * npsmW, K = nl * nosmW * npsmW, No = a.No;
   const bool centred = a.centred != 0;
   const bool fresnel = a.prop == PROP_FRESNEL;
   const bool asp = a.prop == PROP_ASP;
@@ -456,7 +464,7 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
         F, K * L,
         [&](int t, float2(&v)[E]) {
           const int k = t / L, l = t % L;
-          const int o = k / npsm, p = k - (k / npsm) * npsm;
+          const int o = k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
           const int y = line0 + l;
           const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
 #pragma unroll
@@ -589,7 +597,7 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
           [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm.rows, v, t / L, sx0 + t % L); });
     } else {
       // ---------------- ASP: x H, real-space projection, x conj(H)
-      column_filter<E, L>(sm.tile, sm.rows, F, a.aspH, false, crank, K);
+      column_filter<E, L, VAR == VAR_POLY>(sm.tile, sm.rows, F, a.aspH, false, crank, K, nosmW * npsmW);
       cluster_sync(C);
       fft_tasks<E, true>(
           F, K * L,
@@ -624,7 +632,7 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
           },
           [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm.tile, v, t / L, line0 + t % L); });
       cluster_sync(C);
-      column_filter<E, L>(sm.tile, sm.rows, F, a.aspH, true, crank, K);
+      column_filter<E, L, VAR == VAR_POLY>(sm.tile, sm.rows, F, a.aspH, true, crank, K, nosmW * npsmW);
     }
     {
       __syncthreads();  // sm.redD may still be read by the projection's cluster sums
@@ -644,7 +652,7 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
         },
         [&](int t, float2(&v)[E]) {
           const int k = t / L, l = t % L;
-          const int o = k / npsm, p = k - (k / npsm) * npsm;
+          const int o = k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
           const int y = line0 + l;
           const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
           float2* row = sm.rows + t * NP;
@@ -696,7 +704,11 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
               gP[o] = sqrtf(q) / (q + a.regP);  // qNewton.py:131-136 (1/Omax applied later)
           }
         }
-        for (int p = 0; p < npsm; ++p) {
+        // per-wavelength probe mode p; with several wavelengths (ePIE) object
+        // mode o pairs with the probe of wavelength o / nosmW, and the object
+        // and probe steps sum over the wavelengths (ePIE.py:128-160: axes 0,
+        // 2, 3 and 0, 1, 3), every wavelength's copy taking the same step
+        for (int p = 0; p < npsmW; ++p) {
           const float2 P = sm.probe[p * pst + i];
           const float q = cabs2(P);
           float gO;
@@ -712,15 +724,22 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
 #pragma unroll
           for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
             if (o < nosm) {
-              const float2 d = sm.rows[(o * npsm + p) * LN + i];
-              accO[o] = cadd(accO[o], cscale(cmulc(P, d), gO));
+              const float2 Po = nl == 1 ? P : sm.probe[((o / nosmW) * npsmW + p) * pst + i];
+              const float2 d = sm.rows[(o * npsmW + p) * LN + i];
+              accO[o] = cadd(accO[o], cscale(cmulc(Po, d), gO));
               accP = cadd(accP, cscale(cmulc(O[o], d), gP[o]));
             }
           }
-          if (qn)
+          if (qn) {
             sm.U[p * LN + i] = accP;
-          else
+          } else if (nl == 1) {
             sm.probe[p * pst + i] = cadd(P, cscale(accP, stepP));
+          } else {
+            for (int w = 0; w < nl; ++w) {
+              float2* Pw = sm.probe + (w * npsmW + p) * pst + i;
+              *Pw = cadd(*Pw, cscale(accP, stepP));
+            }
+          }
           if (mq) {
             const float2 d = csub(s.probeBuffer[(size_t)p * NP * NP + (size_t)line0 * NP + i], P);
             tdd += (double)d.x * d.x + (double)d.y * d.y;
@@ -733,7 +752,14 @@ __global__ void __launch_bounds__(MQ ? 256 : 512, 1) engine_kernel(const EngineA
 #pragma unroll
         for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
           if (o < nosm) {
-            const float2 On = cadd(O[o], cscale(accO[o], a.betaO));
+            float2 u = accO[o];
+            if (nl > 1) {
+              u = make_float2(0.f, 0.f);
+#pragma unroll
+              for (int o2 = 0; o2 < MAX_OBJECT_MODES; ++o2)
+                if (o2 < nosm && o2 % nosmW == o % nosmW) u = cadd(u, accO[o2]);
+            }
+            const float2 On = cadd(O[o], cscale(u, a.betaO));
             st_cg(s.object + o * No2 + (size_t)(row0 + line0 + l) * No + col0 + x, On);
             onew += cabs(On);
             if (mq) {
@@ -937,55 +963,56 @@ inline cudaLaunchConfig_t launch_config(int cluster, int grid, int threads, size
   return cfg;
 }
 
-template <int E, int L, bool MQ>
+template <int E, int L, int VAR>
 cudaError_t prepare_t(size_t smem) {
-  auto kern = engine_kernel<E, L, MQ>;
+  auto kern = engine_kernel<E, L, VAR>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (32 * E / L > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   return e;
 }
 
-template <int E, int L, bool MQ>
+template <int E, int L, int VAR>
 cudaError_t launch_t(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
-  cudaError_t e = prepare_t<E, L, MQ>(smem);
+  cudaError_t e = prepare_t<E, L, VAR>(smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = launch_config(a.cluster, nscans * a.cluster, threads, smem, st, attr);
-  return cudaLaunchKernelEx(&cfg, engine_kernel<E, L, MQ>, a);
+  return cudaLaunchKernelEx(&cfg, engine_kernel<E, L, VAR>, a);
 }
 
-template <int E, int L, bool MQ>
+template <int E, int L, int VAR>
 cudaError_t clusters_t(int threads, size_t smem, int* out) {
-  cudaError_t e = prepare_t<E, L, MQ>(smem);
+  cudaError_t e = prepare_t<E, L, VAR>(smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = launch_config(32 * E / L, 32 * E / L, threads, smem, 0, attr);
-  return cudaOccupancyMaxActiveClusters(out, (void*)engine_kernel<E, L, MQ>, &cfg);
+  return cudaOccupancyMaxActiveClusters(out, (void*)engine_kernel<E, L, VAR>, &cfg);
 }
 
 // Instantiated shapes: 8 or 16 rows per CTA, at most 16 CTAs per cluster.
 #define PTYG_ENGINE_SHAPES(X) X(1, 8) X(1, 16) X(2, 8) X(2, 16) X(4, 8) X(4, 16) X(8, 16)
 
 
-// Launch / occupancy over the instantiated shapes for one MQ value; each
-// translation unit instantiates one (ptyg_engine.cu: false, ptyg_engine_mq.cu: true).
-template <bool MQ>
+// Launch / occupancy over the instantiated shapes for one variant; each
+// translation unit instantiates one (ptyg_engine.cu: VAR_STD,
+// ptyg_engine_mq.cu: VAR_MQ, ptyg_engine_poly.cu: VAR_POLY).
+template <int VAR>
 cudaError_t engine_max_clusters_t(int Np, int cluster, int threads, size_t smem, int* out) {
   *out = 0;
   const int E = Np / 32, L = Np / cluster;
 #define PTYG_CALL(e, l) \
-  if (E == e && L == l) return clusters_t<e, l, MQ>(threads, smem, out);
+  if (E == e && L == l) return clusters_t<e, l, VAR>(threads, smem, out);
   PTYG_ENGINE_SHAPES(PTYG_CALL)
 #undef PTYG_CALL
   return cudaErrorNotSupported;
 }
 
-template <bool MQ>
+template <int VAR>
 cudaError_t launch_engine_t(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
   const int E = a.Np / 32, L = a.Np / a.cluster;
 #define PTYG_CALL(e, l) \
-  if (E == e && L == l) return launch_t<e, l, MQ>(a, nscans, threads, smem, st);
+  if (E == e && L == l) return launch_t<e, l, VAR>(a, nscans, threads, smem, st);
   PTYG_ENGINE_SHAPES(PTYG_CALL)
 #undef PTYG_CALL
   return cudaErrorNotSupported;

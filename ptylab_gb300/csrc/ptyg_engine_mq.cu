@@ -5,11 +5,11 @@
 namespace ptyg {
 
 cudaError_t engine_max_clusters_mq(int Np, int cluster, int threads, size_t smem, int* out) {
-  return engine_max_clusters_t<true>(Np, cluster, threads, smem, out);
+  return engine_max_clusters_t<VAR_MQ>(Np, cluster, threads, smem, out);
 }
 
 cudaError_t launch_engine_mq(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
-  return launch_engine_t<true>(a, nscans, threads, smem, st);
+  return launch_engine_t<VAR_MQ>(a, nscans, threads, smem, st);
 }
 
 }  // namespace ptyg

@@ -53,15 +53,17 @@ cudaError_t mix_modes(const float2* V, const float2* p, float2* out, int modes, 
 
 int set_last_error(int code, const char* msg);
 
-size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int engine, bool probe_in_smem);
+size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int nlambda, int engine, bool probe_in_smem);
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 bool engine_modes_supported(int Np, int nosm, int npsm);
 bool engine_shape_supported(int Np, int cluster);
 size_t e3pie_smem_bytes(int Np, int C, int npsm);
 cudaError_t e3pie_max_clusters(int Np, int cluster, int threads, size_t smem, int* out);
 cudaError_t launch_e3pie(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
-cudaError_t engine_max_clusters(int Np, int engine, int cluster, int threads, size_t smem, int* out);
+cudaError_t engine_max_clusters(int Np, int engine, int nlambda, int cluster, int threads, size_t smem, int* out);
 cudaError_t engine_max_clusters_mq(int Np, int cluster, int threads, size_t smem, int* out);
 cudaError_t launch_engine_mq(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
+cudaError_t engine_max_clusters_poly(int Np, int cluster, int threads, size_t smem, int* out);
+cudaError_t launch_engine_poly(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 
 }  // namespace ptyg

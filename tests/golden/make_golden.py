@@ -6,7 +6,7 @@ Usage (needs the reference source tree; run where it is present)::
 
 What it writes, all under ``tests/golden/``:
 
-* ``reg_<name>.npz`` -- the eight in-scope configurations of the reference's
+* ``reg_<name>.npz`` -- the nine configurations of the reference's
   engine regression suite (``tests/regression/test_engine_regression.py:47-57``)
   on the dataset of ``tests/regression/conftest.py:22-51`` rebuilt in NumPy.
   Before writing, each result is checked against the reference's own committed
@@ -211,6 +211,11 @@ def run_case(ref, d, case):
         rec.No = d["No"]
     nl, nos, nps, nsl = case.get("modes", (1, 1, 1, 1))
     rec.nlambda, rec.nosm, rec.npsm, rec.nslice = nl, nos, nps, nsl
+    if nl > 1:
+        # tests/regression/test_engine_regression.py:78-80
+        base = float(np.atleast_1d(rec.wavelength)[0])
+        rec.spectralDensity = base * np.linspace(0.98, 1.02, nl)
+        extra_inputs["spectralDensity"] = np.asarray(rec.spectralDensity, dtype=np.float64).copy()
     if nsl > 1:
         rec.dz = case.get("dz", 1e-4)
         rec.refrIndex = 1.0
@@ -339,13 +344,14 @@ def run_propagator(ref, d, prop):
 
 
 REG_CONFIGS = {
-    # tests/regression/test_engine_regression.py:47-57 (in-scope rows)
+    # tests/regression/test_engine_regression.py:47-57 (all nine rows)
     "epie_fraunhofer": dict(
         engine="ePIE", propagator="Fraunhofer", modes=(1, 1, 1, 1), iters=3, keep_detector_error=True
     ),
     "epie_asp": dict(engine="ePIE", propagator="ASP", modes=(1, 1, 1, 1), iters=3),
     "epie_fresnel": dict(engine="ePIE", propagator="Fresnel", modes=(1, 1, 1, 1), iters=3),
     "epie_mixed_state": dict(engine="ePIE", propagator="Fraunhofer", modes=(1, 2, 3, 1), iters=3),
+    "epie_polychrome": dict(engine="ePIE", propagator="polychromeASP", modes=(3, 1, 1, 1), iters=2),
     "mpie_single": dict(engine="mPIE", propagator="Fraunhofer", modes=(1, 1, 1, 1), iters=3),
     "mpie_mixed_state": dict(engine="mPIE", propagator="Fraunhofer", modes=(1, 2, 3, 1), iters=3),
     "qnewton_single": dict(engine="qNewton", propagator="Fraunhofer", modes=(1, 1, 1, 1), iters=3),

@@ -515,3 +515,32 @@ def test_config2_size_e3pie_precision_vs_complex128(torch_cuda):
     for k in keys:
         assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 1e-5, msg
     assert rec.objectProd.shape == (1, 1, 1, 384, 384)
+
+
+@pytest.mark.parametrize("propagator,modes", [("polychromeASP", (2, 1, 2)), ("Fraunhofer", (3, 1, 1)),
+                                              ("polychromeASP", (2, 2, 1))])
+def test_several_wavelengths_follow_the_oracle_on_a_moving_scan(torch_cuda, propagator, modes):
+    """ePIE over several wavelengths on the Fermat scan (the regression
+    dataset's frames all sit at one position): the GPU against the oracle
+    (the reference's algorithm, checked bit-exact against the reference's
+    polychrome golden) from the same seeded start, 2 iterations."""
+    from oracle import ptyoracle as O
+
+    fx = dict(load_fixture("scan_epie_random"))
+    nl, nos, nps = modes
+    m, i, d, p, rec = containers(fx)
+    rec.nlambda, rec.nosm, rec.npsm = nl, nos, nps
+    rec.spectralDensity = float(np.atleast_1d(rec.wavelength)[0]) * np.linspace(0.98, 1.02, nl)
+    np.random.seed(int(fx["meta_seed"]))
+    rec.initializeObjectProbe()
+    fx["meta_modes"] = np.array([nl, nos, nps, 1])
+    fx["meta_propagator"] = np.asarray(propagator)
+    fx["meta_iters"] = np.asarray(2)
+    fx["in_spectralDensity"] = np.asarray(rec.spectralDensity)
+    fx["in_init_object"], fx["in_init_probe"] = rec.object.copy(), rec.probe.copy()
+    got, _ = run_fixture_gpu(fx)
+    want, want128 = O.run_fixture(fx), O.run_fixture(fx, dtype=np.complex128)
+    for key in ("object", "probe", "error"):
+        e = rel_err(getattr(got, key), getattr(want, key))
+        floor = rel_err(getattr(want, key), getattr(want128, key))
+        assert e < max(1e-4, 3 * floor), (key, e, floor)

@@ -49,6 +49,8 @@ def containers(fx):
     rec = Reconstruction(d, p, No=int(i["No"]) if mode == "FPM" else None)
     nl, nos, nps, nsl = (int(v) for v in m["modes"])
     rec.nlambda, rec.nosm, rec.npsm, rec.nslice = nl, nos, nps, nsl
+    if "spectralDensity" in i:
+        rec.spectralDensity = np.array(i["spectralDensity"], copy=True)
     if nsl > 1:
         rec.dz = float(i["dz"])
         rec.refrIndex = 1.0
@@ -173,3 +175,30 @@ def test_reconstruct_batch_rejects_mismatched_engines():
         m, i, d, p, rec = containers(fx)
         rec.object, rec.probe = i["init_object"].copy(), i["init_probe"].copy()
         Engines.reconstruct_batch([make("scan_epie_random"), Engines.qNewton(rec, d, p, DummyMonitor())])
+
+
+def test_several_wavelengths_are_checked_before_device_work():
+    """nlambda > 1 runs with ePIE only; ASP refuses it as PtyLab's does
+    (Operators.py:866-869) and polychromeASP needs a wavelength per slot."""
+    from ptylab_gb300 import DummyMonitor, Engines
+
+    def setup(engine, propagator, spectral=True):
+        fx = load_fixture("reg_epie_polychrome")
+        m, i, d, p, rec = containers(fx)
+        p.propagatorType = propagator
+        if not spectral:
+            rec.spectralDensity = np.atleast_1d(rec.wavelength)
+        rec.object, rec.probe = i["init_object"].copy(), i["init_probe"].copy()
+        rec.initialGuessObject, rec.initialGuessProbe = rec.object.copy(), rec.probe.copy()
+        return getattr(Engines, engine)(rec, d, p, DummyMonitor())
+
+    with pytest.raises(NotImplementedError):
+        setup("mPIE", "polychromeASP")._check_supported()
+    with pytest.raises(NotImplementedError):
+        setup("qNewton", "polychromeASP")._check_supported()
+    with pytest.raises(ValueError):
+        setup("ePIE", "ASP")._check_supported()
+    with pytest.raises(ValueError):
+        setup("ePIE", "polychromeASP", spectral=False)._check_supported()
+    setup("ePIE", "polychromeASP")._check_supported()
+    setup("ePIE", "Fraunhofer")._check_supported()
