@@ -194,7 +194,9 @@ def run_gb300(args, rank, world, local_rank):
     def geometry(nscans, throughput):
         return _native.Geometry(Np=NP, No=NO, nosm=1, npsm=NPSM, nslice=1, num_frames=NPOS, num_scans=nscans,
                                 engine=_native.ENGINES["mPIE"], propagator=0, fftshift=0, fpm=0,
-                                cluster=args.cluster, throughput=throughput)
+                                cluster=args.cluster, throughput=throughput,
+                                threads=args.threads if throughput else 0,
+                                probe_in_smem=args.probe_smem if throughput else 0)
 
     probe_plan = C.c_void_p()
     _native.check(lib.ptyg_plan_create(C.byref(geometry(1, 1)), C.byref(probe_plan)))
@@ -302,7 +304,7 @@ def run_gb300(args, rank, world, local_rank):
         te = time.perf_counter() - t0
         d0, _, r0 = host_scans[0]
         per_scan_h2d = d0.ptychogram.nbytes + 3 * r0.object.nbytes + 3 * r0.probe.nbytes + NPOS * 2 * 4
-        per_scan_d2h = 3 * r0.object.nbytes + 3 * r0.probe.nbytes + NPOS * NP * NP * 4
+        per_scan_d2h = 3 * r0.object.nbytes + 3 * r0.probe.nbytes + NPOS * NP * NP * 8  # detectorError as float64
         h2d = G * (per_scan_h2d + args.steps * NPOS * 5)
         d2h = G * (per_scan_d2h + args.steps * NPOS * 8)
         e2e = {"value": G * NPOS * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
@@ -419,6 +421,9 @@ def main():
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per scan (0: the library's choice)")
     ap.add_argument("--cpu-iters", type=int, default=8, help="iterations of the one-core CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--threads", type=int, default=0, help="CTA size of the batched launch (0 = the plan's choice)")
+    ap.add_argument("--probe-smem", type=int, default=0,
+                    help="batched launch: 0 = plan's choice, 1 = probe rows in L2, 2 = in shared memory")
     ap.add_argument("--ref-procs", type=int, default=0)
     ap.add_argument("--warmup-ref", type=int, default=1)
     args = ap.parse_args()

@@ -158,6 +158,14 @@ typedef struct ptyg_geometry {
                           one per wavelength (polychromeASP, Operators.py:458-505),
                           and the object and probe steps summed over the
                           wavelengths (ePIE.py:128-160) */
+  int32_t threads;     /* threads per CTA, a multiple of 32 in [128, 512]
+                          (mqNewton: at most 256); 0 = one warp per transform
+                          task of a pass, at most 16 warps.  With 256 threads
+                          and a shared-memory layout under half an SM's,
+                          two CTAs share an SM and hide each other's stalls */
+  int32_t probe_in_smem; /* 0 = choose (shared memory when it fits), 1 = keep
+                            the CTA's probe rows in global memory (L2),
+                            2 = require them in shared memory */
 } ptyg_geometry;
 
 /* Engine scalars (ePIE.py:35-42, mPIE.py:233-245, qNewton.py:43-52,
@@ -275,6 +283,12 @@ PTYG_API int ptyg_plan_run(ptyg_plan* plan, const ptyg_update_params* params, in
 /* Per-frame sum_xy |I_meas - I_est| of the frames processed since the plan
  * was bound (FP64), into `host_out` (num_frames doubles); synchronises. */
 PTYG_API int ptyg_plan_frame_errors(ptyg_plan* plan, int scan, double* host_out, void* stream);
+
+/* The same sums into `device_out` (num_frames doubles of device memory),
+ * stream-ordered and without synchronising, so a host loop can queue the
+ * next iteration while this one runs and read every iteration's sums once at
+ * the end. */
+PTYG_API int ptyg_plan_frame_errors_device(ptyg_plan* plan, int scan, double* device_out, void* stream);
 
 /* The recorded |I_meas - I_est| maps (flags bit 0) in natural layout:
  * `out` is device float32 (num_frames, Np, Np). */

@@ -25,6 +25,8 @@ import numpy as np
 from .. import _native, _tables
 from ..Reconstruction import circ
 
+_UPLOAD_SLOTS = 3  # iterations the host may queue ahead of the GPU
+
 # Switches whose branches are not on this path; PtyLab default for all is off.
 _UNSUPPORTED = (
     "CPSCswitch",
@@ -62,6 +64,8 @@ def _torch():
 
 class BaseEngine(object):
     engine_name = "BaseEngine"
+    _err_n = 0  # iterations whose frame sums wait on the device (_record_errors)
+    _err_dev = None
 
     def __init__(self, reconstruction, experimentalData, params, monitor):
         self.betaObject = 0.25
@@ -243,8 +247,18 @@ class BaseEngine(object):
         self._dev["data"] = self._to_device(d.ptychogram, torch.float32)
         self._dev["order"] = torch.zeros(nf, dtype=torch.int32, device=device)
         self._dev["flags"] = torch.zeros(nf, dtype=torch.uint8, device=device)
-        self._order_host = torch.zeros(nf, dtype=torch.int32).pin_memory()
-        self._flags_host = torch.zeros(nf, dtype=torch.uint8).pin_memory()
+        # a ring of pinned staging buffers for the per-iteration order and
+        # momentum flags: the host fills slot n while the copies of earlier
+        # iterations may still be queued; slot n's event (its last copy)
+        # is waited on before the slot is reused
+        self._upload_ring = [
+            (torch.zeros(nf, dtype=torch.int32).pin_memory(), torch.zeros(nf, dtype=torch.uint8).pin_memory())
+            for _ in range(_UPLOAD_SLOTS)
+        ]
+        self._upload_events = [None] * _UPLOAD_SLOTS
+        self._uploads = 0
+        self._err_dev = None  # per-iteration frame sums awaiting readback
+        self._err_n = 0
 
     def _geometry(self, num_scans=1, throughput=0):
         rec, d, p = self.reconstruction, self.experimentalData, self.params
@@ -378,11 +392,19 @@ class BaseEngine(object):
 
     def _upload_order(self, momentum=None):
         torch = _torch()
-        self._order_host.copy_(torch.from_numpy(np.asarray(self.positionIndices, dtype=np.int32)))
-        self._dev["order"].copy_(self._order_host, non_blocking=True)
+        slot = self._uploads % _UPLOAD_SLOTS
+        if self._upload_events[slot] is not None:
+            self._upload_events[slot].synchronize()
+        order_host, flags_host = self._upload_ring[slot]
+        order_host.copy_(torch.from_numpy(np.asarray(self.positionIndices, dtype=np.int32)))
+        self._dev["order"].copy_(order_host, non_blocking=True)
         if momentum is not None:
-            self._flags_host.copy_(torch.from_numpy(np.asarray(momentum, dtype=np.uint8)))
-            self._dev["flags"].copy_(self._flags_host, non_blocking=True)
+            flags_host.copy_(torch.from_numpy(np.asarray(momentum, dtype=np.uint8)))
+            self._dev["flags"].copy_(flags_host, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self._dev["device"]))
+        self._upload_events[slot] = ev
+        self._uploads += 1
 
     def _run_positions(self, start, count, record_detector_error=False):
         torch = _torch()
@@ -409,11 +431,12 @@ class BaseEngine(object):
         self._upload_order()
 
     def _loop_end(self, loop):
-        self.getErrorMetrics()
+        self._record_errors()
         self.applyConstraints(loop)
         self.showReconstruction(loop)
 
     def _finish(self):
+        self._resolve_errors()
         self._move_data_to_cpu(detector_error=self.numIterations > 0)
 
     def _run_loop(self):
@@ -436,7 +459,7 @@ class BaseEngine(object):
             self.positionIndices = np.arange(nf)
         elif order == "random":
             self.positionIndices = np.arange(nf)
-            if len(self.reconstruction.error) >= 2:
+            if len(self.reconstruction.error) + self._err_n >= 2:
                 np.random.shuffle(self.positionIndices)
         elif order == "NA":
             pos = self._positions_host
@@ -449,13 +472,48 @@ class BaseEngine(object):
     def getErrorMetrics(self):
         """BaseEngine.py:819-841, from the per-frame FP64 sums of |I_meas - I_est|."""
         torch = _torch()
-        rec = self.reconstruction
+        self._resolve_errors()
         nf = self.experimentalData.numFrames
         err = np.empty(nf, dtype=np.float64)
         stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
         _native.check(
             self._dev["lib"].ptyg_plan_frame_errors(self._plan, self._scan, err.ctypes.data, stream), "ptyg_plan_frame_errors"
         )
+        self._append_errors(err)
+
+    def _record_errors(self):
+        """getErrorMetrics without waiting for the GPU: this iteration's
+        per-frame sums go to a device row (queued on the stream), and
+        _resolve_errors turns the rows into rec.errorAtPos and rec.error in
+        iteration order once, so the host can queue the next iteration while
+        this one runs."""
+        torch = _torch()
+        nf = self.experimentalData.numFrames
+        if self._err_dev is None or self._err_n == self._err_dev.shape[0]:
+            grown = torch.empty((max(int(self.numIterations), 1) + self._err_n, nf), dtype=torch.float64,
+                                device=self._dev["device"])
+            if self._err_n:
+                grown[: self._err_n].copy_(self._err_dev[: self._err_n])
+            self._err_dev = grown
+        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
+        _native.check(
+            self._dev["lib"].ptyg_plan_frame_errors_device(self._plan, self._scan, self._err_dev[self._err_n].data_ptr(),
+                                                           stream),
+            "ptyg_plan_frame_errors_device",
+        )
+        self._err_n += 1
+
+    def _resolve_errors(self):
+        if not self._err_n:
+            return
+        rows = self._err_dev[: self._err_n].cpu().numpy()
+        self._err_n = 0
+        for err in rows:
+            self._append_errors(err)
+
+    def _append_errors(self, err):
+        rec = self.reconstruction
+        nf = self.experimentalData.numFrames
         energy = np.asarray(self.experimentalData.energyAtPos)
         if self.params.saveMemory:
             # getRMSD stores one sum per position into errorAtPos (BaseEngine.py:857-866)
@@ -548,7 +606,9 @@ class BaseEngine(object):
         _native.check(
             self._dev["lib"].ptyg_plan_detector_error(self._plan, self._scan, out.data_ptr(), stream), "ptyg_plan_detector_error"
         )
-        return out.cpu().numpy().astype(np.float64)
+        # PtyLab stores detectorError as float64: widen on the GPU, where it
+        # costs nothing, rather than on one host core after the copy
+        return out.to(torch.float64).cpu().numpy()
 
     def _check_status(self):
         st = C.c_int(0)

@@ -79,4 +79,5 @@ class mPIE(BaseEngine):
         super()._loop_end(loop)
         vis = getattr(self, "_vis", None)
         if callable(vis):
+            self._resolve_errors()  # the callback sees this iteration's error
             vis(loop, self.reconstruction)

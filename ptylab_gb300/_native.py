@@ -58,6 +58,8 @@ class Geometry(C.Structure):
         ("cluster", C.c_int32),
         ("throughput", C.c_int32),
         ("nlambda", C.c_int32),
+        ("threads", C.c_int32),
+        ("probe_in_smem", C.c_int32),
     ]
 
 
@@ -145,6 +147,7 @@ _SIGNATURES = {
         C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
     ],
     "ptyg_plan_frame_errors": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_plan_frame_errors_device": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_detector_error": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_status": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p],
     "ptyg_plan_set_projection": [C.c_void_p, C.POINTER(Projection), C.c_void_p, C.c_void_p, C.c_void_p],

@@ -397,6 +397,11 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   if (g.nlambda < 1) return fail(PTYG_ERR_INVALID, "nlambda=%d", g.nlambda);
   if (g.nlambda > 1 && g.engine != PTYG_EPIE)
     return fail(PTYG_ERR_UNSUPPORTED, "nlambda=%d: several wavelengths run with the ePIE engine only", g.nlambda);
+  if (g.threads != 0 &&
+      (g.threads % 32 != 0 || g.threads < 128 || g.threads > (g.engine == PTYG_MQNEWTON ? 256 : 512)))
+    return fail(PTYG_ERR_INVALID, "threads=%d: a multiple of 32 in [128, %d]", g.threads,
+                g.engine == PTYG_MQNEWTON ? 256 : 512);
+  if (g.probe_in_smem < 0 || g.probe_in_smem > 2) return fail(PTYG_ERR_INVALID, "probe_in_smem=%d", g.probe_in_smem);
   if (!valid_np(g.Np)) return fail(PTYG_ERR_UNSUPPORTED, "Np=%d: supported sizes are 32, 64, 128, 256", g.Np);
   if (g.No < g.Np) return fail(PTYG_ERR_INVALID, "No=%d smaller than Np=%d", g.No, g.Np);
   if (g.nosm < 1 || g.npsm < 1 || g.nslice < 1 || g.num_frames < 1 || g.num_scans < 1)
@@ -429,9 +434,10 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   for (int c : cluster_candidates(g)) {
     if (!ptyg::engine_shape_supported(g.Np, c)) continue;
     for (bool psm : {true, false}) {
+      if ((g.probe_in_smem == 1 && psm) || (g.probe_in_smem == 2 && !psm)) continue;
       p->C = c;
       p->probeInSmem = psm;
-      p->threads = engine_threads(g, c);
+      p->threads = g.threads > 0 ? g.threads : engine_threads(g, c);
       const bool e3 = g.engine == PTYG_E3PIE;
       if (e3 && psm) continue;  // e3PIE keeps its probe slices in global memory
       p->smem = e3 ? ptyg::e3pie_smem_bytes(g.Np, c, g.npsm)
@@ -729,6 +735,14 @@ extern "C" int ptyg_plan_frame_errors(ptyg_plan* p, int scan, double* host_out, 
   PTYG_CUDA(cudaMemcpyAsync(host_out, o.err, p->g.num_frames * sizeof(double), cudaMemcpyDeviceToHost, st),
             "error readback");
   PTYG_CUDA(cudaStreamSynchronize(st), "error readback");
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_frame_errors_device(ptyg_plan* p, int scan, double* device_out, void* stream) {
+  if (!p || !device_out) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  ScanOwned& o = p->scans[scan];
+  PTYG_CUDA(ptyg::sum_parts(o.errPart, device_out, p->g.num_frames, p->C, (cudaStream_t)stream), "error sum");
   return PTYG_OK;
 }
 
