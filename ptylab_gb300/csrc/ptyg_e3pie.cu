@@ -28,7 +28,7 @@ template <int E, int L>
 __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
   constexpr int NP = 32 * E;
   constexpr int C = NP / L;
-  constexpr int LN = L * NP, ld = L + 1;
+  constexpr int LN = L * NP;
   const int crank = (int)(blockIdx.x % (unsigned)C);
   const ScanDev s = a.scans[blockIdx.x / C];
   const int line0 = crank * L, sx0 = crank * L;
@@ -42,8 +42,8 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
   const int blk0 = asp ? line0 : sx0;
 
   extern __shared__ float4 smem_f4[];
-  float2* tile = reinterpret_cast<float2*>(smem_f4);  // K * NP * ld
-  float2* rows = tile + K * NP * ld;                  // K * LN
+  float2* tile = reinterpret_cast<float2*>(smem_f4);  // K * NP * L (swizzled, tix)
+  float2* rows = tile + K * NP * L;                   // K * LN
   float* fr = reinterpret_cast<float*>(rows + K * LN);
   float* dat = fr + LN;  // 2 * LN
   unsigned* slots = reinterpret_cast<unsigned*>(dat + 2 * LN);
@@ -179,12 +179,12 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           [&](int t, float2(&v)[E]) {
             const int k = t / L, c = t % L;
 #pragma unroll
-            for (int j = 0; j < E; ++j) v[j] = tile[(k * NP + lane + 32 * j) * ld + c];
+            for (int j = 0; j < E; ++j) v[j] = tile[tix<L>(k * NP + lane + 32 * j, c)];
           },
           [&](int t, float2(&v)[E]) {
             const int k = t / L, c = t % L;
 #pragma unroll
-            for (int r = 0; r < E; ++r) tile[(k * NP + 32 * r + lane) * ld + c] = v[r];
+            for (int r = 0; r < E; ++r) tile[tix<L>(k * NP + 32 * r + lane, c)] = v[r];
           });
       __syncthreads();
       {
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
         for (int i = threadIdx.x; i < LN; i += blockDim.x) {
           const int c = i / NP, sy = i % NP;
           float ie = 0.f;
-          for (int k = 0; k < K; ++k) ie += cabs2(tile[(k * NP + sy) * ld + c]);
+          for (int k = 0; k < K; ++k) ie += cabs2(tile[tix<L>(k * NP + sy, c)]);
           ie *= inv2;
           const float im = datc[i];
           const float d = fabsf(im - ie);
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
             const int k = t / L, c = t % L;
 #pragma unroll
             for (int r = 0; r < E; ++r)
-              v[r] = cscale(tile[(k * NP + 32 * r + lane) * ld + c], fr[c * NP + 32 * r + lane]);
+              v[r] = cscale(tile[tix<L>(k * NP + 32 * r + lane, c)], fr[c * NP + 32 * r + lane]);
           },
           [&](int t, float2(&v)[E]) { scatter_column<E, L>(rows, v, t / L, sx0 + t % L); });
     } else {
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
 size_t e3pie_smem_bytes(int Np, int C, int npsm) {
   const int L = Np / C;
   const size_t LN = (size_t)L * Np;
-  const size_t n = (size_t)npsm * Np * (L + 1) + (size_t)npsm * LN;
+  const size_t n = (size_t)npsm * Np * L + (size_t)npsm * LN;
   // redF holds 32 floats per reduced value: MAX_SLICES + 1 of them
   return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
          8 * 32 * sizeof(float) + 64;

@@ -12,9 +12,9 @@ size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int nlambda, int eng
   const bool qn = engine == ENG_QNEWTON || engine == ENG_MQNEWTON;
   const size_t n =
       smem_complex_elems(Np, L, nlambda * nosm * npsm, nlambda * nosm, nlambda * npsm, qn, probe_in_smem);
-  // + fr, dat (3 LN floats), slots, redD (4 x 32 doubles), redF (4 x 32
+  // + fr, dat (2 LN floats), slots, redD (4 x 32 doubles), redF (4 x 32
   // floats), part (4 x 16 doubles), alignment slack
-  return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 4 * 32 * sizeof(double) +
+  return n * sizeof(float2) + 2 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 4 * 32 * sizeof(double) +
          4 * 32 * sizeof(float) + 4 * 16 * sizeof(double) + 64;
 }
 

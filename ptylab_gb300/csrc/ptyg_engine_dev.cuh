@@ -154,18 +154,29 @@ PTYG_DEV float slot_value(const unsigned* slots, int i) {
   return __uint_as_float(*reinterpret_cast<const volatile unsigned*>(slots + i));
 }
 
+// Column block (tile) layout: row (k * NP + y) holds the CTA's L columns,
+// unpadded, column c stored at c ^ swz(row).  The swizzle spreads the 16
+// consecutive rows of a 64-bit half-warp access (a column task: lanes step
+// through y) over 16 distinct bank pairs: swz = row & 15 for L = 16 and
+// (row >> 1) & 7 for L = 8 (where a row pair shares one 16-element span).
+// A row write (lanes step through c) stays one permuted contiguous span.
+template <int L>
+PTYG_DEV int tix(int row, int c) {
+  static_assert(L == 8 || L == 16, "tile swizzle defined for 8 or 16 columns");
+  return row * L + (c ^ ((row / (16 / L)) & (L - 1)));
+}
+
 // A row task's transformed row (Fourier layout: register r, lane l is slot
 // 32r + l) goes to the column blocks of the CTAs owning those slots.
 template <int E, int L>
 PTYG_DEV void scatter_row(float2* tile, const float2 (&v)[E], int k, int y) {
   constexpr int NP = 32 * E;
-  constexpr int ld = L + 1;
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int r = 0; r < E; ++r) {
     const int sx = 32 * r + lane;
     const int owner = sx / L, c = sx - (sx / L) * L;
-    *dsmem(&tile[(k * NP + y) * ld + c], owner) = v[r];
+    *dsmem(&tile[tix<L>(k * NP + y, c)], owner) = v[r];
   }
 }
 
@@ -190,7 +201,6 @@ template <int E, int L, bool SETS = false>
 PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, const float2* H, bool conjH, int crank,
                             int K, int kPerSet) {
   constexpr int NP = 32 * E;
-  constexpr int ld = L + 1;
   const int lane = threadIdx.x & 31;
   const int sx0 = crank * L;
   const float inv2 = 1.f / (float)(NP * NP);
@@ -199,7 +209,7 @@ PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, con
       [&](int t, float2(&v)[E]) {
         const int k = t / L, c = t % L;
 #pragma unroll
-        for (int j = 0; j < E; ++j) v[j] = tile[(k * NP + lane + 32 * j) * ld + c];
+        for (int j = 0; j < E; ++j) v[j] = tile[tix<L>(k * NP + lane + 32 * j, c)];
       },
       [&](int t, float2(&v)[E]) {
         const int k = t / L, c = t % L;
@@ -209,7 +219,7 @@ PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, con
         for (int r = 0; r < E; ++r) {
           float2 hv = __ldg(h + r * 32 + lane);
           if (conjH) hv.y = -hv.y;
-          tile[(k * NP + 32 * r + lane) * ld + c] = cscale(cmul(v[r], hv), inv2);
+          tile[tix<L>(k * NP + 32 * r + lane, c)] = cscale(cmul(v[r], hv), inv2);
         }
       });
   __syncthreads();
@@ -218,7 +228,7 @@ PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, con
       [&](int t, float2(&v)[E]) {
         const int k = t / L, c = t % L;
 #pragma unroll
-        for (int r = 0; r < E; ++r) v[r] = tile[(k * NP + 32 * r + lane) * ld + c];
+        for (int r = 0; r < E; ++r) v[r] = tile[tix<L>(k * NP + 32 * r + lane, c)];
       },
       [&](int t, float2(&v)[E]) { scatter_column<E, L>(rows, v, t / L, sx0 + t % L); });
 }
@@ -226,13 +236,14 @@ PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, con
 // Prefetch the measured intensities of order slot `it` (if it exists and is a
 // valid frame) into dat[it & 1]: the CTA's L*NP block is contiguous in both
 // layouts (Fourier [frame][sx][sy] columns sx0.., or natural rows line0..).
-template <int NP, int L>
+// DOUBLE: dat[it & 1] of a double buffer, else the one buffer.
+template <int NP, int L, bool DOUBLE = true>
 PTYG_DEV void prefetch_data(const EngineArgs& a, const ScanDev& s, float* datBuf, int it, int blk0) {
   if (it < a.count) {
     const int frame = s.order[a.start + it];
     if (frame >= 0 && frame < a.numFrames) {
       const float* src = s.data + ((size_t)frame * NP + blk0) * NP;
-      float* dst = datBuf + (it & 1) * L * NP;
+      float* dst = datBuf + (DOUBLE ? (it & 1) * L * NP : 0);
       for (int i = threadIdx.x; i < L * NP / 4; i += blockDim.x) cp_async16(dst + 4 * i, src + 4 * i);
     }
   }

@@ -296,11 +296,12 @@ __device__ __forceinline__ void object_momentum_strips(float2* object, float2* m
 struct Smem {
   float2* probe;    // npsm * L * NP, the CTA's probe rows (resident all launch)
   float2* obj;      // nosm * L * NP, this position's object patch rows
-  float2* tile;     // K * NP * (L+1): the CTA's column block (written by every CTA)
+  float2* tile;     // K * NP * L: the CTA's column block (written by every CTA; swizzled, tix)
   float2* rows;     // K * L * NP: the CTA's rows, Fourier layout along x
   float2* U;        // qNewton probe numerators, npsm * L * NP
   float* fr;        // L * NP projection factors
-  float* dat;       // 2 x L * NP measured intensities (double buffer)
+  float* dat;       // L * NP measured intensities: this position's, then (once the
+                    // projection has read them) the next position's, in flight
   unsigned* slots;  // 2 * RED_BANK norm slots (used on rank 0)
   double* redD;     // 4 * 32
   float* redF;      // 4 * 32
@@ -310,7 +311,7 @@ struct Smem {
 __host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int nosm, int npsm, bool qn,
                                                      bool probe_in_smem) {
   const size_t LN = (size_t)L * NP;
-  return (probe_in_smem ? (size_t)npsm * LN : 0) + (size_t)nosm * LN + (size_t)K * NP * (L + 1) + (size_t)K * LN +
+  return (probe_in_smem ? (size_t)npsm * LN : 0) + (size_t)nosm * LN + (size_t)K * NP * L + (size_t)K * LN +
          (qn ? npsm * LN : 0);
 }
 
@@ -328,7 +329,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
   // tile's loads in registers)
   constexpr int NP = 32 * E;
   constexpr int C = NP / L;
-  constexpr int LN = L * NP, ld = L + 1;
+  constexpr int LN = L * NP;
   const int crank = (int)(blockIdx.x % (unsigned)C);
   const ScanDev s = a.scans[blockIdx.x / C];
   const int line0 = crank * L, sx0 = crank * L;
@@ -360,11 +361,11 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
   sm.probe = psm ? reinterpret_cast<float2*>(smem_f4) : s.probe + (size_t)line0 * NP;
   sm.obj = reinterpret_cast<float2*>(smem_f4) + (psm ? npsm * LN : 0);
   sm.tile = sm.obj + nosm * LN;
-  sm.rows = sm.tile + K * NP * ld;
+  sm.rows = sm.tile + K * NP * L;
   sm.U = sm.rows + K * LN;
   sm.fr = reinterpret_cast<float*>(sm.U + (qn ? npsm * LN : 0));
   sm.dat = sm.fr + LN;
-  sm.slots = reinterpret_cast<unsigned*>(sm.dat + 2 * LN);
+  sm.slots = reinterpret_cast<unsigned*>(sm.dat + LN);
   sm.redD = reinterpret_cast<double*>(sm.slots + 2 * RED_BANK);
   sm.redF = reinterpret_cast<float*>(sm.redD + 4 * 32);
   sm.part = reinterpret_cast<double*>(sm.redF + 4 * 32);
@@ -377,7 +378,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
     }
   }
   if (threadIdx.x < 2 * RED_BANK) sm.slots[threadIdx.x] = 0u;
-  prefetch_data<NP, L>(a, s, sm.dat, 0, blk0);
+  prefetch_data<NP, L, false>(a, s, sm.dat, 0, blk0);
   WarpFFT<E> F;
   F.init(a.twiddle, lane);
   // mqNewton second moments: every CTA of the cluster carries the same values
@@ -400,16 +401,16 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
   const float inv2 = 1.f / (float)(NP * NP);
 
   for (int it = 0; it < a.count; ++it) {
-    prefetch_data<NP, L>(a, s, sm.dat, it + 1, blk0);
     const int frame = s.order[a.start + it];
     const int row0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame] : -1;
     const int col0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame + 1] : -1;
     if (row0 < 0 || col0 < 0 || row0 > No - NP || col0 > No - NP) {
       if (crank == 0 && threadIdx.x == 0) atomicCAS(s.status, 0, 2);
+      prefetch_data<NP, L, false>(a, s, sm.dat, it + 1, blk0);  // nothing reads dat here
       continue;  // uniform across the cluster
     }
     unsigned* red = slots0 + (it & 1) * RED_BANK;
-    const float* dat = sm.dat + (it & 1) * LN;
+    const float* dat = sm.dat;
 
     // ---------------- A: stage the patch rows, norms, exit waves, row FFT
     for (int i = threadIdx.x; i < nosm * LN; i += blockDim.x) {
@@ -476,7 +477,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
           }
         },
         [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm.tile, v, t / L, line0 + t % L); });
-    cp_async_wait_prev();  // this position's intensities
+    cp_async_wait_all();  // this position's intensities (the one group in flight)
     cluster_sync(C);
 
     // The intensity projection of this CTA's LN detector pixels
@@ -569,19 +570,19 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
           [&](int t, float2(&v)[E]) {
             const int k = t / L, c = t % L;
 #pragma unroll
-            for (int j = 0; j < E; ++j) v[j] = sm.tile[(k * NP + lane + 32 * j) * ld + c];
+            for (int j = 0; j < E; ++j) v[j] = sm.tile[tix<L>(k * NP + lane + 32 * j, c)];
           },
           [&](int t, float2(&v)[E]) {
             const int k = t / L, c = t % L;
 #pragma unroll
-            for (int r = 0; r < E; ++r) sm.tile[(k * NP + 32 * r + lane) * ld + c] = v[r];
+            for (int r = 0; r < E; ++r) sm.tile[tix<L>(k * NP + 32 * r + lane, c)] = v[r];
           });
       __syncthreads();
       err = project(
           [&](int i) {
             const int c = i / NP, sy = i - (i / NP) * NP;
             float ie = 0.f;
-            for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[(k * NP + sy) * ld + c]);
+            for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[tix<L>(k * NP + sy, c)]);
             return ie * inv2;
           },
           inv2);
@@ -592,7 +593,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
             const int k = t / L, c = t % L;
 #pragma unroll
             for (int r = 0; r < E; ++r)
-              v[r] = cscale(sm.tile[(k * NP + 32 * r + lane) * ld + c], sm.fr[c * NP + 32 * r + lane]);
+              v[r] = cscale(sm.tile[tix<L>(k * NP + 32 * r + lane, c)], sm.fr[c * NP + 32 * r + lane]);
           },
           [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm.rows, v, t / L, sx0 + t % L); });
     } else {
@@ -639,6 +640,9 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
       const double t = block_sum(err, sm.redD);
       if (threadIdx.x == 0) s.errPart[(size_t)frame * C + crank] = t;
     }
+    // every read of dat (the projection) is behind the barrier in block_sum:
+    // fetch the next position's intensities into it while C and A run
+    prefetch_data<NP, L, false>(a, s, sm.dat, it + 1, blk0);
     if (crank == 0 && threadIdx.x < RED_BANK) sm.slots[((it & 1) ^ 1) * RED_BANK + threadIdx.x] = 0u;
     cluster_sync(C);
 
