@@ -908,12 +908,45 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
         Xn = make_float2(__fsub_rn(X.x, __fmul_rn(nu, Mn.x)), __fsub_rn(X.y, __fmul_rn(nu, Mn.y)));
       };
       const size_t nobj = (size_t)nosm * No2;
-      for (size_t i = (size_t)crank * blockDim.x + threadIdx.x; i < nobj; i += (size_t)C * blockDim.x) {
-        float2 Xn, Mn;
-        step(ld_cg(s.object + i), ld_cg(s.objectBuffer + i), ld_cg(s.objectMomentum + i), Xn, Mn);
-        st_cg(s.objectMomentum + i, Mn);
-        st_cg(s.object + i, Xn);
-        st_cg(s.objectBuffer + i, Xn);
+      const size_t stride = (size_t)C * blockDim.x;
+      if (s.vec4 && ((reinterpret_cast<uintptr_t>(s.objectBuffer) & 15) == 0)) {
+        // 16-byte accesses (two pixels), MU of them per array in flight per
+        // thread before any is used: the pass streams three arrays, so it
+        // runs at what L2 delivers rather than one load latency per pixel
+        constexpr int MU = 2;
+        const size_t n4 = nobj / 2;  // No even: whole float4s
+        for (size_t i0 = (size_t)crank * blockDim.x + threadIdx.x; i0 < n4; i0 += MU * stride) {
+          float4 X[MU], B[MU], M[MU];
+#pragma unroll
+          for (int u = 0; u < MU; ++u) {
+            const size_t i = i0 + u * stride;
+            const size_t j = 2 * (i < n4 ? i : 0);  // pixel 0 stands in past the end
+            X[u] = ld_cg_early4(s.object + j);
+            B[u] = ld_cg_early4(s.objectBuffer + j);
+            M[u] = ld_cg_early4(s.objectMomentum + j);
+          }
+#pragma unroll
+          for (int u = 0; u < MU; ++u) {
+            const size_t i = i0 + u * stride;
+            if (i < n4) {
+              float2 X0, M0, X1, M1;
+              step(make_float2(X[u].x, X[u].y), make_float2(B[u].x, B[u].y), make_float2(M[u].x, M[u].y), X0, M0);
+              step(make_float2(X[u].z, X[u].w), make_float2(B[u].z, B[u].w), make_float2(M[u].z, M[u].w), X1, M1);
+              const float4 Xn = make_float4(X0.x, X0.y, X1.x, X1.y), Mn = make_float4(M0.x, M0.y, M1.x, M1.y);
+              __stcg(reinterpret_cast<float4*>(s.objectMomentum) + i, Mn);
+              __stcg(reinterpret_cast<float4*>(s.object) + i, Xn);
+              __stcg(reinterpret_cast<float4*>(s.objectBuffer) + i, Xn);
+            }
+          }
+        }
+      } else {
+        for (size_t i = (size_t)crank * blockDim.x + threadIdx.x; i < nobj; i += stride) {
+          float2 Xn, Mn;
+          step(ld_cg(s.object + i), ld_cg(s.objectBuffer + i), ld_cg(s.objectMomentum + i), Xn, Mn);
+          st_cg(s.objectMomentum + i, Mn);
+          st_cg(s.object + i, Xn);
+          st_cg(s.objectBuffer + i, Xn);
+        }
       }
       for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
         const int p = i / LN, rem = i - (i / LN) * LN;
