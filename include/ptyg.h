@@ -353,9 +353,17 @@ PTYG_API int ptyg_nn_gemm(const void* A, const void* B, int M, int N, int K, int
 
 /* 3x3 'same' convolution of X [Bn][H][W][C0] (channel-concatenated with
  * X1 [Bn][H][W][C1] when C1 > 0; C0, C1 multiples of 8) with weights
- * Wt [Co][9 (C0 + C1)]: into out (bf16, + bias, optional ReLU) or C (float). */
+ * Wt [Co][9 (C0 + C1)]: into out (bf16, + bias, optional ReLU) or C (float).
+ * Where the shapes allow (C0, C1 multiples of min(64, C0, C1) in {16, 32, 64},
+ * 128-pixel tiles of whole image rows or row blocks, Co <= 256) the operands
+ * arrive by TMA (cp.async.bulk.tensor) with the padding as out-of-bounds
+ * zero fill; otherwise every thread gathers them with cp.async. */
 PTYG_API int ptyg_nn_conv3(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, const void* Wt, int Co,
                            float* C, void* out, const float* bias, int relu, int* status, void* stream);
+
+/* Select the ptyg_nn_conv3 operand path for the process: 1 (default) TMA
+ * where the shapes allow, 0 the cp.async gather always (for comparisons). */
+PTYG_API int ptyg_nn_conv3_path(int tma);
 
 /* Weight gradients of a 3x3 convolution: C[z][Co][9 (C0 + C1)] = partial sums
  * over `splits` pixel ranges of dY[p][co] times the patches of X (+ X1) at

@@ -133,6 +133,7 @@ _SIGNATURES = {
     "ptyg_propagate_noalloc": [
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
     ],
+    "ptyg_nn_conv3_path": [C.c_int],
     "ptyg_propagate_sets": [
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -26,6 +26,7 @@
 #include <cstdio>
 
 #include "ptyg.h"
+#include "ptyg_nn_tma.cuh"
 #include "ptyg_ops.cuh"
 
 namespace ptyg {
@@ -815,11 +816,24 @@ extern "C" int ptyg_nn_gemm(const void* A, const void* B, int M, int N, int K, i
   return nn_check(launch_gemm(g, A_DENSE, splits, (cudaStream_t)stream), "ptyg_nn_gemm");
 }
 
+static int g_conv_tma = 1;  // ptyg_nn_conv3_path
+
+extern "C" int ptyg_nn_conv3_path(int tma) {
+  g_conv_tma = tma != 0;
+  return PTYG_OK;
+}
+
 extern "C" int ptyg_nn_conv3(const void* X, const void* X1, int C0, int C1, int Bn, int H, int W, const void* Wt,
                              int Co, float* C, void* out, const float* bias, int relu, int* status, void* stream) {
   if (!X || !Wt || C0 < 8 || (C0 % 8) || (C1 % 8) || (C1 && !X1) || Bn < 1 || H < 1 || W < 1 || Co < 1 ||
       (!C && !out))
     return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_conv3: bad arguments (channels: multiples of 8)");
+  if (g_conv_tma) {
+    const cudaError_t e = ptyg::nn::conv3_tma(X, C1 ? X1 : nullptr, C0, C1, Bn, H, W, Wt, Co, C, out, bias, relu,
+                                              status, (cudaStream_t)stream);
+    if (e != cudaErrorNotSupported) return nn_check(e, "ptyg_nn_conv3 (TMA)");
+    cudaGetLastError();
+  }
   GemmArgs g = {};
   g.A = (const bf16*)X;
   g.A1 = (const bf16*)X1;

@@ -167,3 +167,46 @@ def test_training_steps_reduce_the_loss(torch_cuda):
     torch.cuda.synchronize()
     net.check_status()
     assert losses[-1] < 0.3 * losses[0], losses
+
+
+@pytest.mark.parametrize(
+    "B,H,W,C0,C1,Co",
+    [(2, 32, 32, 64, 32, 64), (1, 128, 128, 16, 0, 32), (3, 16, 16, 128, 128, 128), (2, 64, 64, 32, 0, 40),
+     (1, 32, 32, 256, 128, 256)],
+)
+@pytest.mark.parametrize("path", [1, 0])
+def test_conv3_tma_and_gather_paths_match_oracle(torch_cuda, B, H, W, C0, C1, Co, path):
+    """The TMA-fed convolution (path 1; the shapes here all take it) and the
+    cp.async gather (path 0) against the oracle: zero padding from the
+    out-of-bounds fill, the second input of a concatenation, output channels
+    beyond the last full tile, bf16 + bias + ReLU and f32 epilogues."""
+    torch = torch_cuda
+    from oracle import nn_oracle as N
+    from ptylab_gb300 import _native
+
+    lib = _native.require(0)
+    rng = np.random.default_rng(B * H + C0 + C1 + Co)
+    X0 = rng.standard_normal((B, H, W, C0))
+    X1 = rng.standard_normal((B, H, W, C1)) if C1 else None
+    w = rng.standard_normal((Co, 9, C0 + C1)) / np.sqrt(9 * (C0 + C1))
+    b = rng.standard_normal(Co).astype(np.float32)
+    xin = np.concatenate([N.bf16(X0), N.bf16(X1)], -1) if C1 else N.bf16(X0)
+    ref = N.conv3(xin, N.bf16(w), b)
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d0, dw = _bf(torch, X0), _bf(torch, w.reshape(Co, -1))
+    d1 = _bf(torch, X1) if C1 else None
+    db = torch.as_tensor(b).cuda()
+    _native.check(lib.ptyg_nn_conv3_path(path))
+    try:
+        f32 = torch.empty(B * H * W, Co, dtype=torch.float32, device="cuda")
+        _native.check(lib.ptyg_nn_conv3(d0.data_ptr(), d1.data_ptr() if C1 else None, C0, C1, B, H, W, dw.data_ptr(),
+                                        Co, f32.data_ptr(), None, db.data_ptr(), 0, st.data_ptr(), None))
+        o16 = torch.empty(B * H * W, Co, dtype=torch.bfloat16, device="cuda")
+        _native.check(lib.ptyg_nn_conv3(d0.data_ptr(), d1.data_ptr() if C1 else None, C0, C1, B, H, W, dw.data_ptr(),
+                                        Co, None, o16.data_ptr(), db.data_ptr(), 1, st.data_ptr(), None))
+        torch.cuda.synchronize()
+    finally:
+        lib.ptyg_nn_conv3_path(1)
+    assert int(st.item()) == 0
+    assert rel_err(f32.cpu().numpy().reshape(ref.shape), ref) < 1e-5
+    assert rel_err(o16.float().cpu().numpy().reshape(ref.shape), np.maximum(ref, 0)) < 5e-3
