@@ -384,7 +384,7 @@ PTYG_API int ptyg_nn_transpose(const void* in, void* out, int R, int C, void* st
 /* W [Co][9][Ci] -> Wf [Ci][9][Co] with the taps flipped (backward-data weights) */
 PTYG_API int ptyg_nn_flip_weights(const void* w, void* wf, int Co, int Ci, void* stream);
 PTYG_API int ptyg_nn_relu_bwd(const float* dy, const void* y, void* dpre, float* dpre_f32, int64_t n, void* stream);
-/* out[n] = sum_m d[m][n] (N divides 256); part: scratch of ceil(M / 1024) * N floats */
+/* out[n] = sum_m d[m][n] (N divides 256); part: scratch of ceil(M / 256) * N floats */
 PTYG_API int ptyg_nn_col_sum(const float* d, float* part, float* out, int M, int N, void* stream);
 PTYG_API int ptyg_nn_pool2(const void* x, void* y, int Bn, int H, int W, int C, void* stream);
 PTYG_API int ptyg_nn_pool2_bwd(const float* dy, float* dx, int Bn, int H, int W, int C, void* stream);

@@ -576,7 +576,20 @@ static cudaError_t launch_gemm(const GemmArgs& g, int amode, int splits, cudaStr
 // partials [splits][M][N] -> out[M][N] (fixed order)
 __global__ void reduce_splits_kernel(const float* part, float* out, size_t n, int splits) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (4 * i + 3 < n && (n & 3) == 0) {
+    // four outputs per thread, every split's load issued before the sums
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int z = 0; z < splits; ++z) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(part + (size_t)z * n) + i);
+      s.x += v.x;
+      s.y += v.y;
+      s.z += v.z;
+      s.w += v.w;
+    }
+    reinterpret_cast<float4*>(out)[i] = s;
+    return;
+  }
+  if ((n & 3) == 0 || i >= n) return;
   float s = 0.f;
   for (int z = 0; z < splits; ++z) s += part[(size_t)z * n + i];
   out[i] = s;
@@ -658,14 +671,21 @@ __global__ void relu_bwd_kernel(const float* dy, const bf16* y, bf16* dpre, floa
 // db[n] = sum_m d[m][n] in two fixed-order passes: block b sums rows
 // [b R, (b+1) R) column-wise with coalesced reads (consecutive threads read
 // consecutive columns of a row; N divides 256), then one pass over the blocks.
-constexpr int COLSUM_ROWS = 1024;
+constexpr int COLSUM_ROWS = 256;
 __global__ void col_sum_part_kernel(const float* d, float* part, int M, int N) {
   __shared__ float red[256];
   const int rpp = 256 / N;  // rows per pass
   const int c = threadIdx.x % N, r0 = threadIdx.x / N;
   const int m0 = blockIdx.x * COLSUM_ROWS, m1 = min(M, m0 + COLSUM_ROWS);
-  float s = 0.f;
-  for (int m = m0 + r0; m < m1; m += rpp) s += d[(size_t)m * N + c];
+  // four independent running sums keep four loads in flight per thread
+  float s4[4] = {0.f, 0.f, 0.f, 0.f};
+  int m = m0 + r0;
+  for (; m + 3 * rpp < m1; m += 4 * rpp) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s4[u] += d[(size_t)(m + u * rpp) * N + c];
+  }
+  for (int u = 0; m < m1; m += rpp, ++u) s4[u & 3] += d[(size_t)m * N + c];
+  const float s = (s4[0] + s4[1]) + (s4[2] + s4[3]);
   red[threadIdx.x] = s;
   __syncthreads();
   if (threadIdx.x < N) {
@@ -675,12 +695,19 @@ __global__ void col_sum_part_kernel(const float* d, float* part, int M, int N) {
   }
 }
 
+// one block per column: strided partial sums, then a fixed tree (FP64)
 __global__ void col_sum_final_kernel(const float* part, float* out, int nb, int N) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
+  __shared__ double red[256];
+  const int n = blockIdx.x;
   double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += (double)part[(size_t)b * N + n];
-  out[n] = (float)s;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += (double)part[(size_t)b * N + n];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = (float)red[0];
 }
 
 // 2x2 average pooling, NHWC
@@ -856,7 +883,7 @@ extern "C" int ptyg_nn_conv3(const void* X, const void* X1, int C0, int C1, int 
 }
 
 extern "C" int ptyg_nn_reduce_splits(const float* part, float* out, int64_t n, int splits, void* stream) {
-  reduce_splits_kernel<<<blocks(n), 256, 0, (cudaStream_t)stream>>>(part, out, (size_t)n, splits);
+  reduce_splits_kernel<<<blocks(n % 4 == 0 ? n / 4 : n), 256, 0, (cudaStream_t)stream>>>(part, out, (size_t)n, splits);
   return nn_check(cudaGetLastError(), "ptyg_nn_reduce_splits");
 }
 
@@ -896,7 +923,7 @@ extern "C" int ptyg_nn_col_sum(const float* d, float* part, float* out, int M, i
   cudaStream_t st = (cudaStream_t)stream;
   const int nb = (M + COLSUM_ROWS - 1) / COLSUM_ROWS;
   col_sum_part_kernel<<<nb, 256, 0, st>>>(d, part, M, N);
-  col_sum_final_kernel<<<(N + 255) / 256, 256, 0, st>>>(part, out, nb, N);
+  col_sum_final_kernel<<<N, 256, 0, st>>>(part, out, nb, N);
   return nn_check(cudaGetLastError(), "ptyg_nn_col_sum");
 }
 

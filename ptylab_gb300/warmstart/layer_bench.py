@@ -92,10 +92,19 @@ def network_bench(args):
         f = 2.0 * args.batch * side * side * co * k
         fwd += f
         bwd += f if name == "e1a" else 2 * f
-    net = WarmStartNet(seed=0)
     rng = np.random.default_rng(0)
     x = torch.as_tensor(rng.standard_normal((args.batch, args.size, args.size)).astype(np.float32)).cuda()
     dy = torch.as_tensor(rng.standard_normal((args.batch, args.size, args.size, 2)).astype(np.float32)).cuda()
+    for mode in ("eager", "CUDA graphs"):
+        net = WarmStartNet(seed=0)
+        if mode != "eager":
+            net.enable_graphs()
+        _time_passes(net, x, dy, fwd, bwd, args, mode)
+
+
+def _time_passes(net, x, dy, fwd, bwd, args, mode):
+    import torch
+
     for name, f, flop in (("forward", lambda: net.forward(x), fwd), ("backward", lambda: net.backward(dy), bwd)):
         for _ in range(3):
             f()
@@ -107,7 +116,7 @@ def network_bench(args):
         b.record()
         torch.cuda.synchronize()
         t = a.elapsed_time(b) / args.reps / 1e3
-        print(f"network {name} (batch {args.batch}, {args.size}x{args.size}): {t * 1e3:.3f} ms, "
+        print(f"network {name} ({mode}, batch {args.batch}, {args.size}x{args.size}): {t * 1e3:.3f} ms, "
               f"{flop / 1e9:.1f} GFLOP, {flop / t / 1e12:.1f} TFLOP/s")
     net.check_status()
 

@@ -92,6 +92,36 @@ class WarmStartNet:
         self.step = 0
         self._shape = None
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._graphs = None  # enable_graphs(): {(pass, shape): (CUDAGraph, static input, output)}
+
+    def enable_graphs(self, on=True):
+        """Replay forward() and backward() as CUDA graphs, one captured per
+        input shape (the ~60 forward and ~160 backward launches then cost
+        one graph launch each, not one Python call each).  The passes keep
+        their buffers across calls, so a captured graph stays valid until
+        the shape changes."""
+        self._graphs = {} if on else None
+
+    def _replay(self, kind, fn, arg):
+        """Run fn(arg) through the graph captured for (kind, arg's shape)."""
+        torch = _torch()
+        if self._shape is not None and tuple(arg.shape[:3]) != self._shape:
+            # a new batch shape reallocates every buffer the graphs point at
+            self._graphs.clear()
+        key = (kind, tuple(arg.shape))
+        entry = self._graphs.get(key)
+        if entry is None:
+            static = torch.empty_like(arg)
+            static.copy_(arg)
+            fn(static)  # eager run: allocates every buffer, sets kernel attributes
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                out = fn(static)
+            entry = self._graphs[key] = (graph, static, out)
+        graph, static, out = entry
+        static.copy_(arg)
+        graph.replay()
+        return out
 
     # ---------------------------------------------------------------- plumbing
     def _stream(self):
@@ -158,7 +188,7 @@ class WarmStartNet:
         self.a, self.gbuf = a, g
         self.x16 = torch.empty(B * H * W, dtype=bf, device=dev)
         self.col1 = torch.empty(B * H * W, FIRST_K, dtype=bf, device=dev)
-        self.colsum = torch.empty(-(-(B * H * W) // 1024) * 256, dtype=f32, device=dev)  # column-sum partials
+        self.colsum = torch.empty(-(-(B * H * W) // 256) * 256, dtype=f32, device=dev)  # column-sum partials
         self._shape = (B, H, W)
 
     # ---------------------------------------------------------------- forward
@@ -176,6 +206,11 @@ class WarmStartNet:
 
     def forward(self, x):
         """x: float32 tensor [B, H, W] (H, W multiples of 8) -> float32 [B, H, W, 2]."""
+        if self._graphs is not None:
+            return self._replay("forward", self._forward, x)
+        return self._forward(x)
+
+    def _forward(self, x):
         torch = _torch()
         B, H, W = x.shape
         self._alloc(B, H, W)
@@ -269,6 +304,12 @@ class WarmStartNet:
     def backward(self, dout):
         """dout: float32 [B, H, W, 2], the loss gradient w.r.t. forward()'s
         output; fills every parameter's .g."""
+        if self._graphs is not None:
+            self._replay("backward", self._backward, dout.contiguous())
+            return
+        self._backward(dout)
+
+    def _backward(self, dout):
         torch = _torch()
         B, H, W = self._shape
         M = B * H * W
