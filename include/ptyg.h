@@ -393,6 +393,14 @@ PTYG_API int ptyg_nn_up2_bwd(const float* dy, float* dx, int Bn, int H, int W, i
 PTYG_API int ptyg_nn_slice_add(const float* src, int ldsrc, int coff, float* dst, int C, int64_t M, int accumulate,
                                void* stream);
 PTYG_API int ptyg_nn_cast_bf16(const float* x, void* y, int64_t n, void* stream);
+/* The warm start's initial object: complex64 patches [n][Np][Np] added in
+ * order into acc [No][No] (complex64) with the window [Np][Np] at the corners
+ * positions [n][2] (row, column), each patch first rotated by the unit phase
+ * of sum conj(patch) acc window over its footprint (1 where that is zero);
+ * wsum [No][No] accumulates the window.  Corners outside [0, No - Np] are
+ * skipped.  acc and wsum start as the caller leaves them (normally zero). */
+PTYG_API int ptyg_stitch(const void* patches, const int32_t* positions, int n, int Np, int No, const float* window,
+                         void* acc, float* wsum, void* stream);
 PTYG_API int ptyg_nn_adam(float* p, const float* g, float* m, float* v, void* p16, int64_t n, float lr, float b1,
                           float b2, float eps, int step, float weight_decay, void* stream);
 

@@ -134,6 +134,7 @@ _SIGNATURES = {
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
     ],
     "ptyg_nn_conv3_path": [C.c_int],
+    "ptyg_stitch": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
     "ptyg_propagate_sets": [
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -970,6 +970,74 @@ extern "C" int ptyg_nn_adam(float* p, const float* g, float* m, float* v, void* 
   return nn_check(cudaGetLastError(), "ptyg_nn_adam");
 }
 
+// Phase-aligned windowed stitching of n complex patches (Np x Np) into an
+// No x No object, in order: each patch is rotated by the unit phase of its
+// windowed overlap with what is stitched so far, then added with the window.
+// Patch j depends on patches < j, so one CTA walks them: a block reduction
+// (FP64) for the overlap, then the windowed update of the patch's rows.
+__global__ void __launch_bounds__(1024) stitch_kernel(const float2* __restrict__ patches, const int* __restrict__ pos,
+                                                      int n, int Np, int No, const float* __restrict__ w, float2* acc,
+                                                      float* wsum) {
+  __shared__ double red[2][32];
+  __shared__ float2 rot_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int NN = Np * Np;
+  for (int j = 0; j < n; ++j) {
+    const int r = pos[2 * j], c = pos[2 * j + 1];
+    if (r < 0 || c < 0 || r > No - Np || c > No - Np) continue;  // uniform over the block
+    const float2* p = patches + (size_t)j * NN;
+    double ox = 0.0, oy = 0.0;
+    for (int i = tid; i < NN; i += blockDim.x) {
+      const int y = i / Np, x = i - (i / Np) * Np;
+      const float2 pv = p[i], a = acc[(size_t)(r + y) * No + c + x];
+      const double wv = w[i];
+      ox += wv * ((double)pv.x * a.x + (double)pv.y * a.y);  // conj(p) a w
+      oy += wv * ((double)pv.x * a.y - (double)pv.y * a.x);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ox += __shfl_xor_sync(0xffffffffu, ox, o);
+      oy += __shfl_xor_sync(0xffffffffu, oy, o);
+    }
+    if (lane == 0) {
+      red[0][warp] = ox;
+      red[1][warp] = oy;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double sx = 0.0, sy = 0.0;
+      for (int k = 0; k < nw; ++k) {
+        sx += red[0][k];
+        sy += red[1][k];
+      }
+      const double mag = sqrt(sx * sx + sy * sy);
+      rot_s = mag > 0.0 ? make_float2((float)(sx / mag), (float)(sy / mag)) : make_float2(1.f, 0.f);
+    }
+    __syncthreads();
+    const float2 rot = rot_s;
+    for (int i = tid; i < NN; i += blockDim.x) {
+      const int y = i / Np, x = i - (i / Np) * Np;
+      const size_t oi = (size_t)(r + y) * No + c + x;
+      const float2 pv = p[i];
+      const float wv = w[i];
+      const float2 q = make_float2(rot.x * pv.x - rot.y * pv.y, rot.x * pv.y + rot.y * pv.x);
+      acc[oi] = make_float2(acc[oi].x + q.x * wv, acc[oi].y + q.y * wv);
+      wsum[oi] += wv;
+    }
+    __syncthreads();  // this patch's writes before the next patch's overlap
+  }
+}
+
+extern "C" int ptyg_stitch(const void* patches, const int32_t* positions, int n, int Np, int No, const float* window,
+                           void* acc, float* wsum, void* stream) {
+  if (!patches || !positions || !window || !acc || !wsum || n < 0 || Np < 1 || No < Np)
+    return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_stitch: bad arguments");
+  if (n == 0) return PTYG_OK;
+  stitch_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>((const float2*)patches, positions, n, Np, No, window,
+                                                      (float2*)acc, wsum);
+  return nn_check(cudaGetLastError(), "ptyg_stitch");
+}
+
 static int ilog2_exact(int v) {
   int l = 0;
   while ((1 << l) < v) ++l;

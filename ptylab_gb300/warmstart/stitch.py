@@ -31,10 +31,21 @@ def blend_window(Np, radius_fraction=0.25):
     return np.exp(-0.5 * (r / 0.8) ** 2).astype(np.float32)
 
 
+def network_input_device(ptychogram, device):
+    """network_input on the GPU (the same standardised log(1 + I), float32):
+    the patterns go up once and are transformed where they land."""
+    torch = _torch()
+    x = torch.as_tensor(np.asarray(ptychogram, dtype=np.float32), device=device)
+    x = torch.log1p(torch.clamp(x, min=0))
+    mu = x.mean(dim=(-2, -1), keepdim=True)
+    sd = x.std(dim=(-2, -1), keepdim=True, unbiased=False) + 1e-6
+    return (x - mu) / sd
+
+
 def predict_patches(net, ptychogram, batch=64):
     """Complex patches [n, Np, Np] (device tensor) for every pattern."""
     torch = _torch()
-    x = torch.as_tensor(network_input(ptychogram), device=net.device)
+    x = network_input_device(ptychogram, net.device)
     out = []
     for i in range(0, x.shape[0], batch):
         y = net.forward(x[i : i + batch])
@@ -43,21 +54,24 @@ def predict_patches(net, ptychogram, batch=64):
 
 
 def stitch(patches, positions, No, window=None):
-    """Phase-aligned, windowed average of patches [n, Np, Np] at (row, col) corners."""
+    """Phase-aligned, windowed average of patches [n, Np, Np] at (row, col)
+    corners: the patches are added in order by one CTA of ``ptyg_stitch``
+    (each rotated onto the overlap with what is there), then divided by the
+    summed window."""
+    from .. import _native
+
     torch = _torch()
     n, Np, _ = patches.shape
     dev = patches.device
-    w = torch.as_tensor(blend_window(Np) if window is None else window, device=dev)
+    lib = _native.require(dev.index or 0)
+    w = torch.as_tensor(blend_window(Np) if window is None else window, device=dev).to(torch.float32).contiguous()
     acc = torch.zeros(No, No, dtype=torch.complex64, device=dev)
     wsum = torch.zeros(No, No, dtype=torch.float32, device=dev)
-    for j, (r, c) in enumerate(np.asarray(positions)):
-        p = patches[j]
-        a, ws = acc[r : r + Np, c : c + Np], wsum[r : r + Np, c : c + Np]
-        ov = torch.sum(torch.conj(p) * a * w)  # overlap with what is there (zero for the first patch)
-        mag = ov.abs()
-        rot = torch.where(mag > 0, ov / torch.clamp(mag, min=1e-30), torch.ones_like(ov))
-        acc[r : r + Np, c : c + Np] = a + rot * p * w
-        ws += w
+    pos = torch.as_tensor(np.ascontiguousarray(np.asarray(positions), dtype=np.int32), device=dev)
+    p = patches.to(torch.complex64).contiguous()
+    _native.check(lib.ptyg_stitch(p.data_ptr(), pos.data_ptr(), int(n), int(Np), int(No), w.data_ptr(),
+                                  acc.data_ptr(), wsum.data_ptr(), torch.cuda.current_stream(dev).cuda_stream),
+                  "ptyg_stitch")
     out = torch.ones(No, No, dtype=torch.complex64, device=dev)
     m = wsum > 1e-3 * float(wsum.max())
     out[m] = acc[m] / wsum[m]

@@ -100,8 +100,12 @@ def _physics_loss(pred, probe, I_meas):
 
 
 def train(net, data, steps, batch=16, lr=1e-3, lam_phys=0.5, seed=0, log=print, log_every=50):
-    """Adam steps on batches of one scan each; returns the loss history."""
+    """Adam steps on batches of one scan each; returns the loss history.  The
+    network's forward and backward passes run as CUDA graphs (bit-identical
+    to the eager passes; ``net.enable_graphs(False)`` turns them off)."""
     torch = _torch()
+    if net._graphs is None:
+        net.enable_graphs()
     rng = np.random.default_rng(seed)
     dev = net.device
     Np = data[0]["x"].shape[-1]
