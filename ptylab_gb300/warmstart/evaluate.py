@@ -175,6 +175,9 @@ def compare(net, spec=C4, threshold=1e-2, max_iters=200, seed=5, batch=64):
 
     d, p, rec, _, _ = c4_problem(spec)
     rec.object, rec.probe = obj0.copy(), prb0.copy()
+    # warm-up of the inference (graph capture for this batch shape, first
+    # launches), not timed, like the plain run's warm-up above
+    predict_object(net, d.ptychogram, rec.positions, spec.No, spec.Np, batch=batch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     warm_obj, setup = predict_object(net, d.ptychogram, rec.positions, spec.No, spec.Np, batch=batch)
