@@ -15,8 +15,9 @@
 // block of the CTA that owns those columns, and a column pass writes back into
 // the row owners' row buffers, so the 2D transpose never touches L2.  The
 // norm maxima are reduced with cluster-scope atomics into rank 0's shared
-// memory, and each position's measured intensities are prefetched one
-// position ahead with cp.async into a double buffer.
+// memory, and each position's measured intensities are prefetched with
+// cp.async into their buffer as soon as the previous position's projection
+// has read it.
 //
 // Work is split into warp tasks, one 1D transform of one mode each, so a CTA
 // runs K*L independent transforms per pass (K = nosm*npsm); everything that
@@ -28,7 +29,9 @@
 //      wave O_o*P_p [*chirp][*sign], forward row FFT -> work buffer
 //   B  stage the CTA's column block; tasks: forward column FFT; pixels:
 //      I_est, FP64 error partial, frac = sqrt(I_meas/(I_est+1e-10)); tasks:
-//      * frac / Np^2, inverse column FFT; write back
+//      * frac / Np^2, inverse column FFT; write back.  With one warp per
+//      column of the CTA (and a single-pass projection) the warp does all of
+//      this for its column, the intensities summed in registers
 //   C  tasks: inverse row FFT, [sign], [conj chirp], DELTA = eswUpdate - esw;
 //      pixels: object and probe steps (qNewton: whole-object max first)
 //   M  mqNewton: gradient norms; adaptive-momentum step over the whole object
@@ -40,6 +43,8 @@
 // instantiations are split over ptyg_engine.cu (ePIE / mPIE / qNewton) and
 // ptyg_engine_mq.cu (mqNewton) so they compile in parallel.
 #pragma once
+
+#include <type_traits>
 
 #include "ptyg_engine_dev.cuh"
 
@@ -488,7 +493,12 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
     // is the estimate of pixel i; the factor goes to sm.fr[i] times outScale.
     // Tables and the background are in the data layout, this CTA's block at
     // blk0 * NP.  Returns this thread's (FourierMask-weighted) error sum.
-    auto project = [&](auto Iest, float outScale) -> double {
+    // cols (a compile-time tag): warp w handles the E pixels of its own
+    // column w (pixel w * NP + 32 r + lane gets Iest(r)), else every thread
+    // strides over the CTA's LN pixels (pixel i gets Iest(i)).  The column
+    // form serves the fused pass B and only single-pass projections.
+    auto project = [&](auto Iest, float outScale, auto colsTag) -> double {
+      constexpr bool cols = decltype(colsTag)::value;
       const bool det = a.writeDetErr && s.detErr;
       const size_t tb = (size_t)blk0 * NP;
       float* bg = a.bgMode ? s.background + tb : nullptr;
@@ -521,10 +531,9 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
           bg[i] = b;
         }
       };
-      const bool twoPass = a.denoise || a.iconstraint == IC_FLUCTUATION;
+      const bool twoPass = !cols && (a.denoise || a.iconstraint == IC_FLUCTUATION);
       double dn = 0.0;
-      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-        float ie = Iest(i);
+      auto pixel = [&](int i, float ie) {
         if (bg) ie += bg[i];
         const float im = dat[i];
         const float d = fabsf(im - ie);
@@ -536,6 +545,12 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
         } else {
           finish(i, ie, im, d);
         }
+      };
+      if constexpr (cols) {
+#pragma unroll
+        for (int r = 0; r < E; ++r) pixel(warp * NP + 32 * r + lane, Iest(r));
+      } else {
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) pixel(i, Iest(i));
       }
       if (twoPass) {
         if (a.denoise) {
@@ -563,7 +578,66 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
     };
 
     double err = 0.0;
-    if (!asp) {
+    if (!asp && nw == L && !(a.denoise || a.iconstraint == IC_FLUCTUATION)) {
+      // ---------------- B, fused: warp w owns column w of every mode, so it
+      // transforms the column's K modes, sums their intensities in
+      // registers, projects its own pixels and transforms back, with no
+      // block-wide barrier in between (the tile column and its factors are
+      // written and read by this warp only)
+      const int c = warp;
+      float ie[E];
+#pragma unroll
+      for (int r = 0; r < E; ++r) ie[r] = 0.f;
+      auto colLoad = [&](int k, float2(&v)[E]) {
+#pragma unroll
+        for (int j = 0; j < E; ++j) v[j] = sm.tile[tix<L>(k * NP + lane + 32 * j, c)];
+      };
+      auto colStore = [&](int k, const float2(&v)[E]) {
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          sm.tile[tix<L>(k * NP + 32 * r + lane, c)] = v[r];
+          ie[r] += cabs2(v[r]);
+        }
+      };
+      int k = 0;
+      for (; k + 1 < K; k += 2) {
+        float2 v[2][E];
+        colLoad(k, v[0]);
+        colLoad(k + 1, v[1]);
+        F.template fwdm<2>(v);
+        __syncwarp();
+        colStore(k, v[0]);
+        colStore(k + 1, v[1]);
+      }
+      if (k < K) {
+        float2 v[E];
+        colLoad(k, v);
+        F.fwd(v);
+        __syncwarp();
+        colStore(k, v);
+      }
+      err = project([&](int r) { return ie[r] * inv2; }, inv2, std::true_type{});
+      __syncwarp();
+      auto invLoad = [&](int kk, float2(&v)[E]) {
+#pragma unroll
+        for (int r = 0; r < E; ++r)
+          v[r] = cscale(sm.tile[tix<L>(kk * NP + 32 * r + lane, c)], sm.fr[c * NP + 32 * r + lane]);
+      };
+      for (k = 0; k + 1 < K; k += 2) {
+        float2 v[2][E];
+        invLoad(k, v[0]);
+        invLoad(k + 1, v[1]);
+        F.template invm<2>(v);
+        scatter_column<E, L>(sm.rows, v[0], k, sx0 + c);
+        scatter_column<E, L>(sm.rows, v[1], k + 1, sx0 + c);
+      }
+      if (k < K) {
+        float2 v[E];
+        invLoad(k, v);
+        F.inv(v);
+        scatter_column<E, L>(sm.rows, v, k, sx0 + c);
+      }
+    } else if (!asp) {
       // ---------------- B: Fourier-plane intensity projection (BaseEngine.py:870-1012)
       fft_tasks<E, false>(
           F, K * L,
@@ -585,7 +659,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
             for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[tix<L>(k * NP + sy, c)]);
             return ie * inv2;
           },
-          inv2);
+          inv2, std::false_type{});
       __syncthreads();
       fft_tasks<E, true>(
           F, K * L,
@@ -619,7 +693,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
             for (int k = 0; k < K; ++k) ie += cabs2(sm.rows[k * LN + i]);
             return ie;
           },
-          1.f);
+          1.f, std::false_type{});
       __syncthreads();
       fft_tasks<E, false>(
           F, K * L,
