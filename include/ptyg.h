@@ -152,12 +152,14 @@ typedef struct ptyg_geometry {
                           1: most positions per second over many scans (16
                           rows per CTA: fewer CTAs per scan, more scans at once) */
   int32_t nlambda;     /* wavelengths (reconstruction.nlambda; 0 reads as 1).  Above
-                          1: ePIE only, object (nlambda, nosm, ...) and probe
-                          (nlambda, npsm, ...) wavelength-major, exit waves
-                          O_(l,o) P_(l,p) of each wavelength l, the ASP table
-                          one per wavelength (polychromeASP, Operators.py:458-505),
-                          and the object and probe steps summed over the
-                          wavelengths (ePIE.py:128-160) */
+                          1 (ePIE, mPIE, qNewton): object (nlambda, nosm, ...)
+                          and probe (nlambda, npsm, ...) wavelength-major, exit
+                          waves O_(l,o) P_(l,p) of each wavelength l, the ASP
+                          table one per wavelength (polychromeASP,
+                          Operators.py:458-505); ePIE and qNewton sum their
+                          steps over the wavelengths (ePIE.py:128-160,
+                          qNewton.py:108-140), mPIE keeps them per wavelength
+                          (mPIE.py:226-270) */
   int32_t threads;     /* threads per CTA, a multiple of 32 in [128, 512]
                           (mqNewton: at most 256); 0 = one warp per transform
                           task of a pass, at most 16 warps.  With 256 threads

@@ -28,6 +28,7 @@ bool engine_shape_supported(int Np, int cluster) {
 }
 
 cudaError_t engine_max_clusters(int Np, int engine, int nlambda, int cluster, int threads, size_t smem, int* out) {
+  // (the several-wavelength instantiation serves ePIE, mPIE and qNewton)
   if (engine == ENG_MQNEWTON) return engine_max_clusters_mq(Np, cluster, threads, smem, out);
   if (nlambda > 1) return engine_max_clusters_poly(Np, cluster, threads, smem, out);
   return engine_max_clusters_t<VAR_STD>(Np, cluster, threads, smem, out);

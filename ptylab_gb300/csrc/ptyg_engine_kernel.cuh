@@ -782,37 +782,51 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
               gP[o] = sqrtf(q) / (q + a.regP);  // qNewton.py:131-136 (1/Omax applied later)
           }
         }
-        // per-wavelength probe mode p; with several wavelengths (ePIE) object
-        // mode o pairs with the probe of wavelength o / nosmW, and the object
-        // and probe steps sum over the wavelengths (ePIE.py:128-160: axes 0,
-        // 2, 3 and 0, 1, 3), every wavelength's copy taking the same step
+        // per-wavelength probe mode p; with several wavelengths object mode
+        // o pairs with the probe of wavelength o / nosmW.  ePIE and qNewton
+        // sum their steps over the wavelengths (ePIE.py:128-160, qNewton.py
+        // :108-140: axes 0, 2, 3 and 0, 1, 3) and give every wavelength's
+        // copy the same step; mPIE sums over the probe modes (object) and
+        // the object modes (probe) of each wavelength only (mPIE.py:226-270:
+        // axis 2 and axis 1).
+        auto gObj = [&](float qp) {  // the object step's weight for a probe mode of intensity qp
+          if (eng == ENG_EPIE) return invPmax2;  // ePIE.py:138-140
+          if (eng == ENG_MPIE) {
+            float g = 1.f / (a.alphaO * pmax2 + (1.f - a.alphaO) * qp);  // mPIE.py:246-248
+            if (a.fpm) g *= sqrtf(qp) * invPmax2;                         // mPIE.py:237-243
+            return g;
+          }
+          return sqrtf(qp) * invPmax1 / (qp + a.regO);  // qNewton.py:113-119
+        };
+        const bool perLambda = nl > 1 && eng == ENG_MPIE;
         for (int p = 0; p < npsmW; ++p) {
           const float2 P = sm.probe[p * pst + i];
-          const float q = cabs2(P);
-          float gO;
-          if (eng == ENG_EPIE) {
-            gO = invPmax2;  // ePIE.py:138-140
-          } else if (eng == ENG_MPIE) {
-            gO = 1.f / (a.alphaO * pmax2 + (1.f - a.alphaO) * q);  // mPIE.py:246-248
-            if (a.fpm) gO *= sqrtf(q) * invPmax2;                    // mPIE.py:237-243
-          } else {
-            gO = sqrtf(q) * invPmax1 / (q + a.regO);  // qNewton.py:113-119
-          }
+          const float gO = gObj(cabs2(P));
           float2 accP = make_float2(0.f, 0.f);
 #pragma unroll
           for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
             if (o < nosm) {
-              const float2 Po = nl == 1 ? P : sm.probe[((o / nosmW) * npsmW + p) * pst + i];
+              float2 Po = P;
+              float gOo = gO;
+              if (nl > 1) {
+                Po = sm.probe[((o / nosmW) * npsmW + p) * pst + i];
+                gOo = gObj(cabs2(Po));
+              }
               const float2 d = sm.rows[(o * npsmW + p) * LN + i];
-              accO[o] = cadd(accO[o], cscale(cmulc(Po, d), gO));
+              accO[o] = cadd(accO[o], cscale(cmulc(Po, d), gOo));
               accP = cadd(accP, cscale(cmulc(O[o], d), gP[o]));
+              if (perLambda && o % nosmW == nosmW - 1) {
+                // the last object mode of wavelength o / nosmW: its probe step
+                sm.probe[((o / nosmW) * npsmW + p) * pst + i] = cadd(Po, cscale(accP, stepP));
+                accP = make_float2(0.f, 0.f);
+              }
             }
           }
           if (qn) {
-            sm.U[p * LN + i] = accP;
+            sm.U[p * LN + i] = accP;  // several wavelengths: summed over them
           } else if (nl == 1) {
             sm.probe[p * pst + i] = cadd(P, cscale(accP, stepP));
-          } else {
+          } else if (!perLambda) {
             for (int w = 0; w < nl; ++w) {
               float2* Pw = sm.probe + (w * npsmW + p) * pst + i;
               *Pw = cadd(*Pw, cscale(accP, stepP));
@@ -831,7 +845,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
         for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
           if (o < nosm) {
             float2 u = accO[o];
-            if (nl > 1) {
+            if (nl > 1 && !perLambda) {
               u = make_float2(0.f, 0.f);
 #pragma unroll
               for (int o2 = 0; o2 < MAX_OBJECT_MODES; ++o2)
@@ -890,9 +904,12 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
       cluster_sync(C);  // every contribution to the whole-object max (and mqNewton's partial sums) is in
       const float scale = a.betaP / slot_value(red, RED_OMAXW);
       if (!mq) {
+        // several wavelengths: every wavelength's probe mode p takes the
+        // numerator summed over the wavelengths, U[p % npsmW]
         for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
           const int p = i / LN, rem = i - (i / LN) * LN;
-          sm.probe[p * pst + rem] = cadd(sm.probe[p * pst + rem], cscale(sm.U[i], scale));
+          const int pu = nl == 1 ? p : p % npsmW;
+          sm.probe[p * pst + rem] = cadd(sm.probe[p * pst + rem], cscale(sm.U[pu * LN + rem], scale));
         }
       } else {
         // ---------------- M: adaptive momentum (mqNewton.py:142-224) after every

@@ -359,6 +359,9 @@ REG_CONFIGS = {
 }
 
 SCAN_CONFIGS = {
+    # several wavelengths (tests/regression/test_engine_regression.py:78-80 spectral density)
+    "qnewton_polychrome": dict(engine="qNewton", propagator="polychromeASP", modes=(3, 1, 2, 1), iters=3),
+    "mpie_polychrome": dict(engine="mPIE", propagator="polychromeASP", modes=(2, 2, 1, 1), iters=3, order="random"),
     "epie_random": dict(engine="ePIE", order="random", iters=4, keep_detector_error=True),
     "epie_fftshift": dict(engine="ePIE", order="random", fftshift=True, iters=3),
     "epie_fresnel": dict(engine="ePIE", propagator="Fresnel", iters=3),
