@@ -57,6 +57,11 @@ PTYG_DEV double warp_tree_sum(double v) {
   for (int o = 1; o < 32; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+PTYG_DEV float warp_tree_sumf(float v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
 
 // Sum of v[0, n), n a power of two of at most 128, as the balanced binary tree
 // over index order, on every lane.  The tree is fixed by n alone, so n values

@@ -750,12 +750,13 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
     // mqNewton sums over the patch: |objectBuffer - object|^2, and with
     // d = probeBuffer - probe and the probe numerator U: |d|^2, Re(conj(d) U),
     // |U|^2, from which |probeBuffer - (probe + U/Omax)|^2 follows once Omax is
-    // known.  A pixel's terms are exact double products summed over the modes;
-    // a warp sums its 32-pixel row segment in a fixed tree, and the segments
-    // (in sm.tile, free in this pass) are summed in the balanced tree over
-    // segment order, per CTA here and over the cluster in pass M: the same
-    // tree for every CTA shape, so a batched launch gives a single-scan
-    // launch's bits.
+    // known.  A pixel's terms are FP32 with explicit rounding, summed over
+    // the modes in order; a warp sums its 32-pixel row segment in a fixed
+    // FP32 tree, and the segment sums (FP64, in sm.tile, free in this pass)
+    // in the balanced tree over segment order, per CTA here and over the
+    // cluster in pass M: the same tree for every CTA shape, so a batched
+    // launch gives a single-scan launch's bits.  (FP64 per pixel would cost
+    // more than the rest of the pass on this GPU's FP64 rate.)
     const int nseg = LN / 32;
     double* segSum = reinterpret_cast<double*>(sm.tile);  // [4][nseg]
     {
@@ -767,7 +768,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
       for (int i = threadIdx.x; i < LN; i += blockDim.x) {
         float2 O[MAX_OBJECT_MODES], accO[MAX_OBJECT_MODES];
         float gP[MAX_OBJECT_MODES];
-        double tgO = 0.0, tdd = 0.0, tdu = 0.0, tuu = 0.0;
+        float tgO = 0.f, tdd = 0.f, tdu = 0.f, tuu = 0.f;
 #pragma unroll
         for (int o = 0; o < MAX_OBJECT_MODES; ++o) {
           if (o < nosm) {
@@ -834,9 +835,9 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
           }
           if (mq) {
             const float2 d = csub(s.probeBuffer[(size_t)p * NP * NP + (size_t)line0 * NP + i], P);
-            tdd += (double)d.x * d.x + (double)d.y * d.y;
-            tdu += (double)d.x * accP.x + (double)d.y * accP.y;
-            tuu += (double)accP.x * accP.x + (double)accP.y * accP.y;
+            tdd = __fadd_rn(tdd, __fmaf_rn(d.x, d.x, __fmul_rn(d.y, d.y)));
+            tdu = __fadd_rn(tdu, __fmaf_rn(d.x, accP.x, __fmul_rn(d.y, accP.y)));
+            tuu = __fadd_rn(tuu, __fmaf_rn(accP.x, accP.x, __fmul_rn(accP.y, accP.y)));
           }
         }
         const int l = i / NP, x = i - (i / NP) * NP;
@@ -861,17 +862,18 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
               // it is the patch as it was before this step; kept for pass M
               const float2 g = csub(O[o], On);
               sm.obj[o * LN + i] = g;
-              tgO += (double)g.x * g.x + (double)g.y * g.y;
+              tgO = __fadd_rn(tgO, __fmaf_rn(g.x, g.x, __fmul_rn(g.y, g.y)));
             }
           }
         }
         if (mq) {
           // warp-uniform: LN and blockDim are multiples of 32
-          tgO = warp_tree_sum(tgO);
-          tdd = warp_tree_sum(tdd);
-          tdu = warp_tree_sum(tdu);
-          tuu = warp_tree_sum(tuu);
-          if (lane < 4) segSum[lane * nseg + (i >> 5)] = lane == 0 ? tgO : lane == 1 ? tdd : lane == 2 ? tdu : tuu;
+          tgO = warp_tree_sumf(tgO);
+          tdd = warp_tree_sumf(tdd);
+          tdu = warp_tree_sumf(tdu);
+          tuu = warp_tree_sumf(tuu);
+          if (lane < 4)
+            segSum[lane * nseg + (i >> 5)] = (double)(lane == 0 ? tgO : lane == 1 ? tdd : lane == 2 ? tdu : tuu);
         }
         if (qn) {
           omaxPatch = fmaxf(omaxPatch, onew);
