@@ -2,7 +2,11 @@
 object error, plain against warm-started, on the evaluation scan.
 
     python -m ptylab_gb300.warmstart.benchmark [--scans 60] [--steps 3000]
-        [--max-iters 1200] [--weights out.npz]
+        [--max-iters 1200] [--weights out.npz] [--photons 1e6]
+
+--photons sets the dose of the evaluation scan only (the training scans keep
+theirs), e.g. 1e9 to see where the error of plain mPIE levels off without
+the noise of the configured 1e6.
 
 Prints one JSON line: training time, the warm start's own object error, and
 for both runs the GPU seconds to errors 1e-1, 3e-2 and 1e-2 (null where the
@@ -14,6 +18,7 @@ from __future__ import annotations
 import argparse
 import json
 import time
+from dataclasses import replace
 
 
 def main():
@@ -31,6 +36,7 @@ def main():
     ap.add_argument("--lam-phys", type=float, default=0.1)
     ap.add_argument("--max-iters", type=int, default=1200)
     ap.add_argument("--weights", default=None, help="save the trained weights here (.npz)")
+    ap.add_argument("--photons", type=float, default=None, help="photons per pattern of the evaluation scan")
     args = ap.parse_args()
     t0 = time.perf_counter()
     data = TR.make_training_set(args.scans, log=None)
@@ -43,9 +49,10 @@ def main():
     t_train = time.perf_counter() - t0
     if args.weights:
         TR.save_weights(net, args.weights)
-    plain, warm, e0 = EV.compare(net, max_iters=args.max_iters)
+    spec = EV.C4 if args.photons is None else replace(EV.C4, photons=args.photons)
+    plain, warm, e0 = EV.compare(net, spec=spec, max_iters=args.max_iters)
     out = {
-        "evaluation": "1024-position Fermat scan, Np=128, No=640, npsm=2, 1e6 photons (synthetic, seeded)",
+        "evaluation": f"1024-position Fermat scan, Np=128, No=640, npsm=2, {spec.photons:g} photons (synthetic, seeded)",
         "training": {"scans": args.scans, "patterns": args.scans * 100, "steps": args.steps, "batch": args.batch,
                      "data_seconds": round(t_data, 2), "train_seconds": round(t_train, 2),
                      "final_supervised_loss": float(sum(h[0] for h in hist[-100:]) / 100)},
