@@ -101,3 +101,38 @@ def test_ctypes_structs_match_the_header(cname, pyname):
         kind = {C.c_int32: "c_int", C.c_int: "c_int", C.c_float: "c_float", C.c_double: "c_double"}.get(t, "c_void_p")
         got.append((n, kind))
     assert got == want
+
+
+def test_new_entry_points_reject_bad_arguments_before_touching_a_device(lib):
+    """Argument checks of the wavelength-set propagators, the several-
+    wavelength and CTA-size plan fields, the stitcher and the convolution
+    path switch run on the host: the errors come back without a GPU."""
+    import ctypes as C
+
+    from ptylab_gb300 import _native
+
+    dummy = C.c_void_p(16)
+    # nsets must divide the batch; SCALED_ASP takes one table set
+    assert lib.ptyg_propagate_sets(3, 0, 64, 4, 3, dummy, dummy, dummy, dummy, None, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_propagate_sets(4, 0, 64, 4, 2, dummy, dummy, dummy, dummy, None, None) == _native.PTYG_ERR_INVALID
+    # a propagator of ptyg_propagate is not a set propagator, and the tables are required
+    assert lib.ptyg_propagate_sets(0, 0, 64, 4, 1, dummy, dummy, dummy, dummy, None, None) == _native.PTYG_ERR_UNSUPPORTED
+    assert lib.ptyg_propagate_sets(5, 0, 64, 4, 1, dummy, dummy, dummy, None, None, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_propagate_sets(6, 0, 48, 4, 1, dummy, dummy, dummy, dummy, None, None) == _native.PTYG_ERR_UNSUPPORTED
+    # several wavelengths: not with mqNewton; CTA sizes: multiples of 32 in range
+    plan = C.c_void_p()
+    g = _native.Geometry(Np=64, No=128, nosm=1, npsm=1, nslice=1, num_frames=4, num_scans=1,
+                         engine=_native.ENGINES["mqNewton"], nlambda=2)
+    assert lib.ptyg_plan_create(C.byref(g), C.byref(plan)) == _native.PTYG_ERR_UNSUPPORTED
+    assert b"wavelengths" in lib.ptyg_last_error()
+    for threads in (100, 64, 1024):
+        g = _native.Geometry(Np=64, No=128, nosm=1, npsm=1, nslice=1, num_frames=4, num_scans=1,
+                             engine=_native.ENGINES["ePIE"], threads=threads)
+        assert lib.ptyg_plan_create(C.byref(g), C.byref(plan)) == _native.PTYG_ERR_INVALID
+    g = _native.Geometry(Np=64, No=128, nosm=1, npsm=1, nslice=1, num_frames=4, num_scans=1,
+                         engine=_native.ENGINES["ePIE"], probe_in_smem=3)
+    assert lib.ptyg_plan_create(C.byref(g), C.byref(plan)) == _native.PTYG_ERR_INVALID
+    # the stitcher needs its buffers and No >= Np
+    assert lib.ptyg_stitch(None, dummy, 1, 32, 64, dummy, dummy, dummy, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_stitch(dummy, dummy, 1, 64, 32, dummy, dummy, dummy, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_nn_conv3_path(1) == 0
