@@ -1,8 +1,8 @@
 """Measurement container, mirroring PtyLab's ``ExperimentalData``
 (PtyLab/ExperimentalData/ExperimentalData.py:21-288) for the fields the
-reconstruction loop reads.  HDF5 loading is not part of this package: assign
-the fields (or pass PtyLab's own ExperimentalData to the engines) and call
-``_setData()``.
+reconstruction loop reads.  ``loadData`` reads PtyLab's HDF5 measurement
+files through ``ptylab_gb300.io`` (no h5py or PyTables needed); the fields
+can also be assigned directly, followed by ``_setData()``.
 """
 
 from __future__ import annotations
@@ -37,7 +37,13 @@ class ExperimentalData:
             raise ValueError('operationMode is not properly set, choose "CPM" or "FPM"')
 
     def loadData(self, filename=None):
-        """Only the in-memory stub dataset (ExperimentalData.py:101-115) is supported."""
+        """Load a measurement file (ExperimentalData.py:86-149): the stub
+        ``test:nodata``, or an .hdf5/.h5/.mat (HDF5-based) file holding the
+        mode's required fields and any of its optional ones."""
+        import os
+
+        from .io import readHdf5
+
         if str(filename) == "test:nodata":
             self.filename = filename
             self.ptychogram = np.zeros((1, 16, 16), dtype=np.float32)
@@ -51,9 +57,42 @@ class ExperimentalData:
             self.emptyBeam = None
             self._setData()
             return
-        raise NotImplementedError(
-            "HDF5 loading is outside this package; load with PtyLab or assign the fields and call _setData()"
-        )
+        if not os.path.exists(filename) and str(filename).startswith("example:"):
+            raise FileNotFoundError(
+                f"{filename}: PtyLab's example datasets are downloaded files that this package does not ship"
+            )
+        self.filename = filename
+        readHdf5.checkDataFields(self.filename, self.requiredFields)
+        measurementDict = readHdf5.loadInputData(self.filename, self.requiredFields, self.optionalFields)
+        for a in measurementDict.keys():
+            attribute = str(a)
+            if not isinstance(getattr(type(self), attribute, None), property):
+                setattr(self, attribute, measurementDict[a])
+            self.logger.debug("Setting %s", a)
+        self._setData()
+        # last: the orientation can change the ptychogram itself
+        self.setOrientation(readHdf5.getOrientation(self.filename))
+
+    def setOrientation(self, orientation, force_contiguous=True):
+        """Flip/transpose the frames to the ptypy orientation convention
+        (ExperimentalData.py:192-232): 0 none, 1 columns reversed, 2 rows
+        reversed, 3 both, 4 transposed, 5-7 transposed then reversed as 1-3."""
+        if orientation is None:
+            return
+        if not isinstance(orientation, int):
+            raise TypeError("Orientation value is not valid.")
+        if orientation == 0:
+            return
+        if orientation < 0 or orientation > 7:
+            raise ValueError(f"Orientation {orientation} is not implemented")
+        if orientation >= 4:
+            self.ptychogram = np.transpose(self.ptychogram, (0, 2, 1))
+        if orientation in (1, 3, 5, 7):
+            self.ptychogram = np.flip(self.ptychogram, axis=-1)
+        if orientation in (2, 3, 6, 7):
+            self.ptychogram = np.flip(self.ptychogram, axis=-2)
+        if force_contiguous:
+            self.ptychogram = np.ascontiguousarray(self.ptychogram)
 
     def _setData(self):
         """Derived detector quantities (ExperimentalData.py:234-250)."""

@@ -162,6 +162,11 @@ class Reconstruction(object):
         if type_of_init is not None:
             self.initialObject = type_of_init
         self.shape_O = (self.nlambda, self.nosm, 1, self.nslice, self.No, self.No)
+        if self.initialObject == "recon":
+            # Reconstruction.py:370-372 reads the object from the file named
+            # by initialProbe_filename
+            self.initialGuessObject = self.loadResults(self.initialProbe_filename, datatype="object")
+            return
         self.initialGuessObject = initialProbeOrObject(self.shape_O, self.initialObject, self, self.logger).astype(
             np.complex64
         )
@@ -170,6 +175,9 @@ class Reconstruction(object):
         if self.data.entrancePupilDiameter is None:
             self.data.entrancePupilDiameter = self.Lp / 3
         self.shape_P = (self.nlambda, 1, self.npsm, self.nslice, int(self.Np), int(self.Np))
+        if self.initialProbe == "recon":
+            self.initialGuessProbe = self.loadResults(self.initialProbe_filename, datatype="probe")
+            return
         self.initialGuessProbe = initialProbeOrObject(self.shape_P, self.initialProbe, self).astype(np.complex64)
 
     def initializeObjectMomentum(self):
@@ -177,6 +185,107 @@ class Reconstruction(object):
 
     def initializeProbeMomentum(self):
         self.probeMomentum = np.zeros_like(self.initialGuessProbe)
+
+    # ------------------------------------------------------------ result files
+    @staticmethod
+    def loadResults(fileName, datatype="probe"):
+        """One array of a result file (Reconstruction.py:377-384)."""
+        from .io import hdf5
+
+        with hdf5.File(fileName, "r") as archive:
+            data = np.copy(np.array(archive[datatype]))
+        return data
+
+    def load_object(self, filename):
+        """The object of an earlier reconstruction, cut to ``shape_O``
+        (Reconstruction.py:420-450)."""
+        from .io import hdf5
+
+        with hdf5.File(filename, "r") as archive:
+            obj = np.array(archive["object"])
+            stored = obj.shape
+        obj = obj[tuple(slice(0, n) for n in self.shape_O)]
+        if obj.shape != tuple(self.shape_O):
+            raise RuntimeError(
+                f"Shape of saved probe cannot be extended to shape of required probe. File: {stored}. Need: {self.shape_O}"
+            )
+        self.object = obj
+
+    def load_probe(self, filename, expand_npsm=False, center_phase=False):
+        """The probe of an earlier reconstruction, its centre cut to
+        ``shape_P`` (Reconstruction.py:452-483)."""
+        from .io import hdf5
+
+        if center_phase:
+            raise NotImplementedError("center_phase needs scikit-image's phase_cross_correlation")
+        with hdf5.File(filename, "r") as archive:
+            probe = np.array(archive["probe"])
+        n_read = probe.shape[-1]
+        Np = int(self.Np)
+        ss = slice(max(n_read // 2 - Np // 2, 0), min(max(n_read // 2 - Np // 2 + Np, 0), n_read))
+        stored = probe.shape
+        probe = probe[: self.nlambda, :1, : self.npsm, : self.nslice, ss, ss]
+        if probe.shape != tuple(self.shape_P):
+            raise RuntimeError(
+                f"Shape of saved probe cannot be extended to shape of required probe. File: {stored}. Need: {self.shape_P}"
+            )
+        self.probe = probe
+
+    def load(self, filename):
+        """The arrays ``saveResults`` wrote (Reconstruction.py:495-508)."""
+        from .io import hdf5
+
+        with hdf5.File(filename, "r") as archive:
+            for key in ("probe", "object", "error", "wavelength", "dxp", "purityProbe", "purityObject", "zo"):
+                setattr(self, key, np.array(archive[key]))
+            if "theta" in archive.keys():
+                self.theta = np.array(archive["theta"])
+
+    def saveResults(self, fileName="recent", type="all", squeeze=False):
+        """Write the reconstruction as HDF5 with the reference's dataset names
+        and types (Reconstruction.py:510-576)."""
+        from .io import hdf5
+
+        allowed_save_types = ["all", "object", "probe", "probe_stack"]
+        if type not in allowed_save_types:
+            raise NotImplementedError(f"Only {allowed_save_types} are allowed keywords for type")
+        squeezefun = np.squeeze if squeeze else (lambda x: x)
+        host = lambda x: x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
+        if type == "all":
+            probe, obj = host(self.probe), host(self.object)
+            if self.data.operationMode == "CPM":
+                with hdf5.File(fileName, "w") as hf:
+                    hf.create_dataset("probe", data=probe, dtype="complex64")
+                    hf.create_dataset("object", data=obj, dtype="complex64")
+                    hf.create_dataset("error", data=np.asarray(self.error), dtype="f")
+                    hf.create_dataset("zo", data=self._zo, dtype="f")
+                    hf.create_dataset("wavelength", data=self.wavelength, dtype="f")
+                    hf.create_dataset("dxp", data=self.dxp, dtype="f")
+                    hf.create_dataset("purityProbe", data=self.purityProbe, dtype="f")
+                    hf.create_dataset("purityObject", data=self.purityObject, dtype="f")
+                    hf.create_dataset("I object", data=abs(obj), dtype="f")
+                    hf.create_dataset("I probe", data=abs(probe), dtype="f")
+                    hf.create_dataset("encoder_corrected", data=host(self.encoder_corrected))
+                    if getattr(self, "theta", None) is not None:
+                        hf.create_dataset("theta", data=self.theta, dtype="f")
+            if self.data.operationMode == "FPM":
+                with hdf5.File(fileName, "w") as hf:
+                    hf.create_dataset("probe", data=probe, dtype="complex64")
+                    hf.create_dataset("object", data=obj, dtype="complex64")
+                    hf.create_dataset("error", data=np.asarray(self.error), dtype="f")
+                    hf.create_dataset("zled", data=self.zled, dtype="f")
+                    hf.create_dataset("wavelength", data=self.wavelength, dtype="f")
+                    hf.create_dataset("dxp", data=self.dxp, dtype="f")
+        elif type == "probe":
+            with hdf5.File(fileName, "w") as hf:
+                hf.create_dataset("probe", data=squeezefun(host(self.probe)), dtype="complex64")
+        elif type == "object":
+            with hdf5.File(fileName, "w") as hf:
+                hf.create_dataset("object", data=squeezefun(host(self.object)), dtype="complex64")
+        elif type == "probe_stack":
+            with hdf5.File(str(fileName) + "_probe_stack.hdf5", "w") as hf:
+                hf.create_dataset("probe_stack", data=host(self.probe_stack.get()), dtype="complex64")
+        self.logger.info("The reconstruction results (%s) have been saved", type)
 
     # ------------------------------------------------------------ geometry
     @property
