@@ -147,6 +147,14 @@ class FPMSpec:
     photons: float = 5e4
     sigma_px: float = 4.0
     seed: int = 20240607
+    # misalignment of the LED array the images are made with; the returned
+    # encoder stays the nominal grid (what an illumination calibration fixes)
+    led_rotation_deg: float = 0.0
+    led_shift: tuple = (0.0, 0.0)
+    true_NA: float | None = None
+    # object contrast: amplitude 1 - amp_contrast * (1 - field), phase phase_scale * field
+    amp_contrast: float = 0.5
+    phase_scale: float = np.pi
 
 
 def simulate_fpm(spec: FPMSpec):
@@ -157,16 +165,22 @@ def simulate_fpm(spec: FPMSpec):
     c = (np.arange(spec.grid) - (spec.grid - 1) / 2) * spec.pitch
     yy, xx = np.meshgrid(c, c, indexing="ij")
     encoder = np.stack([yy.ravel(), xx.ravel()], axis=1)
-    amp = 0.5 + 0.5 * gaussian_random_field(rng, No, spec.sigma_px)
-    phase = np.pi * gaussian_random_field(rng, No, spec.sigma_px)
+    amp = 1.0 - spec.amp_contrast + spec.amp_contrast * gaussian_random_field(rng, No, spec.sigma_px)
+    phase = spec.phase_scale * gaussian_random_field(rng, No, spec.sigma_px)
     obj = amp * np.exp(1j * phase)
     spectrum = np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(obj), norm="ortho"))
-    pupil_d = 2 * dxp**2 * Np * spec.NA / spec.wavelength
+    NA = spec.NA if spec.true_NA is None else spec.true_NA
+    pupil_d = 2 * dxp**2 * Np * NA / spec.wavelength
     x = np.linspace(-Np / 2, Np / 2, Np) * dxp
     X, Y = np.meshgrid(x, x)
     pupil = (X**2 + Y**2) < (pupil_d / 2) ** 2
     conv = -(1 / spec.wavelength) * dxp * Np
-    shift = np.round(conv * encoder / np.sqrt(encoder[:, 0] ** 2 + encoder[:, 1] ** 2 + spec.zled**2)[..., None])
+    leds = encoder
+    if spec.led_rotation_deg or any(spec.led_shift):
+        t = np.deg2rad(spec.led_rotation_deg)
+        rot = np.array([[np.cos(t), -np.sin(t)], [np.sin(t), np.cos(t)]])
+        leds = encoder @ rot.T + np.asarray(spec.led_shift, dtype=np.float64)
+    shift = np.round(conv * leds / np.sqrt(leds[:, 0] ** 2 + leds[:, 1] ** 2 + spec.zled**2)[..., None])
     pos = (shift + No // 2 - Np // 2).astype(int)
     I = np.empty((len(pos), Np, Np), np.float64)
     for j, (py, px) in enumerate(pos):
