@@ -411,6 +411,71 @@ def run_reference(args):
     }
 
 
+def run_calibration(args):
+    """FPM illumination calibration (PtyLab's IlluminationCalibration with the
+    example script's settings: radius calibration, translation fit) on a
+    synthetic 15 x 15 LED scan of 256 x 256 frames whose LED array is shifted
+    and whose NA is given 8 % low: GPU end to end (host frames in, encoder
+    out), best of ``--calib-reps``, against the NumPy/SciPy oracle on one
+    core, run once on the same data; "agree" says whether every integer
+    decision (brightfield split, per-LED positions, fitted positions) matched."""
+    import types
+
+    import numpy as np
+    import torch
+
+    from oracle import calib_oracle as co
+    from ptylab_gb300.CalibrationFPM import IlluminationCalibration
+    from ptylab_gb300.simulate import FPMSpec, simulate_fpm
+
+    spec = FPMSpec(Np=256, No=1024, grid=15, photons=1e5, amp_contrast=0.2, phase_scale=0.3 * np.pi,
+                   led_shift=(6e-4, 4e-4), NA=0.092, true_NA=0.1)
+    I, enc, _, _, dxp = simulate_fpm(spec)
+    conv = -(1 / spec.wavelength) * dxp * spec.Np
+    pos = np.round(conv * enc / np.sqrt(enc[:, 0] ** 2 + enc[:, 1] ** 2 + spec.zled**2)[..., None])
+    pos = (pos + spec.No // 2 - spec.Np // 2).astype(int)
+
+    def gpu_once():
+        rec = types.SimpleNamespace(Np=spec.Np, No=spec.No, dxp=dxp, dxo=dxp, wavelength=spec.wavelength,
+                                    NA=spec.NA, zled=spec.zled, positions=pos.copy())
+        data = types.SimpleNamespace(ptychogram=I, encoder=enc.copy())
+        ic = IlluminationCalibration(rec, data)
+        ic.calibrateRadius = True
+        ic.fit_mode = "Translation"
+        np.random.seed(1234)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ic.runCalibration()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, ic
+
+    gpu_once()  # library and allocator warm-up
+    times, ic = [], None
+    for _ in range(max(1, args.calib_reps)):
+        t, ic = gpu_once()
+        times.append(t)
+    oracle = co.CalibrationOracle(spec.Np, spec.No, dxp, spec.wavelength, spec.NA, calibrateRadius=True,
+                                  fit_mode="Translation")
+    np.random.seed(1234)
+    t0 = time.perf_counter()
+    _, _, _, fitted = oracle.run(I.copy(), pos)
+    cpu = time.perf_counter() - t0
+    agree = (np.array_equal(ic.brightfieldIndices, oracle.brightfieldIndices)
+             and np.array_equal(ic.calibrated_positions, oracle.calibrated_positions)
+             and np.array_equal(ic.positionsFitted, fitted) and ic.apertRadiusPixel == oracle.apertRadiusPixel)
+    return {
+        "metric": "FPM illumination calibration time", "value": round(min(times), 4), "unit": "s",
+        "higher_is_better": False, "n_gpus": 1, "steps": len(times), "warmup": 1,
+        "dtype": "f32 frames, c64 transforms, f64 decisions", "data": "synthetic: shifted 15 x 15 LED array, NA 8 % low",
+        "config": {"workload": "IlluminationCalibration.runCalibration, 225 LEDs, 256 x 256 frames, "
+                               "calibrateRadius=True, fit_mode='Translation'",
+                   "brightfield": int(np.sum(ic.brightfieldIndices)), "search_rounds": int(ic.rounds)},
+        "times_s": [round(t, 4) for t in times], "agree": bool(agree),
+        "cpu_baseline": {"value": round(cpu, 3), "unit": "s", "cores": 1, "kind": "port",
+                         "sample": "the same calibration once (NumPy/SciPy oracle)"},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -426,7 +491,13 @@ def main():
                     help="batched launch: 0 = plan's choice, 1 = probe rows in L2, 2 = in shared memory")
     ap.add_argument("--ref-procs", type=int, default=0)
     ap.add_argument("--warmup-ref", type=int, default=1)
+    ap.add_argument("--calibration", action="store_true",
+                    help="time the FPM illumination calibration instead of the reconstruction")
+    ap.add_argument("--calib-reps", type=int, default=3)
     args = ap.parse_args()
+    if args.calibration:
+        print(json.dumps(run_calibration(args)), flush=True)
+        return
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
 

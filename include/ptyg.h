@@ -406,6 +406,47 @@ PTYG_API int ptyg_stitch(const void* patches, const int32_t* positions, int n, i
 PTYG_API int ptyg_nn_adam(float* p, const float* g, float* m, float* v, void* p16, int64_t n, float lr, float b1,
                           float b2, float eps, int step, float weight_decay, void* stream);
 
+/* ---------------------------------------------------------------------
+ * FPM illumination calibration (PtyLab/Reconstruction/CalibrationFPM.py).
+ * PtyLab runs it in NumPy/SciPy (IlluminationCalibration, :33-919); these
+ * calls do its arithmetic, the host keeps its decisions.  Frames are
+ * N x N float32 (N = 32, 64, 128 or 256), C order; all pointers are device
+ * pointers unless marked host.
+ *
+ * ptyg_calib_spectra (convertToFourierSpace, :113-136 up to the mean):
+ *   windowed[f] = float(frames[f] * window)  (window: N*N float64),
+ *   frame_sums[f] = sum of windowed[f] (FP64),
+ *   spectra[f] = ifft2c(windowed[f])  (complex64, n*N*N),
+ *   ft[f] = |spectra[f]|, norm = mean over f of ft (float32, N*N).
+ * ptyg_calib_normalise (:137-145): ft = |ft / max(norm, floor_value)|.
+ * ptyg_calib_gaussian (skimage.filters.gaussian = scipy.ndimage.
+ *   gaussian_filter, mode "nearest"): host half_weights[0..radius], the
+ *   centre weight first; in == out allowed.
+ * ptyg_calib_arcs (generateCircularArcsVectorized + map_coordinates +
+ *   mean, :149-288, :482-495, :586-610): for task t, radius r and grid
+ *   shift (a, b), the mean over the angles k kept in task_keep[t] (bit k)
+ *   of images[task_image[t]] sampled bilinearly at
+ *   (float(R_r sin_k + N/2 + p0 + a - search), float(R_r cos_k + N/2 + p1 + b - search)),
+ *   p = task_pos[2t..2t+1]; out[t][r][a][b], float32; NaN when no angle is kept.
+ *   Host arrays: radii (nradii <= 64), sin_angles, cos_angles (nangles <= 64).
+ *   task_image[t] must index a frame of `images` (not checked on the device).
+ * ptyg_calib_rms (calculateRMSE, :290-358): for candidate k,
+ *   sqrt(mean((images[l] - |ifft2c(pupil_k * spectra[l])|)^2)), l = cand_led[k],
+ *   pupil_k = ((i - N/2 + q0)^2 + (j - N/2 + q1)^2 <= radius^2),
+ *   (q0, q1) = cand_q[2k..2k+1] (position + error, integers); rms[k] FP64;
+ *   cand_led[k] must index a frame of `spectra` and `images`. */
+PTYG_API int ptyg_calib_spectra(int n, int N, const float* frames, const double* window, float* windowed,
+                                double* frame_sums, void* spectra, float* ft, float* norm, void* stream);
+PTYG_API int ptyg_calib_normalise(int n, int N, float* ft, const float* norm, float floor_value, void* stream);
+PTYG_API int ptyg_calib_gaussian(int n, int N, int radius, const double* half_weights, const float* in, float* out,
+                                 void* stream);
+PTYG_API int ptyg_calib_arcs(int N, const float* images, int ntasks, const int* task_image, const double* task_pos,
+                             const unsigned long long* task_keep, int nradii, const double* radii, int nangles,
+                             const double* sin_angles, const double* cos_angles, int search, float* out,
+                             void* stream);
+PTYG_API int ptyg_calib_rms(int N, const void* spectra, const float* images, int ncand, const int* cand_led,
+                            const int* cand_q, double radius, double* rms, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -134,6 +134,16 @@ _SIGNATURES = {
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
     ],
     "ptyg_nn_conv3_path": [C.c_int],
+    "ptyg_calib_spectra": [C.c_int, C.c_int] + [C.c_void_p] * 8,
+    "ptyg_calib_normalise": [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p],
+    "ptyg_calib_gaussian": [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "ptyg_calib_arcs": [
+        C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+        C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+    ],
+    "ptyg_calib_rms": [
+        C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+    ],
     "ptyg_stitch": [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
     "ptyg_propagate_sets": [
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
