@@ -98,6 +98,11 @@ class Reconstruction(object):
         if self.encoder_corrected is None:
             self.encoder_corrected = data.encoder.copy()
 
+    def reset_positioncorrection(self):
+        """Positions from the data's encoder again (Reconstruction.py:136-138),
+        e.g. after an illumination calibration rewrote it."""
+        self.encoder_corrected = self.data.encoder.copy()
+
     @property
     def zo(self):
         return self._zo

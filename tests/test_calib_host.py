@@ -163,3 +163,31 @@ def test_plot_and_sizes_are_refused():
     ic.plot = True
     with pytest.raises(NotImplementedError):
         ic.runCalibration()
+
+
+def test_calibrated_encoder_reaches_positions_after_reset():
+    """As in the reference, the calibration rewrites the data's encoder; the
+    reconstruction's positions follow after reset_positioncorrection()."""
+    from ptylab_gb300 import ExperimentalData, Params, Reconstruction
+
+    g, settings = load_case("affine_small")
+    d = ExperimentalData(None, "FPM")
+    d.ptychogram = g["ptychogram"].astype(np.float32)
+    d.encoder = g["encoder"].copy()
+    d.dxd = float(g["dxp"]) * 4.0
+    d.magnification = 4.0
+    d.zled = float(g["zled"])
+    d.wavelength = float(g["wavelength"])
+    d.NA = float(g["NA_in"])
+    d._setData()
+    rec = Reconstruction(d, Params(), No=int(g["No"]))
+    np.testing.assert_array_equal(rec.positions, g["positions"])
+    ic = cal.IlluminationCalibration(rec, d)
+    for k, v in settings.items():
+        setattr(ic, k, v)
+    ic._dev = NumpyDevice(co.CalibrationOracle(rec.Np, rec.No, rec.dxp, rec.wavelength, rec.NA, **settings))
+    ic.runCalibration()
+    np.testing.assert_allclose(d.encoder, g["encoder_out"], rtol=0, atol=1e-15)
+    np.testing.assert_array_equal(rec.positions, g["positions"])  # encoder_corrected untouched
+    rec.reset_positioncorrection()
+    assert not np.array_equal(rec.positions, g["positions"])

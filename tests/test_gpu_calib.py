@@ -47,7 +47,10 @@ def load_case(name):
 
 
 def rel(a, b):
-    return float(np.max(np.abs(np.asarray(a, np.float64) - b)) / max(np.max(np.abs(b)), 1e-30))
+    """Largest difference relative to the largest magnitude (complex-safe)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.max(np.abs(a.astype(np.complex128) - b)) / max(float(np.max(np.abs(b))), 1e-30))
 
 
 @pytest.mark.parametrize("N", [64, 128, 256])

@@ -377,3 +377,16 @@ def test_results_load_back(tmp_path):
         rec.saveResults(str(q), type=name, squeeze=True)
         with hdf5.File(q) as f:
             assert f[name].shape == np.squeeze(getattr(rec, name)).shape
+
+
+def test_easy_initialize_from_files():
+    """PtyLab's easyInitialize (PtyLab/__init__.py:11-58) on measurement files."""
+    import ptylab_gb300 as P
+
+    d, rec, params, monitor, engine = P.easyInitialize(str(INPUTS / "cpm_simulation.hdf5"), engine=P.Engines.mPIE)
+    assert type(engine).__name__ == "mPIE" and rec.probe.shape[-1] == d.ptychogram.shape[-1]
+    d, rec, params, monitor, engine, calib = P.easyInitialize(str(INPUTS / "fpm_leds.hdf5"), operationMode="FPM")
+    assert type(engine).__name__ == "ePIE" and type(calib).__name__ == "IlluminationCalibration"
+    assert params.positionOrder == "NA" and params.probeBoundary
+    with pytest.raises(NotImplementedError):
+        P.easyInitialize(str(INPUTS / "cpm_simulation.hdf5"), operationMode="XYZ")
