@@ -356,10 +356,10 @@ class IlluminationCalibration:
         self.x_range = len(self.gridSearch_x_init)
         self.y_range = len(self.gridSearch_y_init)
 
-    def _fourier(self, ptychogram):
+    def _fourier(self, ptychogram, smooth=True):
         """convertToFourierSpace on the device: (windowed frames, frame sums,
-        inverse transforms of the windowed frames, smoothed normalised
-        Fourier magnitudes)."""
+        inverse transforms of the windowed frames, normalised Fourier
+        magnitudes, Gaussian-smoothed unless ``smooth`` is False)."""
         dev = self._device()
         if self.img_size not in (32, 64, 128, 256) or ptychogram.shape[-1] != self.img_size:
             raise NotImplementedError("the calibration kernels take frames of 32, 64, 128 or 256 pixels")
@@ -367,7 +367,8 @@ class IlluminationCalibration:
         normalization = dev.to_host(norm)
         mean_outside_support = np.mean(normalization[self.OTF == 0])
         dev.normalise(ft, norm, np.float32(2 * mean_outside_support))
-        dev.gaussian(ft, self.gaussSigma)
+        if smooth:
+            dev.gaussian(ft, self.gaussSigma)
         return windowed, dev.to_host(sums), spectra, ft
 
     def convertToFourierSpace(self, ptychogram):
@@ -596,18 +597,23 @@ class IlluminationCalibration:
         """CalibrationFPM.py:830-919."""
         if self.plot:
             raise NotImplementedError("plotting the calibration is not available")
-        ptychogram = np.array(self.experimentalData.ptychogram, dtype=np.float32, copy=True)
+        # the windowed frames go to a new device buffer, so the data's frames
+        # are read as they are (the reference deep-copies them to window in place)
+        ptychogram = np.asarray(self.experimentalData.ptychogram, dtype=np.float32)
         self.initialPositions = np.array(self.reconstructor.positions, copy=True)
         self.initialPositions = self.initialPositions - self.reconstructor.No // 2 + self.reconstructor.Np // 2
         self.initialize_error_search_space()
-        windowed, sums, spectra, ft = self._fourier(ptychogram)
+        # the smoothing is per frame and only the brightfield frames are
+        # searched, so only they are smoothed (the reference smooths all)
+        windowed, sums, spectra, ft = self._fourier(ptychogram, smooth=False)
         if not hasattr(self.brightfieldIndices, "__len__"):
             self.brightfieldIndices = self.findBrightfielIndices(frame_sums=sums)
         bf = np.asarray(self.brightfieldIndices)
         bf_idx = np.flatnonzero(bf) if bf.dtype == bool else bf
         dev = self._device()
+        ft_bf = dev.gaussian(dev.take(ft, bf_idx), self.gaussSigma)
         if self.calibrateRadius:
-            oldRadius, newRadius = self.findCalibratedRadius(None, dev.take(ft, bf_idx), self.initialPositions[bf])
+            oldRadius, newRadius = self.findCalibratedRadius(None, ft_bf, self.initialPositions[bf])
             logger.info("Initial radius was %spx, calibrated radius is %spx", np.round(oldRadius, 2),
                         np.round(newRadius, 2))
             self.reconstructor.NA = np.round(newRadius / self.dxp * self.wavelength / self.img_size, 3)
@@ -615,8 +621,7 @@ class IlluminationCalibration:
         else:
             self.reconstructor.NA = self.apertRadiusPixel / self.dxp * self.wavelength / self.img_size
         self.calibMatrix, _ = self.findPositionCalibrationMatrix(
-            dev.take(windowed, bf_idx), dev.take(ft, bf_idx), self.initialPositions[bf, :],
-            spectra=dev.take(spectra, bf_idx))
+            dev.take(windowed, bf_idx), ft_bf, self.initialPositions[bf, :], spectra=dev.take(spectra, bf_idx))
         positionsFitted = matrix_transform(self.initialPositions, self.calibMatrix.params)
         self.reconstructor.entrancePupilDiameter = self.apertRadiusPixel * self.dxp * 2
         self.positionsFitted = positionsFitted.astype(int)

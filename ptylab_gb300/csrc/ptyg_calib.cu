@@ -152,51 +152,71 @@ __device__ float pairwise_sum_f32(const float* a, int n) {
 }
 
 // Mean over the kept angles of the bilinearly sampled image on the circle
-// of radius R_r about (N/2 + p0 + g_a, N/2 + p1 + g_b).  One thread per
-// (task, r, a, b); out[task][r][a][b].
+// of radius R_r about (N/2 + p0 + g_a, N/2 + p1 + g_b).  One block per
+// (task, radius): the row coordinate of every (angle, a) and the column
+// coordinate of every (angle, b) are computed once into shared memory (the
+// reference's float64 sums rounded to float32, floor and fraction, both
+// exact), then each thread takes grid shifts (a, b) and interpolates in
+// double in SciPy's corner order.  out[task][r][a][b].
 __global__ void arcs_kernel(const float* __restrict__ images, int N, const int* __restrict__ task_image,
                             const double* __restrict__ task_pos, const unsigned long long* __restrict__ task_keep,
-                            Radii radii, int R, Angles ang, int nang, int S, float* __restrict__ out,
-                            size_t total) {
-  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= total) return;
+                            Radii radii, int R, Angles ang, int nang, int S, float* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char arcs_smem[];
+  __shared__ int kidx[kMaxAngles];
+  __shared__ int nk;
+  const int t = blockIdx.x / R, r = blockIdx.x - (blockIdx.x / R) * R;
   const int G = 2 * S + 1;
-  size_t rest = idx;
-  const int b = (int)(rest % G);
-  rest /= G;
-  const int a = (int)(rest % G);
-  rest /= G;
-  const int r = (int)(rest % R);
-  const int t = (int)(rest / R);
-  const float* img = images + (size_t)task_image[t] * N * N;
-  const double p0 = task_pos[2 * t], p1 = task_pos[2 * t + 1];
   const unsigned long long keep = task_keep[t];
+  if (threadIdx.x == 0) {
+    int n = 0;
+    for (int k = 0; k < nang; ++k)
+      if ((keep >> k) & 1ull) kidx[n++] = k;
+    nk = n;
+  }
+  __syncthreads();
+  const int n = nk;
+  int* xi = (int*)arcs_smem;
+  float* xt = (float*)(xi + nang * G);
+  int* yi = (int*)(xt + nang * G);
+  float* yt = (float*)(yi + nang * G);
   const double half = (double)N / 2.0;
   const double rad = radii.r[r];
-  float vals[kMaxAngles];
-  int n = 0;
-  for (int k = 0; k < nang; ++k) {
-    if (!((keep >> k) & 1ull)) continue;
-    const float xf = __double2float_rn(
+  const double p0 = task_pos[2 * t], p1 = task_pos[2 * t + 1];
+  for (int e = threadIdx.x; e < n * G; e += blockDim.x) {
+    const int kk = e / G, a = e - (e / G) * G;
+    const int k = kidx[kk];
+    const double cx = (double)__double2float_rn(
         __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(rad, ang.s[k]), half), p0), (double)(a - S)));
-    const float yf = __double2float_rn(
-        __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(rad, ang.c[k]), half), p1), (double)(b - S)));
-    const double cx = (double)xf, cy = (double)yf;
+    const double cy = (double)__double2float_rn(
+        __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(rad, ang.c[k]), half), p1), (double)(a - S)));
     const double fx = floor(cx), fy = floor(cy);
-    const int x0 = (int)fx, y0 = (int)fy;
-    const double tx = __dsub_rn(cx, fx), ty = __dsub_rn(cy, fy);
-    const double wx[2] = {__dsub_rn(1.0, tx), tx};
-    const double wy[2] = {__dsub_rn(1.0, ty), ty};
-    double acc = 0.0;
-    for (int u = 0; u < 2; ++u)
-      for (int v = 0; v < 2; ++v) {
-        const int xi = x0 + u, yi = y0 + v;
-        const double px = (xi >= 0 && xi < N && yi >= 0 && yi < N) ? (double)img[xi * N + yi] : 0.0;
-        acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(px, wx[u]), wy[v]));
-      }
-    vals[n++] = __double2float_rn(acc);
+    xi[e] = (int)fx;
+    xt[e] = (float)__dsub_rn(cx, fx);  // exact: a float32 coordinate's fraction
+    yi[e] = (int)fy;
+    yt[e] = (float)__dsub_rn(cy, fy);
   }
-  out[idx] = n ? __fdiv_rn(pairwise_sum_f32(vals, n), (float)n) : nanf("");
+  __syncthreads();
+  const float* img = images + (size_t)task_image[t] * N * N;
+  float* o = out + (size_t)blockIdx.x * G * G;
+  for (int ab = threadIdx.x; ab < G * G; ab += blockDim.x) {
+    const int a = ab / G, b = ab - (ab / G) * G;
+    float vals[kMaxAngles];
+    for (int kk = 0; kk < n; ++kk) {
+      const int x0 = xi[kk * G + a], y0 = yi[kk * G + b];
+      const double tx = xt[kk * G + a], ty = yt[kk * G + b];
+      const double wx[2] = {__dsub_rn(1.0, tx), tx};
+      const double wy[2] = {__dsub_rn(1.0, ty), ty};
+      double acc = 0.0;
+      for (int u = 0; u < 2; ++u)
+        for (int v = 0; v < 2; ++v) {
+          const int xx = x0 + u, yy = y0 + v;
+          const double px = (xx >= 0 && xx < N && yy >= 0 && yy < N) ? (double)img[xx * N + yy] : 0.0;
+          acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(px, wx[u]), wy[v]));
+        }
+      vals[kk] = __double2float_rn(acc);
+    }
+    o[ab] = n ? __fdiv_rn(pairwise_sum_f32(vals, n), (float)n) : nanf("");
+  }
 }
 
 // Spectrum of LED cand_led[k] inside the pupil centred where the reference
@@ -308,9 +328,16 @@ extern "C" int ptyg_calib_arcs(int N, const float* images, int ntasks, const int
   Radii rad{};
   for (int k = 0; k < nradii; ++k) rad.r[k] = radii[k];
   const int G = 2 * search + 1;
-  const size_t total = (size_t)ntasks * nradii * G * G;
-  arcs_kernel<<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
-      images, N, task_image, task_pos, task_keep, rad, nradii, ang, nangles, search, out, total);
+  const size_t smem = (size_t)nangles * G * 16;
+  if (smem > 200 * 1024) return ptyg::set_last_error(PTYG_ERR_UNSUPPORTED, "search grid too large for one block");
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(arcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "calib arcs shared memory");
+  }
+  const long long blocks = (long long)ntasks * nradii;
+  if (blocks > 0x7fffffffLL) return invalid("too many tasks");
+  arcs_kernel<<<(unsigned)blocks, 256, smem, (cudaStream_t)stream>>>(images, N, task_image, task_pos, task_keep,
+                                                                     rad, nradii, ang, nangles, search, out);
   return cuda_status(cudaGetLastError(), "calib arcs");
 }
 
