@@ -49,7 +49,13 @@ enum ptyg_engine { PTYG_EPIE = 0, PTYG_MPIE = 1, PTYG_QNEWTON = 2, PTYG_E3PIE = 
 /* mqNewton.momentum_method (PtyLab/Engines/mqNewton.py:68-79, 142-182) */
 enum ptyg_momentum { PTYG_MOMENTUM = 0, PTYG_ADAM = 1, PTYG_NADAM = 2 };
 /* params.intensityConstraint (PtyLab/Engines/BaseEngine.py:913-961) */
-enum ptyg_intensity_constraint { PTYG_STANDARD = 0, PTYG_POISSION = 1, PTYG_EXPONENTIAL = 2, PTYG_FLUCTUATION = 3 };
+enum ptyg_intensity_constraint {
+  PTYG_STANDARD = 0,
+  PTYG_POISSION = 1,
+  PTYG_EXPONENTIAL = 2,
+  PTYG_FLUCTUATION = 3,
+  PTYG_INTERFEROMETRIC = 4 /* a detector-plane reference field R per mode: I_est = sum |Psi + R|^2 */
+};
 enum ptyg_propagator {
   PTYG_FRAUNHOFER = 0,
   PTYG_FRESNEL = 1,
@@ -264,6 +270,15 @@ typedef struct ptyg_projection {
  * fluctuation constraint, its per-frame intensity scaling (set to 1). */
 PTYG_API int ptyg_plan_set_projection(ptyg_plan* plan, const ptyg_projection* projection, const float* W,
                                       const float* intensity_mask, void* stream);
+
+/* The interferometric constraint's reference field of scan `scan`
+ * (reconstruction.reference, BaseEngine.py:371-374, 883-891, 975-982):
+ * ptyg_plan_set_projection sets it to ones for every mode (as the reference
+ * does at every reconstruct()); each position then sets
+ * Psi' = (Psi + R) frac - R and R' = (Psi + R) frac - Psi per mode.  Read
+ * out as device complex64 (nlambda * nosm * npsm, Np, Np), natural layout
+ * (fftshifted when fftshift).  Fraunhofer and Fresnel plans only. */
+PTYG_API int ptyg_plan_get_reference(ptyg_plan* plan, int scan, void* reference, void* stream);
 
 /* Background of scan `scan` (reconstruction.background), device float32
  * (Np, Np) in the ptychogram's layout: load it into the plan, or read it out. */

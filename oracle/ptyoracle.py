@@ -364,6 +364,7 @@ class State:
     probeMomentum_v: Optional[np.ndarray] = None
     purityProbe: float = 1.0
     background: Optional[np.ndarray] = None  # backgroundModeSwitch (float64, Np x Np)
+    reference: Optional[np.ndarray] = None  # 'interferometric': detector-plane reference field
     intensityScaling: Optional[np.ndarray] = None  # 'fluctuation': per-frame scaling (params.intensityScaling)
 
 
@@ -421,6 +422,8 @@ class OracleEngine:
             self.fftshiftFlag = True
         if s.backgroundModeSwitch:  # _checkMISC BaseEngine.py:361-364
             st.background = 1e-1 * np.ones((g.Np, g.Np))
+        if s.intensityConstraint == "interferometric":  # BaseEngine.py:371-374 (float64 ones)
+            st.reference = np.ones(st.probe[0, 0, 0, 0, ...].shape)
         if s.probePowerCorrectionSwitch:  # BaseEngine.py:227-235
             maxProbePower = np.sqrt(np.max(np.sum(self.ptychogram, (-1, -2))))
             st.probe = st.probe / np.sqrt(np.sum(st.probe * st.probe.conj())) * maxProbePower
@@ -450,7 +453,10 @@ class OracleEngine:
         s, st = self.s, self.st
         gimmel = 1e-10
         ESW = object2detector(esw, s.propagator, s.fftshift, self.g)
-        Iest = np.sum(np.abs(ESW) ** 2, axis=(0, 1, 2))[-1]
+        if s.intensityConstraint == "interferometric":  # BaseEngine.py:883-888
+            Iest = np.sum(np.abs(ESW + st.reference) ** 2, axis=(0, 1, 2))[-1]
+        else:
+            Iest = np.sum(np.abs(ESW) ** 2, axis=(0, 1, 2))[-1]
         if s.backgroundModeSwitch:
             Iest += st.background
         Imeas = self.ptychogram[j]
@@ -481,11 +487,15 @@ class OracleEngine:
             frac = W * frac + (1 - W)
         elif c == "poission":
             frac = Imeas / (Iest + gimmel)
-        elif c == "standard":
+        elif c in ("standard", "interferometric"):
             frac = np.sqrt(Imeas / (Iest + gimmel))
         else:
             raise ValueError("intensity constraint not properly specified!")
-        if s.intensityMask:
+        if c == "interferometric":  # BaseEngine.py:975-982: the reference takes the ESW's shape
+            temp = (ESW + st.reference) * frac - ESW
+            ESW = (ESW + st.reference) * frac - st.reference
+            st.reference = temp
+        elif s.intensityMask:
             ESW = ESW * (frac * self.intensity_mask + (self.intensity_mask - 1))
         else:
             ESW = ESW * frac

@@ -88,7 +88,10 @@ class BaseEngine(object):
         p, rec = self.params, self.reconstruction
         ic = p.intensityConstraint
         if ic == "interferometric":
-            raise NotImplementedError("intensityConstraint 'interferometric' is not supported by the GB300 engines")
+            if self.engine_name not in ("ePIE", "mPIE", "qNewton"):
+                raise NotImplementedError("the interferometric constraint runs with the GB300 ePIE, mPIE and qNewton")
+            if p.propagatorType.lower() not in ("fraunhofer", "fresnel"):
+                raise NotImplementedError("the interferometric constraint runs with the Fraunhofer and Fresnel propagators")
         if ic not in _native.INTENSITY_CONSTRAINTS:
             raise ValueError("intensity constraint not properly specified!")  # BaseEngine.py:963-964
         if ic == "fluctuation" and not hasattr(p, "intensityScaling"):
@@ -132,6 +135,8 @@ class BaseEngine(object):
             rec.background = 1e-1 * np.ones((rec.Np, rec.Np))
         if self.params.intensityConstraint == "fluctuation":  # BaseEngine.py:367-369
             self.intensityScaling = np.ones(self.experimentalData.numFrames)
+        if self.params.intensityConstraint == "interferometric":  # BaseEngine.py:371-374
+            rec.reference = np.ones((int(rec.Np), int(rec.Np)))
 
     def _projection_switches_on(self):
         p = self.params
@@ -646,6 +651,14 @@ class BaseEngine(object):
             bg = self._dev["background"]
             _native.check(lib.ptyg_plan_get_background(self._plan, self._scan, bg.data_ptr(), stream), "ptyg_plan_get_background")
             rec.background = bg.cpu().numpy().astype(np.float64)
+        if p.intensityConstraint == "interferometric":
+            # reconstruction.reference takes the exit wave's shape after the
+            # first position (BaseEngine.py:975-982)
+            shape = (int(getattr(rec, "nlambda", 1)), int(rec.nosm), int(rec.npsm), 1, int(rec.Np), int(rec.Np))
+            ref = torch.empty(shape, dtype=torch.complex64, device=self._dev["device"])
+            _native.check(lib.ptyg_plan_get_reference(self._plan, self._scan, ref.data_ptr(), stream),
+                          "ptyg_plan_get_reference")
+            rec.reference = ref.cpu().numpy()
         if p.intensityConstraint == "fluctuation":
             nf = self.experimentalData.numFrames
             out = np.empty(nf, dtype=np.float64)

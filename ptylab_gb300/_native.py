@@ -26,7 +26,7 @@ PTYG_ERR_DEVICE = -6
 
 ENGINES = {"ePIE": 0, "mPIE": 1, "qNewton": 2, "e3PIE": 3, "mqNewton": 4}
 MOMENTUM_METHODS = {"momentum": 0, "ADAM": 1, "NADAM": 2}
-INTENSITY_CONSTRAINTS = {"standard": 0, "poission": 1, "exponential": 2, "fluctuation": 3}
+INTENSITY_CONSTRAINTS = {"standard": 0, "poission": 1, "exponential": 2, "fluctuation": 3, "interferometric": 4}
 # the engines' propagators: polychromeASP is the ASP kernel with one table per wavelength
 PROPAGATORS = {"fraunhofer": 0, "fresnel": 1, "asp": 2, "polychromeasp": 2}
 # ptyg_propagate_sets (include/ptyg.h enum ptyg_propagator)
@@ -164,6 +164,7 @@ _SIGNATURES = {
     "ptyg_plan_status": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p],
     "ptyg_plan_set_projection": [C.c_void_p, C.POINTER(Projection), C.c_void_p, C.c_void_p, C.c_void_p],
     "ptyg_plan_set_background": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_plan_get_reference": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_get_background": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_intensity_scaling": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_multislice_workspace_bytes": [C.POINTER(Multislice)],

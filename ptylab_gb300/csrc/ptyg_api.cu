@@ -317,6 +317,7 @@ struct ScanOwned {
   float* tileMax = nullptr;
   float* background = nullptr;  // data layout
   double* iscale = nullptr;
+  float2* reference = nullptr;  // interferometric: K planes, data layout
   unsigned* red = nullptr;
   int* status = nullptr;
   bool bound = false;
@@ -351,6 +352,7 @@ static void plan_free(ptyg_plan* p) {
   cudaFree(p->imask);
   for (auto& s : p->scans) {
     cudaFree(s.background);
+    cudaFree(s.reference);
     cudaFree(s.iscale);
     cudaFree(s.data);
     cudaFree(s.work);
@@ -598,6 +600,7 @@ extern "C" int ptyg_plan_bind_scan(ptyg_plan* p, int scan, const ptyg_scan_buffe
   d.vec4 = p->g.No % 2 == 0 && ((uintptr_t)b->object % 16) == 0 && ((uintptr_t)b->object_momentum % 16) == 0;
   d.background = o.background;
   d.iscale = o.iscale;
+  d.reference = o.reference;
   o.bound = true;
   o.orderLen = p->g.num_frames;
   PTYG_CUDA(cudaMemcpyAsync(p->dScans + scan, &d, sizeof(ScanDev), cudaMemcpyHostToDevice, st), "scan upload");
@@ -783,6 +786,11 @@ static int from_data_layout(const ptyg_plan* p, const float* in, float* out, cud
   return PTYG_OK;
 }
 
+// planes of the interferometric reference field: one per exit-wave mode
+static int ref_planes(const ptyg_plan* p) {
+  return (p->g.nlambda > 0 ? p->g.nlambda : 1) * p->g.nosm * p->g.npsm;
+}
+
 static __global__ void fill_kernel(float* x, size_t n, float v) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] = v;
@@ -796,8 +804,12 @@ extern "C" int ptyg_plan_set_projection(ptyg_plan* p, const ptyg_projection* pr,
                                         const float* intensity_mask, void* stream) {
   if (!p || !pr) return fail(PTYG_ERR_INVALID, "null argument");
   const ptyg_projection& q = *pr;
-  if (q.intensity_constraint < PTYG_STANDARD || q.intensity_constraint > PTYG_FLUCTUATION)
+  if (q.intensity_constraint < PTYG_STANDARD || q.intensity_constraint > PTYG_INTERFEROMETRIC)
     return fail(PTYG_ERR_INVALID, "intensity_constraint=%d", q.intensity_constraint);
+  if (q.intensity_constraint == PTYG_INTERFEROMETRIC && p->g.propagator == PTYG_ASP)
+    return fail(PTYG_ERR_UNSUPPORTED, "the interferometric constraint runs with Fraunhofer and Fresnel plans");
+  if (q.intensity_constraint == PTYG_INTERFEROMETRIC && p->g.engine == PTYG_MQNEWTON)
+    return fail(PTYG_ERR_UNSUPPORTED, "the interferometric constraint runs with ePIE, mPIE and qNewton plans");
   const bool any = q.intensity_constraint || q.adaptive_denoising || q.background_mode || q.fourier_mask ||
                    q.intensity_mask;
   if (p->g.engine == PTYG_E3PIE && any)
@@ -828,12 +840,28 @@ extern "C" int ptyg_plan_set_projection(ptyg_plan* p, const ptyg_projection* pr,
       fill_kernel_d<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(o.iscale, nf, 1.0);
       PTYG_CUDA(cudaGetLastError(), "fill");
     }
+    if (q.intensity_constraint == PTYG_INTERFEROMETRIC) {
+      const int planes = ref_planes(p);
+      if (!o.reference) PTYG_CUDA(cudaMalloc(&o.reference, (size_t)planes * n2 * sizeof(float2)), "allocation");
+      PTYG_CUDA(ptyg::reference_init(o.reference, planes, p->g.Np, !p->g.fftshift, st), "reference init");
+    }
     p->hScans[s].background = o.background;
     p->hScans[s].iscale = o.iscale;
+    p->hScans[s].reference = o.reference;
     PTYG_CUDA(cudaMemcpyAsync(p->dScans + s, &p->hScans[s], sizeof(ScanDev), cudaMemcpyHostToDevice, st),
               "scan upload");
   }
   p->proj = q;
+  return PTYG_OK;
+}
+
+extern "C" int ptyg_plan_get_reference(ptyg_plan* p, int scan, void* reference, void* stream) {
+  if (!p || !reference) return fail(PTYG_ERR_INVALID, "null argument");
+  if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
+  if (!p->scans[scan].reference) return fail(PTYG_ERR_INVALID, "the interferometric constraint is off");
+  PTYG_CUDA(ptyg::reference_natural(p->scans[scan].reference, (float2*)reference, ref_planes(p), p->g.Np,
+                                    !p->g.fftshift, (cudaStream_t)stream),
+            "reference readout");
   return PTYG_OK;
 }
 

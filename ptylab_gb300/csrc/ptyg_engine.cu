@@ -36,7 +36,7 @@ cudaError_t engine_max_clusters(int Np, int engine, int nlambda, int cluster, in
 
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
   if (a.engine == ENG_MQNEWTON) return launch_engine_mq(a, nscans, threads, smem, st);
-  if (a.nlambda > 1) return launch_engine_poly(a, nscans, threads, smem, st);
+  if (a.nlambda > 1 || a.iconstraint == IC_INTERFEROMETRIC) return launch_engine_poly(a, nscans, threads, smem, st);
   return launch_engine_t<VAR_STD>(a, nscans, threads, smem, st);
 }
 

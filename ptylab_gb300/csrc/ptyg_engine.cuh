@@ -9,7 +9,7 @@ namespace ptyg {
 enum Engine { ENG_EPIE = 0, ENG_MPIE = 1, ENG_QNEWTON = 2, ENG_E3PIE = 3, ENG_MQNEWTON = 4 };
 enum Momentum { MOM_PLAIN = 0, MOM_ADAM = 1, MOM_NADAM = 2 };
 // params.intensityConstraint (BaseEngine.py:913-961)
-enum IntensityConstraint { IC_STANDARD = 0, IC_POISSON = 1, IC_EXPONENTIAL = 2, IC_FLUCTUATION = 3 };
+enum IntensityConstraint { IC_STANDARD = 0, IC_POISSON = 1, IC_EXPONENTIAL = 2, IC_FLUCTUATION = 3, IC_INTERFEROMETRIC = 4 };
 
 // Object modes the pixel-update loop carries in registers.
 constexpr int MAX_OBJECT_MODES = 4;
@@ -51,6 +51,7 @@ struct ScanDev {
   int vec4;                // No even and object / objectMomentum 16-byte aligned: 16-byte accesses
   float* background;       // backgroundModeSwitch: Np x Np, data layout (plan-owned)
   double* iscale;          // 'fluctuation': per-frame intensity scaling aleph (plan-owned)
+  float2* reference;       // 'interferometric': K planes of Np x Np, data layout, scaled N * M * R (plan-owned)
 };
 
 // Side of the object tiles whose maxima qNewton keeps up to date.

@@ -497,6 +497,10 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
     // column w (pixel w * NP + 32 r + lane gets Iest(r)), else every thread
     // strides over the CTA's LN pixels (pixel i gets Iest(i)).  The column
     // form serves the fused pass B and only single-pass projections.
+    // the interferometric constraint is compiled into the several-wavelength
+    // instantiation only (which serves ePIE, mPIE and qNewton for any nlambda),
+    // so the standard kernel's registers stay as they are
+    const bool interf = VAR == VAR_POLY && a.iconstraint == IC_INTERFEROMETRIC;
     auto project = [&](auto Iest, float outScale, auto colsTag) -> double {
       constexpr bool cols = decltype(colsTag)::value;
       const bool det = a.writeDetErr && s.detErr;
@@ -520,10 +524,12 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
           frac = w * sqrtf(q) + (1.f - w);
         } else if (a.iconstraint == IC_FLUCTUATION) {
           frac = (1.f + aleph) * 0.5f * q;
-        } else {
+        } else {  // standard and interferometric (BaseEngine.py:955-962)
           frac = sqrtf(q);
         }
-        sm.fr[i] = (Mt ? frac * Mt[i] + (Mt[i] - 1.f) : frac) * outScale;
+        // interferometric: the raw factor, applied with the reference field
+        // after the projection (no intensity mask there, BaseEngine.py:975-982)
+        sm.fr[i] = interf ? frac : (Mt ? frac * Mt[i] + (Mt[i] - 1.f) : frac) * outScale;
         if (bg) {
           const float u = 1.f + a.invFrames * (sqrtf(frac) - 1.f);
           float b = bg[i] * (u * u);
@@ -578,7 +584,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
     };
 
     double err = 0.0;
-    if (!asp && nw == L && !(a.denoise || a.iconstraint == IC_FLUCTUATION)) {
+    if (!asp && nw == L && !(a.denoise || a.iconstraint == IC_FLUCTUATION || interf)) {
       // ---------------- B, fused: warp w owns column w of every mode, so it
       // transforms the column's K modes, sums their intensities in
       // registers, projects its own pixels and transforms back, with no
@@ -652,14 +658,41 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
             for (int r = 0; r < E; ++r) sm.tile[tix<L>(k * NP + 32 * r + lane, c)] = v[r];
           });
       __syncthreads();
+      // interferometric: the reference field of this CTA's pixels, plane k at
+      // + k * NP * NP, held as N M R in the tile's scale and sign
+      float2* refb = interf ? s.reference + (size_t)blk0 * NP : nullptr;
       err = project(
           [&](int i) {
             const int c = i / NP, sy = i - (i / NP) * NP;
             float ie = 0.f;
-            for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[tix<L>(k * NP + sy, c)]);
+            if (interf) {  // BaseEngine.py:883-888: sum |Psi + R|^2
+              for (int k = 0; k < K; ++k) {
+                const float2 v = sm.tile[tix<L>(k * NP + sy, c)], r = refb[(size_t)k * NP * NP + i];
+                ie += cabs2(make_float2(v.x + r.x, v.y + r.y));
+              }
+            } else {
+              for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[tix<L>(k * NP + sy, c)]);
+            }
             return ie * inv2;
           },
           inv2, std::false_type{});
+      if (interf) {
+        // BaseEngine.py:975-982: Psi' = (Psi + R) frac - R, R' = (Psi + R) frac - Psi
+        __syncthreads();
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          const int c = i / NP, sy = i - (i / NP) * NP;
+          const float f = sm.fr[i];
+          for (int k = 0; k < K; ++k) {
+            float2& v = sm.tile[tix<L>(k * NP + sy, c)];
+            float2* rp = refb + (size_t)k * NP * NP + i;
+            const float2 r = *rp, psi = v;
+            const float2 sf = make_float2((psi.x + r.x) * f, (psi.y + r.y) * f);
+            *rp = make_float2(sf.x - psi.x, sf.y - psi.y);
+            v = make_float2(sf.x - r.x, sf.y - r.y);
+          }
+          sm.fr[i] = inv2;
+        }
+      }
       __syncthreads();
       fft_tasks<E, true>(
           F, K * L,

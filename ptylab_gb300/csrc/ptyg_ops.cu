@@ -216,6 +216,39 @@ __global__ void to_fourier_layout_kernel(const float* __restrict__ in, float* __
   }
 }
 
+// The interferometric reference field in the kernels' data layout and
+// scale: the detector tile holds V = N M Psi (M = (-1)^(ky+kx) for centred
+// transforms, 1 otherwise), so the field is kept as N M R.  Initial R = 1.
+__global__ void reference_init_kernel(float2* __restrict__ out, int planes, int Np, int centred) {
+  const size_t n = (size_t)planes * Np * Np;
+  const int E = Np / 32;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int rem = (int)(i % ((size_t)Np * Np));
+    const int sx = rem / Np, sy = rem % Np;
+    const int ky = slot_to_index(sy, E), kx = slot_to_index(sx, E);
+    const float m = (centred && ((ky + kx) & 1)) ? -1.f : 1.f;
+    out[i] = make_float2(m * (float)Np, 0.f);
+  }
+}
+
+// R in natural order from the data layout: out[k][ky][kx] = M in[k][sx][sy] / N
+__global__ void reference_natural_kernel(const float2* __restrict__ in, float2* __restrict__ out, int planes, int Np,
+                                         int centred) {
+  const size_t n = (size_t)planes * Np * Np;
+  const int E = Np / 32;
+  const float inv = 1.f / (float)Np;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t f = i / ((size_t)Np * Np);
+    const int rem = (int)(i - f * Np * Np);
+    const int ky = rem / Np, kx = rem % Np;
+    const int sy = 32 * (ky % E) + (int)bitrev5((unsigned)(ky / E));
+    const int sx = 32 * (kx % E) + (int)bitrev5((unsigned)(kx / E));
+    const float m = (centred && ((ky + kx) & 1)) ? -inv : inv;
+    const float2 v = in[(f * Np + sx) * Np + sy];
+    out[i] = make_float2(v.x * m, v.y * m);
+  }
+}
+
 // out[f][ky][kx] = in[f][sx(kx)][sy(ky)]  (inverse of the above)
 __global__ void from_fourier_layout_kernel(const float* __restrict__ in, float* __restrict__ out, int frames, int Np) {
   const size_t n = (size_t)frames * Np * Np;
@@ -233,6 +266,16 @@ __global__ void from_fourier_layout_kernel(const float* __restrict__ in, float* 
 
 cudaError_t to_fourier_layout(const float* in, float* out, int frames, int Np, cudaStream_t st) {
   to_fourier_layout_kernel<<<1024, 256, 0, st>>>(in, out, frames, Np);
+  return cudaGetLastError();
+}
+
+cudaError_t reference_init(float2* out, int planes, int Np, bool centred, cudaStream_t st) {
+  reference_init_kernel<<<256, 256, 0, st>>>(out, planes, Np, centred ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t reference_natural(const float2* in, float2* out, int planes, int Np, bool centred, cudaStream_t st) {
+  reference_natural_kernel<<<256, 256, 0, st>>>(in, out, planes, Np, centred ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -46,6 +46,10 @@ cudaError_t prop_cols(int Np, const float2* in, float2* out, int batch, const Co
                       cudaStream_t st);
 cudaError_t to_fourier_layout(const float* in, float* out, int frames, int Np, cudaStream_t st);
 cudaError_t from_fourier_layout(const float* in, float* out, int frames, int Np, cudaStream_t st);
+// the interferometric reference field (planes of Np x Np): ones in the data
+// layout and scale (N M R), and back to R in natural order
+cudaError_t reference_init(float2* out, int planes, int Np, bool centred, cudaStream_t st);
+cudaError_t reference_natural(const float2* in, float2* out, int planes, int Np, bool centred, cudaStream_t st);
 cudaError_t sum_parts(const double* part, double* err, int frames, int C, cudaStream_t st);
 cudaError_t mul_window(float2* x, const float* w, long long n, long long nw, cudaStream_t st);
 cudaError_t gram(const float2* p, int modes, long long n, double2* G, cudaStream_t st);

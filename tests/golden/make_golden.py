@@ -293,6 +293,8 @@ def run_case(ref, d, case):
         outputs["background"] = np.asarray(rec.background)
     if case.get("intensityScaling"):
         outputs["intensityScaling"] = np.asarray(params.intensityScaling)
+    if getattr(params, "intensityConstraint", "standard") == "interferometric":
+        outputs["reference"] = np.asarray(rec.reference)
     return inputs, outputs
 
 
@@ -406,6 +408,12 @@ SCAN_CONFIGS = {
         params=dict(intensityConstraint="fluctuation", probePowerCorrectionSwitch=True),
     ),
     "epie_intensity_mask": dict(engine="ePIE", iters=3, intensity_mask=True, params=dict(intensityMask=True)),
+    # the interferometric constraint: a detector-plane reference field,
+    # updated at every position (BaseEngine.py:371-374, 883-891, 975-982)
+    "epie_interferometric": dict(engine="ePIE", iters=3, params=dict(intensityConstraint="interferometric")),
+    "mpie_interferometric_modes": dict(
+        engine="mPIE", modes=(1, 1, 2, 1), iters=3, params=dict(intensityConstraint="interferometric")
+    ),
     "epie_asp_denoise_background": dict(
         engine="ePIE", propagator="ASP", iters=3, params=dict(adaptiveDenoisingSwitch=True, backgroundModeSwitch=True)
     ),

@@ -52,7 +52,7 @@ def reference_spread(fx):
     from oracle import ptyoracle as O
 
     st = O.run_fixture(fx, dtype=np.complex128)
-    keys = ("object", "probe", "error", "errorAtPos", "background", "intensityScaling")
+    keys = ("object", "probe", "error", "errorAtPos", "background", "intensityScaling", "reference")
     return {k: rel_err(fx[f"out_{k}"], getattr(st, k)) for k in keys if f"out_{k}" in fx}
 
 
@@ -84,6 +84,10 @@ def test_engine_matches_reference_fixture(torch_cuda, name):
     if "objectMomentum" in target:
         assert rel_err(rec.objectMomentum, target["objectMomentum"]) < max(1e-2, 3 * floor["object"])
         assert rel_err(rec.probeMomentum, target["probeMomentum"]) < max(1e-2, 3 * floor["probe"])
+    if "out_reference" in fx:
+        # the interferometric reference field (BaseEngine.py:975-982), per mode
+        assert rec.reference.shape == fx["out_reference"].shape
+        assert rel_err(rec.reference, fx["out_reference"]) < max(TOL_FIXTURE, 3 * floor["reference"])
     for key in ("background", "intensityScaling"):
         if f"out_{key}" in fx and platform_reproduces_order(fx):
             got = rec.background if key == "background" else run_fixture_gpu.params.intensityScaling
@@ -132,13 +136,17 @@ def test_stepwise_equals_reconstruct(torch_cuda):
 def test_unsupported_switch_raises(torch_cuda):
     from ptylab_gb300 import DummyMonitor, Engines
 
-    fx = load_fixture("reg_epie_fraunhofer")
+    fx = load_fixture("scan_epie_asp")
     m, i, d, p, rec = containers(fx)
     rec.object, rec.probe = i["init_object"].copy(), i["init_probe"].copy()
-    p.intensityConstraint = "interferometric"
+    p.intensityConstraint = "interferometric"  # with ASP: not on this path
     eng = Engines.ePIE(rec, d, p, DummyMonitor())
     with pytest.raises(NotImplementedError):
         eng.reconstruct()
+    p.propagatorType = "Fraunhofer"
+    rec.initialGuessObject, rec.initialGuessProbe = i["init_object"].copy(), i["init_probe"].copy()
+    with pytest.raises(NotImplementedError):  # with mqNewton: not on this path
+        Engines.mqNewton(rec, d, p, DummyMonitor()).reconstruct()
     p.intensityConstraint = "sigmoid"  # not a constraint PtyLab knows (BaseEngine.py:963-964)
     with pytest.raises(ValueError):
         Engines.ePIE(rec, d, p, DummyMonitor()).reconstruct()

@@ -34,7 +34,8 @@ def test_oracle_reproduces_reference(name):
     if "out_objectMomentum" in fx:
         np.testing.assert_allclose(st.objectMomentum, fx["out_objectMomentum"], rtol=1e-5, atol=1e-7)
         np.testing.assert_allclose(st.probeMomentum, fx["out_probeMomentum"], rtol=1e-5, atol=1e-7)
-    for key in ("objectBuffer", "probeBuffer", "objectMomentum_v", "probeMomentum_v", "background", "intensityScaling"):
+    for key in ("objectBuffer", "probeBuffer", "objectMomentum_v", "probeMomentum_v", "background", "intensityScaling",
+                "reference"):
         if f"out_{key}" in fx:
             np.testing.assert_allclose(getattr(st, key), fx[f"out_{key}"], rtol=1e-5, atol=1e-7, err_msg=key)
 
