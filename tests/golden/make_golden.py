@@ -414,6 +414,17 @@ SCAN_CONFIGS = {
     "mpie_interferometric_modes": dict(
         engine="mPIE", modes=(1, 1, 2, 1), iters=3, params=dict(intensityConstraint="interferometric")
     ),
+    # ... uncentred transforms (no centring sign on the field), Fresnel, and
+    # three wavelengths (one field per wavelength and mode)
+    "qnewton_interferometric_fftshift": dict(
+        engine="qNewton", fftshift=True, iters=3, params=dict(intensityConstraint="interferometric")
+    ),
+    "epie_interferometric_fresnel": dict(
+        engine="ePIE", propagator="Fresnel", iters=3, params=dict(intensityConstraint="interferometric")
+    ),
+    "epie_interferometric_polychrome": dict(
+        engine="ePIE", modes=(3, 1, 1, 1), iters=3, params=dict(intensityConstraint="interferometric")
+    ),
     "epie_asp_denoise_background": dict(
         engine="ePIE", propagator="ASP", iters=3, params=dict(adaptiveDenoisingSwitch=True, backgroundModeSwitch=True)
     ),
