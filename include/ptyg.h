@@ -158,7 +158,7 @@ typedef struct ptyg_geometry {
                           1: most positions per second over many scans (16
                           rows per CTA: fewer CTAs per scan, more scans at once) */
   int32_t nlambda;     /* wavelengths (reconstruction.nlambda; 0 reads as 1).  Above
-                          1 (ePIE, mPIE, qNewton): object (nlambda, nosm, ...)
+                          1 (ePIE, mPIE, qNewton, mqNewton): object (nlambda, nosm, ...)
                           and probe (nlambda, npsm, ...) wavelength-major, exit
                           waves O_(l,o) P_(l,p) of each wavelength l, the ASP
                           table one per wavelength (polychromeASP,

@@ -110,8 +110,8 @@ class BaseEngine(object):
         if getattr(p, "comStabilizationSwitch", None) not in (None, False):
             raise NotImplementedError("params.comStabilizationSwitch is not supported by the GB300 engines")
         nl = int(getattr(rec, "nlambda", 1))
-        if nl != 1 and self.engine_name not in ("ePIE", "mPIE", "qNewton"):
-            raise NotImplementedError(f"nlambda = {nl}: several wavelengths run with the GB300 ePIE, mPIE and qNewton")
+        if nl != 1 and self.engine_name not in ("ePIE", "mPIE", "qNewton", "mqNewton"):
+            raise NotImplementedError(f"nlambda = {nl}: several wavelengths run with the GB300 ePIE, mPIE, qNewton and mqNewton")
         if nl != 1 and getattr(p, "orthogonalizationSwitch", False):
             raise NotImplementedError("orthogonalizationSwitch with several wavelengths is not on this path")
         kind = p.propagatorType.lower()

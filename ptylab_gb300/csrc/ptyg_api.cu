@@ -397,8 +397,9 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   ptyg_geometry g = *geometry;
   if (g.nlambda == 0) g.nlambda = 1;
   if (g.nlambda < 1) return fail(PTYG_ERR_INVALID, "nlambda=%d", g.nlambda);
-  if (g.nlambda > 1 && g.engine != PTYG_EPIE && g.engine != PTYG_MPIE && g.engine != PTYG_QNEWTON)
-    return fail(PTYG_ERR_UNSUPPORTED, "nlambda=%d: several wavelengths run with ePIE, mPIE and qNewton only",
+  if (g.nlambda > 1 && g.engine != PTYG_EPIE && g.engine != PTYG_MPIE && g.engine != PTYG_QNEWTON &&
+      g.engine != PTYG_MQNEWTON)
+    return fail(PTYG_ERR_UNSUPPORTED, "nlambda=%d: several wavelengths run with ePIE, mPIE, qNewton and mqNewton",
                 g.nlambda);
   if (g.threads != 0 &&
       (g.threads % 32 != 0 || g.threads < 128 || g.threads > (g.engine == PTYG_MQNEWTON ? 256 : 512)))

@@ -29,13 +29,16 @@ bool engine_shape_supported(int Np, int cluster) {
 
 cudaError_t engine_max_clusters(int Np, int engine, int nlambda, int cluster, int threads, size_t smem, int* out) {
   // (the several-wavelength instantiation serves ePIE, mPIE and qNewton)
-  if (engine == ENG_MQNEWTON) return engine_max_clusters_mq(Np, cluster, threads, smem, out);
+  if (engine == ENG_MQNEWTON)
+    return nlambda > 1 ? engine_max_clusters_mq_poly(Np, cluster, threads, smem, out)
+                       : engine_max_clusters_mq(Np, cluster, threads, smem, out);
   if (nlambda > 1) return engine_max_clusters_poly(Np, cluster, threads, smem, out);
   return engine_max_clusters_t<VAR_STD>(Np, cluster, threads, smem, out);
 }
 
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st) {
-  if (a.engine == ENG_MQNEWTON) return launch_engine_mq(a, nscans, threads, smem, st);
+  if (a.engine == ENG_MQNEWTON)
+    return a.nlambda > 1 ? launch_engine_mq_poly(a, nscans, threads, smem, st) : launch_engine_mq(a, nscans, threads, smem, st);
   if (a.nlambda > 1 || a.iconstraint == IC_INTERFEROMETRIC) return launch_engine_poly(a, nscans, threads, smem, st);
   return launch_engine_t<VAR_STD>(a, nscans, threads, smem, st);
 }

@@ -324,11 +324,14 @@ __host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int n
 // E: Np / 32 points per lane; L: rows (and Fourier columns) per CTA, so the
 // cluster has C = Np / L CTAs.  Both compile-time so index arithmetic is shifts.
 // VAR: VAR_MQ is the mqNewton instantiation (engine == ENG_MQNEWTON), VAR_POLY
-// ePIE over several wavelengths, VAR_STD ePIE / mPIE / qNewton at one.
-enum { VAR_STD = 0, VAR_MQ = 1, VAR_POLY = 2 };
+// ePIE / mPIE / qNewton over several wavelengths, VAR_STD ePIE / mPIE /
+// qNewton at one, VAR_MQ_POLY mqNewton over several wavelengths.
+enum { VAR_STD = 0, VAR_MQ = 1, VAR_POLY = 2, VAR_MQ_POLY = 3 };
 template <int E, int L, int VAR>
-__global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(const EngineArgs a) {
-  constexpr bool MQ = VAR == VAR_MQ;
+__global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 512, 1)
+    engine_kernel(const EngineArgs a) {
+  constexpr bool MQ = VAR == VAR_MQ || VAR == VAR_MQ_POLY;
+  constexpr bool POLY = VAR == VAR_POLY || VAR == VAR_MQ_POLY;
   // (512 threads x 128 registers: one CTA of 16 warps, or two of 8 warps, per
   // SM; mqNewton: at most 256 threads, so its momentum pass keeps all of a
   // tile's loads in registers)
@@ -343,7 +346,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
   // object and probe modes of every wavelength (wavelength-major); an exit
   // wave k = (l * nosmW + o) * npsmW + p pairs object mode l * nosmW + o with
   // probe mode l * npsmW + p of the same wavelength l
-  const int nl = VAR == VAR_POLY ? a.nlambda : 1;  // a compile-time 1 outside VAR_POLY
+  const int nl = POLY ? a.nlambda : 1;  // a compile-time 1 outside the several-wavelength instantiations
   const int nosmW = a.nosm, npsmW = a.npsm;
   const int nosm = nl * nosmW, npsm = nl * npsmW, K = nl * nosmW * npsmW, No = a.No;
   const bool centred = a.centred != 0;
@@ -705,7 +708,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
           [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm.rows, v, t / L, sx0 + t % L); });
     } else {
       // ---------------- ASP: x H, real-space projection, x conj(H)
-      column_filter<E, L, VAR == VAR_POLY>(sm.tile, sm.rows, F, a.aspH, false, crank, K, nosmW * npsmW);
+      column_filter<E, L, POLY>(sm.tile, sm.rows, F, a.aspH, false, crank, K, nosmW * npsmW);
       cluster_sync(C);
       fft_tasks<E, true>(
           F, K * L,
@@ -740,7 +743,7 @@ __global__ void __launch_bounds__(VAR == VAR_MQ ? 256 : 512, 1) engine_kernel(co
           },
           [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm.tile, v, t / L, line0 + t % L); });
       cluster_sync(C);
-      column_filter<E, L, VAR == VAR_POLY>(sm.tile, sm.rows, F, a.aspH, true, crank, K, nosmW * npsmW);
+      column_filter<E, L, POLY>(sm.tile, sm.rows, F, a.aspH, true, crank, K, nosmW * npsmW);
     }
     {
       __syncthreads();  // sm.redD may still be read by the projection's cluster sums
@@ -1159,7 +1162,8 @@ cudaError_t clusters_t(int threads, size_t smem, int* out) {
 
 // Launch / occupancy over the instantiated shapes for one variant; each
 // translation unit instantiates one (ptyg_engine.cu: VAR_STD,
-// ptyg_engine_mq.cu: VAR_MQ, ptyg_engine_poly.cu: VAR_POLY).
+// ptyg_engine_mq.cu: VAR_MQ, ptyg_engine_poly.cu: VAR_POLY,
+// ptyg_engine_mq_poly.cu: VAR_MQ_POLY).
 template <int VAR>
 cudaError_t engine_max_clusters_t(int Np, int cluster, int threads, size_t smem, int* out) {
   *out = 0;

@@ -390,6 +390,9 @@ SCAN_CONFIGS = {
         params=dict(orthogonalizationSwitch=True, orthogonalizationFrequency=2),
     ),
     "mqnewton_momentum": dict(engine="mqNewton", iters=3, engine_attrs=dict(momentum_method="momentum")),
+    # mqNewton over three wavelengths: qNewton's steps summed over them
+    # (mqNewton.py:226-251), the adaptive momentum on every wavelength's copy
+    "mqnewton_polychrome": dict(engine="mqNewton", order="random", modes=(3, 1, 2, 1), iters=3),
     # intensity-projection switches (BaseEngine.py:870-1012, 1805-1822)
     # the unsquared constraints need an initial probe of the data's power
     "epie_poission": dict(

@@ -178,9 +178,9 @@ def test_reconstruct_batch_rejects_mismatched_engines():
 
 
 def test_several_wavelengths_are_checked_before_device_work():
-    """nlambda > 1 runs with ePIE, mPIE and qNewton; ASP refuses it as
-    PtyLab's does (Operators.py:866-869) and polychromeASP needs a wavelength
-    per slot."""
+    """nlambda > 1 runs with ePIE, mPIE, qNewton and mqNewton (not e3PIE);
+    ASP refuses it as PtyLab's does (Operators.py:866-869) and polychromeASP
+    needs a wavelength per slot."""
     from ptylab_gb300 import DummyMonitor, Engines
 
     def setup(engine, propagator, spectral=True):
@@ -193,8 +193,7 @@ def test_several_wavelengths_are_checked_before_device_work():
         rec.initialGuessObject, rec.initialGuessProbe = rec.object.copy(), rec.probe.copy()
         return getattr(Engines, engine)(rec, d, p, DummyMonitor())
 
-    with pytest.raises(NotImplementedError):
-        setup("mqNewton", "polychromeASP")._check_supported()
+    setup("mqNewton", "polychromeASP")._check_supported()
     setup("mPIE", "polychromeASP")._check_supported()
     setup("qNewton", "polychromeASP")._check_supported()
     with pytest.raises(ValueError):
