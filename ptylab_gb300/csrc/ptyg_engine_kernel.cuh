@@ -870,10 +870,16 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
             }
           }
           if (mq) {
-            const float2 d = csub(s.probeBuffer[(size_t)p * NP * NP + (size_t)line0 * NP + i], P);
-            tdd = __fadd_rn(tdd, __fmaf_rn(d.x, d.x, __fmul_rn(d.y, d.y)));
-            tdu = __fadd_rn(tdu, __fmaf_rn(d.x, accP.x, __fmul_rn(d.y, accP.y)));
-            tuu = __fadd_rn(tuu, __fmaf_rn(accP.x, accP.x, __fmul_rn(accP.y, accP.y)));
+            // the probe gradient's norm covers every wavelength's copy: each
+            // takes the same numerator U (mqNewton.py:205-215 on the whole probe)
+            for (int w = 0; w < nl; ++w) {
+              const int pw = w * npsmW + p;
+              const float2 Pw = nl == 1 ? P : sm.probe[pw * pst + i];
+              const float2 d = csub(s.probeBuffer[(size_t)pw * NP * NP + (size_t)line0 * NP + i], Pw);
+              tdd = __fadd_rn(tdd, __fmaf_rn(d.x, d.x, __fmul_rn(d.y, d.y)));
+              tdu = __fadd_rn(tdu, __fmaf_rn(d.x, accP.x, __fmul_rn(d.y, accP.y)));
+              tuu = __fadd_rn(tuu, __fmaf_rn(accP.x, accP.x, __fmul_rn(accP.y, accP.y)));
+            }
           }
         }
         const int l = i / NP, x = i - (i / NP) * NP;
@@ -993,7 +999,8 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
           const int p = i / LN, rem = i - (i / LN) * LN;
           const size_t gi = (size_t)p * NP * NP + (size_t)line0 * NP + rem;
-          const float2 P = cadd(sm.probe[p * pst + rem], cscale(sm.U[i], scale));
+          const int pu = nl == 1 ? p : p % npsmW;  // every wavelength takes U summed over them
+          const float2 P = cadd(sm.probe[p * pst + rem], cscale(sm.U[pu * LN + rem], scale));
           const float2 g = csub(s.probeBuffer[gi], P);
           float2 M = s.probeMomentum[gi];
           float2 Pn;

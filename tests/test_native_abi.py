@@ -119,10 +119,10 @@ def test_new_entry_points_reject_bad_arguments_before_touching_a_device(lib):
     assert lib.ptyg_propagate_sets(0, 0, 64, 4, 1, dummy, dummy, dummy, dummy, None, None) == _native.PTYG_ERR_UNSUPPORTED
     assert lib.ptyg_propagate_sets(5, 0, 64, 4, 1, dummy, dummy, dummy, None, None, None) == _native.PTYG_ERR_INVALID
     assert lib.ptyg_propagate_sets(6, 0, 48, 4, 1, dummy, dummy, dummy, dummy, None, None) == _native.PTYG_ERR_UNSUPPORTED
-    # several wavelengths: not with mqNewton; CTA sizes: multiples of 32 in range
+    # several wavelengths: not with e3PIE; CTA sizes: multiples of 32 in range
     plan = C.c_void_p()
     g = _native.Geometry(Np=64, No=128, nosm=1, npsm=1, nslice=1, num_frames=4, num_scans=1,
-                         engine=_native.ENGINES["mqNewton"], nlambda=2)
+                         engine=_native.ENGINES["e3PIE"], nlambda=2)
     assert lib.ptyg_plan_create(C.byref(g), C.byref(plan)) == _native.PTYG_ERR_UNSUPPORTED
     assert b"wavelengths" in lib.ptyg_last_error()
     for threads in (100, 64, 1024):
