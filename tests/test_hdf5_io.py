@@ -32,7 +32,7 @@ def golden():
 
 
 def test_lookup3_published_vectors():
-    # the driver vectors of Bob Jenkins' lookup3.c
+    # the self-test vectors of Bob Jenkins' lookup3.c
     assert hdf5.lookup3(b"") == 0xDEADBEEF
     assert hdf5.lookup3(b"Four score and seven years ago") == 0x17770551
     assert hdf5.lookup3(b"Four score and seven years ago", 1) == 0xCD628161
