@@ -1,0 +1,187 @@
+"""The reader on the newer on-disk structures (what libhdf5 writes with
+libver="latest"): superblock version 2, version-2 object headers with their
+checksums and a continuation block, compact link messages, dataspace
+version 2, fill value version 3, layout version 4 (contiguous, and chunked
+with the single-chunk, implicit and fixed-array indexes), filter pipeline
+version 2, attribute version 3.  No file of this kind exists here, so a
+test-only encoder builds them from the published format specification; the
+checks are that every structure parses and every value comes back."""
+
+from __future__ import annotations
+
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+from ptylab_gb300.io import hdf5
+
+U = hdf5.UNDEF
+
+
+def ohdr(messages, continuation=None):
+    """A version-2 object header (4-byte chunk size field)."""
+    body = b"".join(struct.pack("<BHB", t, len(d), f) + d for t, d, f in messages)
+    if continuation is not None:
+        body += struct.pack("<BHB", hdf5.MSG_CONTINUATION, 16, 0) + struct.pack("<QQ", *continuation)
+    head = b"OHDR" + struct.pack("<BBI", 2, 2, len(body))
+    blob = head + body
+    return blob + struct.pack("<I", hdf5.lookup3(blob))
+
+
+def ochk(messages):
+    body = b"OCHK" + b"".join(struct.pack("<BHB", t, len(d), f) + d for t, d, f in messages)
+    return body + struct.pack("<I", hdf5.lookup3(body))
+
+
+def dataspace2(shape):
+    return struct.pack("<BBBB", 2, len(shape), 0, 1 if shape else 0) + b"".join(struct.pack("<Q", n) for n in shape)
+
+
+def link(name, addr):
+    nb = name.encode()
+    return struct.pack("<BBB", 1, 0, len(nb)) + nb + struct.pack("<Q", addr)
+
+
+FILL3 = struct.pack("<BB", 3, 0x0A)
+
+
+class Builder:
+    def __init__(self):
+        self.buf = bytearray(48)  # superblock v2, written last
+
+    def put(self, blob, align=8):
+        self.buf += b"\0" * ((-len(self.buf)) % align)
+        a = len(self.buf)
+        self.buf += blob
+        return a
+
+    def reserve(self, n):
+        return self.put(b"\0" * n)
+
+    def finish(self, root):
+        sb = hdf5.SIGNATURE + struct.pack("<BBBB", 2, 8, 8, 0) + struct.pack("<QQQQ", 0, U, len(self.buf), root)
+        sb += struct.pack("<I", hdf5.lookup3(sb))
+        self.buf[:48] = sb
+        return bytes(self.buf)
+
+
+def dataset(b, arr, layout, extra=()):
+    msgs = [(hdf5.MSG_DATASPACE, dataspace2(arr.shape), 0),
+            (hdf5.MSG_DATATYPE, hdf5._encode_datatype(arr.dtype), 1),
+            (hdf5.MSG_FILL, FILL3, 1)]
+    msgs += list(extra)
+    msgs.append((hdf5.MSG_LAYOUT, layout, 0))
+    return b.put(ohdr(msgs))
+
+
+@pytest.fixture(scope="module")
+def v2file(tmp_path_factory):
+    rng = np.random.default_rng(11)
+    want = {}
+    b = Builder()
+    # contiguous
+    a = rng.standard_normal((5, 7)).astype(np.float32)
+    addr = b.put(a.tobytes())
+    objs = {"contig": dataset(b, a, struct.pack("<BBQQ", 4, 1, addr, a.nbytes))}
+    want["contig"] = a
+    # single chunk, deflate through a version-2 pipeline
+    c = (rng.standard_normal((6, 4)) + 1j * rng.standard_normal((6, 4))).astype(np.complex64)
+    raw = zlib.compress(c.tobytes(), 6)
+    caddr = b.put(raw)
+    lay = struct.pack("<BBBBB", 4, 2, 0x02, 3, 4) + struct.pack("<III", 6, 4, 8) + struct.pack("<B", 1)
+    lay += struct.pack("<QI", len(raw), 0) + struct.pack("<Q", caddr)
+    pipe = struct.pack("<BB", 2, 1) + struct.pack("<HHH", hdf5.FILTER_DEFLATE, 1, 1) + struct.pack("<I", 6)
+    objs["single_chunk_gzip"] = dataset(b, c, lay, [(hdf5.MSG_PIPELINE, pipe, 0)])
+    want["single_chunk_gzip"] = c
+    # implicit index: unfiltered chunks in row-major order, edge chunks full size
+    m = np.arange(7 * 10, dtype=np.int32).reshape(7, 10)
+    chunk = (3, 4)
+    grid = (3, 3)
+    blocks = b""
+    for i in range(grid[0]):
+        for j in range(grid[1]):
+            blk = np.zeros(chunk, np.int32)
+            part = m[i * 3:(i + 1) * 3, j * 4:(j + 1) * 4]
+            blk[: part.shape[0], : part.shape[1]] = part
+            blocks += blk.tobytes()
+    iaddr = b.put(blocks)
+    lay = struct.pack("<BBBBB", 4, 2, 0, 3, 4) + struct.pack("<III", 3, 4, 4) + struct.pack("<B", 2) + struct.pack("<Q", iaddr)
+    objs["implicit"] = dataset(b, m, lay)
+    want["implicit"] = m
+    # fixed-array index, unpaged, unfiltered chunks stored out of order
+    f = rng.standard_normal((4, 6)).astype(np.float64)
+    order = [(1, 1), (0, 0), (1, 0), (0, 1)]
+    where = {}
+    for i, j in order:
+        where[(i, j)] = b.put(np.ascontiguousarray(f[i * 2:(i + 1) * 2, j * 3:(j + 1) * 3]).tobytes())
+    elems = b"".join(struct.pack("<Q", where[(i, j)]) for i in range(2) for j in range(2))
+    fahd_addr = len(b.buf) + ((-len(b.buf)) % 8)
+    fahd_len = 4 + 4 + 8 + 8 + 4
+    fadb = b"FADB" + struct.pack("<BBQ", 0, 0, fahd_addr) + elems
+    fadb += struct.pack("<I", hdf5.lookup3(fadb))
+    fahd = b"FAHD" + struct.pack("<BBBB", 0, 0, 8, 10) + struct.pack("<Q", 4)
+    fadb_addr = fahd_addr + fahd_len
+    fahd += struct.pack("<Q", fadb_addr)
+    fahd += struct.pack("<I", hdf5.lookup3(fahd))
+    assert b.put(fahd) == fahd_addr and len(fahd) == fahd_len
+    assert b.put(fadb, align=1) == fadb_addr
+    lay = struct.pack("<BBBBB", 4, 2, 0, 3, 4) + struct.pack("<III", 2, 3, 8) + struct.pack("<BB", 3, 10)
+    lay += struct.pack("<Q", fahd_addr)
+    objs["fixed_array"] = dataset(b, f, lay)
+    want["fixed_array"] = f
+    # a scalar with a version-3 attribute
+    s = np.array(2.5)
+    saddr = b.put(s.tobytes())
+    name = b"units"
+    tdt = struct.pack("<B3sI", 0x13, (0).to_bytes(3, "little"), 6)
+    sds = dataspace2(())
+    attr = struct.pack("<BBHHHB", 3, 0, len(name), len(tdt), len(sds), 0) + name + tdt + sds + b"metres"
+    objs["scalar"] = dataset(b, s, struct.pack("<BBQQ", 4, 1, saddr, 8), [(hdf5.MSG_ATTRIBUTE, attr, 0)])
+    want["scalar"] = s
+    # a subgroup with one link, and the root group: links split across a continuation block
+    sub_ds = dataset(b, a, struct.pack("<BBQQ", 4, 1, addr, a.nbytes))
+    li = struct.pack("<BBQQ", 0, 0, U, U)
+    gi = struct.pack("<BB", 0, 0)
+    sub = b.put(ohdr([(hdf5.MSG_LINK_INFO, li, 0), (hdf5.MSG_GROUP_INFO, gi, 0), (hdf5.MSG_LINK, link("inner", sub_ds), 0)]))
+    names = sorted(objs)
+    first, rest = names[:2], names[2:]
+    cont = ochk([(hdf5.MSG_LINK, link(n, objs[n]), 0) for n in rest] + [(hdf5.MSG_LINK, link("group", sub), 0)])
+    caddr = b.put(cont)
+    root = b.put(ohdr([(hdf5.MSG_LINK_INFO, li, 0), (hdf5.MSG_GROUP_INFO, gi, 0)]
+                      + [(hdf5.MSG_LINK, link(n, objs[n]), 0) for n in first], continuation=(caddr, len(cont))))
+    path = tmp_path_factory.mktemp("v2") / "latest.h5"
+    path.write_bytes(b.finish(root))
+    return path, want
+
+
+def test_v2_structures_read_back(v2file):
+    path, want = v2file
+    with hdf5.File(path) as f:
+        assert f.keys() == sorted(list(want) + ["group"])
+        for k, v in want.items():
+            got = f[k][()]
+            assert got.shape == v.shape and got.dtype == v.dtype, k
+            np.testing.assert_array_equal(got, v, err_msg=k)
+        assert f["scalar"].attrs == {"units": b"metres"}
+        np.testing.assert_array_equal(f["group/inner"][()], want["contig"])
+        assert "group/inner" in f and "group/missing" not in f
+
+
+def test_v2_checksums_are_checked(v2file, tmp_path):
+    path, _ = v2file
+    buf = bytearray(path.read_bytes())
+    bad = tmp_path / "bad_superblock.h5"
+    buf2 = bytearray(buf)
+    buf2[12] ^= 0xFF  # base address byte inside the checksummed superblock
+    bad.write_bytes(bytes(buf2))
+    with pytest.raises(hdf5.HDF5FormatError):
+        hdf5.File(bad)
+    i = buf.find(b"OCHK")
+    buf3 = bytearray(buf)
+    buf3[i + 6] ^= 0x01  # inside the continuation block's first message
+    bad2 = tmp_path / "bad_continuation.h5"
+    bad2.write_bytes(bytes(buf3))
+    with pytest.raises(hdf5.HDF5FormatError):
+        hdf5.File(bad2)
