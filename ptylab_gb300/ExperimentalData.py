@@ -94,6 +94,29 @@ class ExperimentalData:
         if force_contiguous:
             self.ptychogram = np.ascontiguousarray(self.ptychogram)
 
+    def reduce_positions(self, start, end):
+        """Keep frames and encoder rows [start, end) (ExperimentalData.py:151-156)."""
+        self.ptychogram = self.ptychogram[start:end]
+        self.encoder = self.encoder[start:end]
+
+    def cropCenter(self, size):
+        """Crop every frame to size x size about the centre, starting one
+        pixel past N // 2 - size // 2 as PtyLab does (ExperimentalData.py:158-171)."""
+        if not isinstance(size, int):
+            raise TypeError("Crop value is not valid. Int expected")
+        first = self.ptychogram.shape[-1] // 2 - size // 2 + 1
+        self.ptychogram = self.ptychogram[..., first:first + size, first:first + size]
+
+    def binData(self, binning):
+        """Average binning x binning pixel blocks of every frame into a float64
+        ptychogram (ExperimentalData.py:173-190)."""
+        n, ny, nx = self.ptychogram.shape
+        frames = np.copy(self.ptychogram)
+        out = np.zeros((n, ny // binning, nx // binning))
+        for f in range(n):
+            out[f] = frames[f].reshape(ny // binning, binning, nx // binning, binning).mean(axis=(1, 3))
+        self.ptychogram = out
+
     def _setData(self):
         """Derived detector quantities (ExperimentalData.py:234-250)."""
         self.Nd = self.ptychogram.shape[-1]

@@ -214,6 +214,14 @@ def main():
                 out[f"{tag}/{field}"] = np.asarray(v)
         out[f"{tag}/none"] = np.array(none)
 
+    # data preparation on a loaded file (ExperimentalData.py:151-190)
+    for step, call in (("reduce", lambda e: e.reduce_positions(1, 5)), ("crop", lambda e: e.cropCenter(10)),
+                       ("crop_odd", lambda e: e.cropCenter(7)), ("bin", lambda e: e.binData(2))):
+        ed = ref_ed.ExperimentalData(str(OUT_DIR / "cpm_simulation.hdf5"), operationMode="CPM")
+        call(ed)
+        out[f"prep_{step}/ptychogram"] = np.asarray(ed.ptychogram)
+        out[f"prep_{step}/encoder"] = np.asarray(ed.encoder)
+
     attrs = result_inputs()
     ns = types.SimpleNamespace(**attrs)
     ns.data = types.SimpleNamespace(operationMode="CPM")

@@ -390,3 +390,19 @@ def test_easy_initialize_from_files():
     assert params.positionOrder == "NA" and params.probeBoundary
     with pytest.raises(NotImplementedError):
         P.easyInitialize(str(INPUTS / "cpm_simulation.hdf5"), operationMode="XYZ")
+
+
+@pytest.mark.parametrize("step", ["reduce", "crop", "crop_odd", "bin"])
+def test_data_preparation_matches_reference(golden, step):
+    """reduce_positions / cropCenter / binData on a loaded file, against the
+    reference's ExperimentalData on the same file (ExperimentalData.py:151-190)."""
+    ed = ExperimentalData(str(INPUTS / "cpm_simulation.hdf5"))
+    {"reduce": lambda: ed.reduce_positions(1, 5), "crop": lambda: ed.cropCenter(10),
+     "crop_odd": lambda: ed.cropCenter(7), "bin": lambda: ed.binData(2)}[step]()
+    for key in ("ptychogram", "encoder"):
+        want = golden[f"prep_{step}/{key}"]
+        got = np.asarray(getattr(ed, key))
+        assert got.dtype == want.dtype and got.shape == want.shape
+        np.testing.assert_array_equal(got, want)
+    with pytest.raises(TypeError):
+        ed.cropCenter(4.0)
