@@ -17,7 +17,8 @@ reading
   * dataspaces (scalar, simple, null), datatypes: integers, IEEE floats,
     fixed-length strings, bitfields, opaque, compounds (complex numbers
     stored as {r, i} or {real, imag} become numpy complex), enums (h5py's
-    booleans become numpy bool), arrays;
+    booleans become numpy bool), arrays, variable-length strings (str) and
+    sequences (numpy arrays) from the global heap;
   * layouts: compact, contiguous, chunked with a version-1 B-tree index or
     (layout version 4) a single chunk, an implicit index or an unpaged fixed
     array; filters deflate, shuffle and fletcher32;
@@ -28,8 +29,8 @@ writing
     dataset per name: the classic layout libhdf5 itself writes with its
     default format settings, so h5py, PyTables and MATLAB read it.
 
-Anything outside this subset (variable-length data, dense link storage,
-other filters or chunk indexes) raises ``NotImplementedError`` naming it.
+Anything outside this subset (dense link storage, other filters or chunk
+indexes) raises ``NotImplementedError`` naming it.
 """
 
 from __future__ import annotations
@@ -244,8 +245,15 @@ def _decode_datatype(cur: _Cursor, reader=None) -> np.dtype:
         if base.itemsize == 1 and dict(zip(mnames, values)) == {b"FALSE": 0, b"TRUE": 1}:
             return np.dtype(np.bool_)
         return base
-    if cls == 9:
-        raise NotImplementedError("variable-length datatypes (strings or sequences)")
+    if cls == 9:  # variable length: each element is (length, global heap id)
+        kind = bits & 0x0F  # 0 sequence, 1 string
+        charset = (bits >> 8) & 0x0F
+        base = _decode_datatype(cur, reader)
+        so = size - 8
+        if so not in (2, 4, 8):
+            raise HDF5FormatError(f"variable-length element of {size} bytes")
+        return np.dtype([("len", "<u4"), ("addr", f"<u{so}"), ("idx", "<u4")],
+                        metadata={"vlen": "str" if kind == 1 else "seq", "base": base, "charset": charset})
     if cls == 10:  # array
         ndims = cur.u(1)
         if version < 3:
@@ -256,6 +264,10 @@ def _decode_datatype(cur: _Cursor, reader=None) -> np.dtype:
         base = _decode_datatype(cur, reader)
         return np.dtype((base, dims))
     raise NotImplementedError(f"datatype class {cls}")
+
+
+def _is_vlen(dt) -> bool:
+    return dt.metadata is not None and "vlen" in dt.metadata
 
 
 def _as_complex(arr: np.ndarray) -> np.ndarray:
@@ -577,6 +589,50 @@ class _Reader:
             return None
         return tuple(c.u(self.sl) for _ in range(rank))
 
+    def global_heap_object(self, addr, index):
+        """Object ``index`` of the global heap collection at ``addr``."""
+        cache = self.__dict__.setdefault("_gcol", {})
+        if addr not in cache:
+            head = self.cursor(addr, 8 + self.sl)
+            if head.raw(4) != b"GCOL":
+                raise HDF5FormatError("bad global heap signature")
+            head.skip(4)
+            size = head.u(self.sl)
+            c = self.cursor(addr, size)
+            c.skip(8 + self.sl)
+            objs = {}
+            while c.pos + 8 + self.sl <= size:
+                idx = c.u(2)
+                c.skip(6)
+                n = c.u(self.sl)
+                if idx == 0:
+                    break
+                objs[idx] = c.raw(n)
+                c.skip((-n) % 8)
+            cache[addr] = objs
+        try:
+            return cache[addr][index]
+        except KeyError:
+            raise HDF5FormatError(f"global heap object {index} missing") from None
+
+    def resolve_vlen(self, arr):
+        """(length, heap id) records -> an object array of str (strings) or
+        numpy arrays of the base type (sequences)."""
+        meta = arr.dtype.metadata
+        base = meta["base"]
+        out = np.empty(arr.shape, dtype=object)
+        flat = arr.reshape(-1)
+        res = out.reshape(-1)
+        for k in range(flat.size):
+            n, addr, idx = int(flat[k]["len"]), int(flat[k]["addr"]), int(flat[k]["idx"])
+            if meta["vlen"] == "str":
+                raw = self.global_heap_object(addr, idx)[:n] if n else b""
+                res[k] = raw.rstrip(b"\0").decode("utf-8" if meta["charset"] == 1 else "ascii", errors="replace")
+            else:
+                raw = self.global_heap_object(addr, idx) if n else b""
+                res[k] = np.frombuffer(raw, dtype=base, count=n).copy()
+        return out
+
     def read_fill(self, msgs, dtype):
         for m in msgs:
             if m.type == MSG_FILL:
@@ -656,7 +712,10 @@ class _Reader:
                 raise HDF5FormatError(f"layout class {cls}")
         else:
             raise NotImplementedError(f"layout message version {version}")
-        return _as_complex(np.asarray(arr).reshape(shape))
+        arr = np.asarray(arr).reshape(shape)
+        if _is_vlen(dtype):
+            return self.resolve_vlen(arr)
+        return _as_complex(arr)
 
     def _contiguous(self, addr, nbytes, dtype, nelem):
         if self.undef(addr):  # storage never allocated: all fill value
@@ -864,6 +923,10 @@ class _Reader:
                 continue
             n = int(np.prod(shape, dtype=np.int64)) if shape else 1
             val = np.frombuffer(c.raw(n * dt.itemsize), dtype=dt, count=n).reshape(shape)
+            if _is_vlen(dt):
+                v = self.resolve_vlen(val)
+                attrs[name] = v[()] if shape == () else v
+                continue
             val = _as_complex(val)
             attrs[name] = val[()] if shape == () else val.copy()
         return attrs
@@ -888,7 +951,8 @@ class Dataset:
     def dtype(self):
         for m in self._msgs:
             if m.type == MSG_DATATYPE:
-                return _as_complex(np.empty(0, self._reader.datatype(m))).dtype
+                dt = self._reader.datatype(m)
+                return np.dtype(object) if _is_vlen(dt) else _as_complex(np.empty(0, dt)).dtype
         raise HDF5FormatError("dataset without a datatype")
 
     def read(self):

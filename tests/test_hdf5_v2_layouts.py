@@ -185,3 +185,65 @@ def test_v2_checksums_are_checked(v2file, tmp_path):
     bad2.write_bytes(bytes(buf3))
     with pytest.raises(hdf5.HDF5FormatError):
         hdf5.File(bad2)
+
+
+def vlen_type(kind, base, charset=0):
+    """Datatype message of a variable-length string (kind 1) or sequence (0)."""
+    bits = kind | (charset << 8)
+    return struct.pack("<B3sI", 0x19, bits.to_bytes(3, "little"), 16) + base
+
+
+def global_heap(objects):
+    """A global heap collection holding ``objects`` (index 1, 2, ...)."""
+    body = b""
+    for i, data in enumerate(objects, start=1):
+        body += struct.pack("<HHIQ", i, 1, 0, len(data)) + data + b"\0" * ((-len(data)) % 8)
+    body += struct.pack("<HHIQ", 0, 0, 0, 0)  # free space
+    size = 16 + len(body)
+    return b"GCOL" + struct.pack("<B3xQ", 1, size) + body
+
+
+def test_variable_length_strings_and_sequences(tmp_path):
+    """h5py writes Python strings as variable-length strings in a global heap;
+    sequences of int32 the same way."""
+    b = Builder()
+    texts = ["LED array, 4 mm pitch", "", "ünïcode"]
+    seqs = [np.arange(3, dtype=np.int32), np.array([7], dtype=np.int32)]
+    heap_objs = [texts[0].encode(), texts[2].encode("utf-8"), seqs[0].tobytes(), seqs[1].tobytes(),
+                 b"metres"]
+    gaddr = b.put(global_heap(heap_objs))
+    u8 = struct.pack("<B3sIHH", 0x10, b"\0\0\0", 1, 0, 8)
+    i32 = hdf5._encode_datatype(np.dtype("<i4"))
+    # 1-D string dataset: (length, collection, index); the empty string has length 0
+    recs = struct.pack("<IQI", len(heap_objs[0]), gaddr, 1) + struct.pack("<IQI", 0, 0, 0) + \
+        struct.pack("<IQI", len(heap_objs[1]), gaddr, 2)
+    saddr = b.put(recs)
+    tstr = vlen_type(1, u8, charset=1)
+    sattr_name = b"units"
+    sds = dataspace2(())
+    attr = struct.pack("<BBHHHB", 3, 0, len(sattr_name), len(tstr), len(sds), 1) + sattr_name + tstr + sds + \
+        struct.pack("<IQI", 6, gaddr, 5)
+    d1 = b.put(ohdr([(hdf5.MSG_DATASPACE, dataspace2((3,)), 0), (hdf5.MSG_DATATYPE, tstr, 1),
+                     (hdf5.MSG_ATTRIBUTE, attr, 0),
+                     (hdf5.MSG_LAYOUT, struct.pack("<BBQQ", 4, 1, saddr, len(recs)), 0)]))
+    recs2 = struct.pack("<IQI", 3, gaddr, 3) + struct.pack("<IQI", 1, gaddr, 4)
+    qaddr = b.put(recs2)
+    d2 = b.put(ohdr([(hdf5.MSG_DATASPACE, dataspace2((2,)), 0), (hdf5.MSG_DATATYPE, vlen_type(0, i32), 1),
+                     (hdf5.MSG_LAYOUT, struct.pack("<BBQQ", 4, 1, qaddr, len(recs2)), 0)]))
+    # a scalar string in compact storage
+    rec3 = struct.pack("<IQI", len(heap_objs[0]), gaddr, 1)
+    d3 = b.put(ohdr([(hdf5.MSG_DATASPACE, dataspace2(()), 0), (hdf5.MSG_DATATYPE, tstr, 1),
+                     (hdf5.MSG_LAYOUT, struct.pack("<BBH", 4, 0, len(rec3)) + rec3, 0)]))
+    li = struct.pack("<BBQQ", 0, 0, U, U)
+    root = b.put(ohdr([(hdf5.MSG_LINK_INFO, li, 0), (hdf5.MSG_LINK, link("comment", d1), 0),
+                       (hdf5.MSG_LINK, link("runs", d2), 0), (hdf5.MSG_LINK, link("title", d3), 0)]))
+    path = tmp_path / "vlen.h5"
+    path.write_bytes(b.finish(root))
+    with hdf5.File(path) as f:
+        got = f["comment"][()]
+        assert got.dtype == object and list(got) == texts
+        assert f["comment"].dtype == np.dtype(object)
+        assert f["comment"].attrs == {"units": "metres"}
+        runs = f["runs"][()]
+        assert len(runs) == 2 and all(np.array_equal(r, s) for r, s in zip(runs, seqs))
+        assert f["title"][()] == texts[0]
