@@ -12,8 +12,9 @@ candidate selection, edge repeats, the radius iteration, the RANSAC fit and
 the encoder update.  The reference treats each LED on its own, so the
 search rounds of all LEDs run together, one batch of kernels per round.
 
-Differences from the reference, by design: plotting (``plot = True``) is
-not available; the RANSAC draws come from a fixed-seed generator, so a
+Differences from the reference, by design: plotting (``plot = True``,
+``plotCalibration``) is not available; frames must be 32, 64, 128 or 256
+pixels square (the sizes of the library's transforms); the RANSAC draws come from a fixed-seed generator, so a
 calibration is reproducible (scikit-image's draws are unseeded); the k-means
 split is two-cluster Lloyd iterations started from the faintest and the
 brightest frame (scikit-learn's KMeans starts from random draws).
@@ -563,6 +564,11 @@ class IlluminationCalibration:
             calibMatrix = SimilarityTransform(np.eye(3))
             updatedPositions = initialPositions
         return calibMatrix, updatedPositions
+
+    def plotCalibration(self, FT_ptychogram, initialPositions, calibrated_positions):
+        """CalibrationFPM.py:667-743 draws the fitted circles with matplotlib;
+        no plotting is available here."""
+        raise NotImplementedError("plotting the calibration is not available")
 
     def fitCoordinates(self, src, dst, mode):
         """CalibrationFPM.py:745-789."""

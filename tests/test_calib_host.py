@@ -191,3 +191,13 @@ def test_calibrated_encoder_reaches_positions_after_reset():
     np.testing.assert_array_equal(rec.positions, g["positions"])  # encoder_corrected untouched
     rec.reset_positioncorrection()
     assert not np.array_equal(rec.positions, g["positions"])
+
+
+def test_refused_sizes_and_plotting():
+    g, settings = load_case(CASES[0])
+    ic, rec, data, oracle = build(g, settings)
+    with pytest.raises(NotImplementedError):
+        ic.plotCalibration(None, None, None)
+    ic.img_size = 96
+    with pytest.raises(NotImplementedError):
+        ic._fourier(np.zeros((2, 96, 96), np.float32))
