@@ -12,8 +12,9 @@ reading
   * object headers version 1 and 2, continuation chunks, committed
     (shared) datatypes;
   * groups stored as symbol tables (version-1 B-tree + local heap; what
-    libhdf5 writes by default, MATLAB 7.3 and PyTables included) and as
-    compact link messages;
+    libhdf5 writes by default, MATLAB 7.3 and PyTables included), as compact
+    link messages and as dense link storage (a fractal heap with a direct or
+    one-level indirect root block, a one-leaf version-2 name index);
   * dataspaces (scalar, simple, null), datatypes: integers, IEEE floats,
     fixed-length strings, bitfields, opaque, compounds (complex numbers
     stored as {r, i} or {real, imag} become numpy complex), enums (h5py's
@@ -29,7 +30,7 @@ writing
     dataset per name: the classic layout libhdf5 itself writes with its
     default format settings, so h5py, PyTables and MATLAB read it.
 
-Anything outside this subset (dense link storage, other filters or chunk
+Anything outside this subset (larger dense groups, other filters or chunk
 indexes) raises ``NotImplementedError`` naming it.
 """
 
@@ -514,13 +515,119 @@ class _Reader:
                 if flags & 1:
                     c.skip(8)
                 fheap = c.u(self.so)
+                names_bt = c.u(self.so)
                 if not self.undef(fheap):
-                    raise NotImplementedError("groups with dense link storage (fractal heap)")
+                    for data in self._dense_link_messages(fheap, names_bt):
+                        name, addr = self._decode_link(data)
+                        if addr is not None:
+                            links[name] = addr
             elif m.type == MSG_LINK:
                 name, addr = self._decode_link(m.data)
                 if addr is not None:
                     links[name] = addr
         return links
+
+    # -- dense link storage: a fractal heap of link messages, indexed by a
+    # version-2 B-tree of name hashes (format specification III.G, III.A.2)
+    def _dense_link_messages(self, heap_addr, btree_addr):
+        heap = self._fractal_heap(heap_addr)
+        for heap_id in self._btree2_records(btree_addr, id_len=heap["id_len"]):
+            yield self._heap_object(heap, heap_id)
+
+    def _fractal_heap(self, addr):
+        c = self.cursor(addr, 4 + 1 + 2 + 2 + 1 + 4 + 12 * max(self.so, self.sl) + 2 + 2 * self.sl + 2 + 2 + self.so + 2)
+        if c.raw(4) != b"FRHP":
+            raise HDF5FormatError("bad fractal heap signature")
+        c.skip(1)
+        h = {"id_len": c.u(2)}
+        filters_len = c.u(2)
+        c.skip(1)  # flags
+        h["max_obj"] = c.u(4)
+        c.skip(self.sl)  # next huge object id
+        c.skip(self.so)  # huge object B-tree
+        c.skip(self.sl)  # free space in managed blocks
+        c.skip(self.so)  # free space manager
+        c.skip(6 * self.sl)  # managed space, allocated, iterator, managed/huge/tiny counts and sizes (first six)
+        c.skip(2 * self.sl)  # tiny objects: size and count
+        h["width"] = c.u(2)
+        h["start"] = c.u(self.sl)
+        h["max_direct"] = c.u(self.sl)
+        h["max_heap_bits"] = c.u(2)
+        c.skip(2)  # starting rows in the root indirect block
+        h["root"] = c.u(self.so)
+        h["root_rows"] = c.u(2)
+        if filters_len:
+            raise NotImplementedError("filtered fractal heaps")
+        # heap id fields: the offset in bytes for max_heap_bits; the length
+        # in the smaller of the bytes for an offset inside the largest direct
+        # block and the bytes that encode the largest managed object
+        h["off_bytes"] = (h["max_heap_bits"] + 7) // 8
+        dir_bytes = ((h["max_direct"].bit_length() - 1) + 7) // 8
+        obj_bytes = (h["max_obj"].bit_length() - 1) // 8 + 1
+        h["len_bytes"] = max(1, min(dir_bytes, obj_bytes))
+        return h
+
+    def _btree2_records(self, addr, id_len):
+        c = self.cursor(addr, 4 + 1 + 1 + 4 + 2 + 2 + 1 + 1 + self.so + 2 + self.sl)
+        if c.raw(4) != b"BTHD":
+            raise HDF5FormatError("bad version-2 B-tree signature")
+        c.skip(1)
+        btype = c.u(1)
+        c.skip(4)  # node size
+        rec_size = c.u(2)
+        depth = c.u(2)
+        c.skip(2)
+        root = c.u(self.so)
+        nrec = c.u(2)
+        if btype != 5:
+            raise NotImplementedError(f"version-2 B-tree of type {btype} for links")
+        if depth != 0:
+            raise NotImplementedError("link name index deeper than one leaf")
+        if self.undef(root) or nrec == 0:
+            return []
+        leaf = self.cursor(root, 6 + nrec * rec_size)
+        if leaf.raw(4) != b"BTLF":
+            raise HDF5FormatError("bad version-2 B-tree leaf signature")
+        leaf.skip(2)
+        out = []
+        for _ in range(nrec):
+            leaf.skip(4)  # name hash
+            out.append(leaf.raw(id_len))
+            leaf.skip(rec_size - 4 - id_len)
+        return out
+
+    def _heap_object(self, h, heap_id):
+        kind = (heap_id[0] >> 4) & 3
+        if kind == 2:  # tiny: the object is in the id
+            n = (heap_id[0] & 0x0F) + 1
+            return bytes(heap_id[1:1 + n])
+        if kind != 0:
+            raise NotImplementedError("huge objects in a fractal heap")
+        cur = _Cursor(heap_id, 1)
+        off = cur.u(h["off_bytes"])
+        n = cur.u(h["len_bytes"])
+        if h["root_rows"] == 0:  # the root is one direct block holding offsets from 0
+            return self.at(h["root"] + off, n)
+        # root indirect block: rows of `width` direct blocks (start, start,
+        # 2 start, 4 start, ...); children listed row by row
+        width, start = h["width"], h["start"]
+        c = self.cursor(h["root"], 5 + self.so + h["off_bytes"] + h["root_rows"] * width * self.so)
+        if c.raw(4) != b"FHIB":
+            raise HDF5FormatError("bad fractal heap indirect block signature")
+        c.skip(1 + self.so + h["off_bytes"])
+        block_off = 0
+        for row in range(h["root_rows"]):
+            size = start if row < 2 else start << (row - 1)
+            if size > h["max_direct"]:
+                raise NotImplementedError("fractal heap with nested indirect blocks")
+            for _ in range(width):
+                child = c.u(self.so)
+                if block_off <= off < block_off + size:
+                    if self.undef(child):
+                        raise HDF5FormatError("heap object in an unallocated block")
+                    return self.at(child + off - block_off, n)
+                block_off += size
+        raise HDF5FormatError("heap offset beyond the root indirect block")
 
     def _walk_group_btree(self, addr, names, links, depth):
         if depth > 32:

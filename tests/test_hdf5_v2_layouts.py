@@ -247,3 +247,81 @@ def test_variable_length_strings_and_sequences(tmp_path):
         runs = f["runs"][()]
         assert len(runs) == 2 and all(np.array_equal(r, s) for r, s in zip(runs, seqs))
         assert f["title"][()] == texts[0]
+
+
+def dense_group(b, links, root_indirect=False):
+    """A group whose links live in a fractal heap (dense storage) with a
+    one-leaf version-2 name index; returns the group's header address."""
+    width, start, max_direct, heap_bits = 4, 512, 65536, 32
+    off_bytes, len_bytes = 4, 2  # id = type byte + offset + length = 7 bytes
+    msgs = [link(n, a) for n, a in links]
+    # objects packed after a 32-byte block header area
+    hdr_room = 32
+    placed, off = [], hdr_room
+    for m in msgs:
+        placed.append((off, len(m)))
+        off += len(m)
+    assert off <= start
+    block = bytearray(start)
+    for (o, n), m in zip(placed, msgs):
+        block[o:o + n] = m
+    heap_addr = b.reserve(200)
+    block_off = 0
+    if root_indirect:
+        # the objects sit in the third direct block of the first row
+        block_off = 2 * start
+        placed = [(o + block_off, n) for o, n in placed]
+    dblock = b"FHDB" + bytes([0]) + struct.pack("<Q", heap_addr) + struct.pack("<I", block_off)
+    block[:len(dblock)] = dblock
+    daddr = b.put(bytes(block))
+    if root_indirect:
+        children = [U, U, daddr, U]
+        iblock = b"FHIB" + bytes([0]) + struct.pack("<Q", heap_addr) + struct.pack("<I", 0)
+        iblock += b"".join(struct.pack("<Q", a) for a in children)
+        iblock += struct.pack("<I", hdf5.lookup3(iblock))
+        root, rows = b.put(iblock), 1
+    else:
+        root, rows = daddr, 0
+    frhp = b"FRHP" + struct.pack("<BHHBI", 0, 7, 0, 0, 4096)
+    frhp += struct.pack("<QQQQ", 0, U, 0, U)
+    frhp += struct.pack("<QQQQQQ", start, start, 0, len(msgs), 0, 0)
+    frhp += struct.pack("<QQ", 0, 0)
+    frhp += struct.pack("<HQQHHQH", width, start, max_direct, heap_bits, 1 if root_indirect else 0, root, rows)
+    frhp += struct.pack("<I", hdf5.lookup3(frhp))
+    b.buf[heap_addr:heap_addr + len(frhp)] = frhp
+    recs = b""
+    for (n, _), (o, ln) in zip(links, placed):
+        heap_id = bytes([0]) + struct.pack("<I", o) + struct.pack("<H", ln)
+        recs += struct.pack("<I", hdf5.lookup3(n.encode())) + heap_id
+    leaf = b"BTLF" + struct.pack("<BB", 0, 5) + recs
+    leaf += struct.pack("<I", hdf5.lookup3(leaf))
+    laddr = b.put(leaf)
+    bthd = b"BTHD" + struct.pack("<BBIHHBBQHQ", 0, 5, 512, 11, 0, 100, 40, laddr, len(links), len(links))
+    bthd += struct.pack("<I", hdf5.lookup3(bthd))
+    baddr = b.put(bthd)
+    li = struct.pack("<BBQQ", 0, 0, heap_addr, baddr)
+    return b.put(ohdr([(hdf5.MSG_LINK_INFO, li, 0), (hdf5.MSG_GROUP_INFO, struct.pack("<BB", 0, 0), 0)]))
+
+
+@pytest.mark.parametrize("root_indirect", [False, True])
+def test_dense_link_storage(tmp_path, root_indirect):
+    """More than 8 links in a group written with libver="latest": the link
+    messages sit in a fractal heap, found through the name index."""
+    b = Builder()
+    data = {}
+    links = []
+    for k in range(12):
+        arr = np.full((2, 3), k, dtype=np.int16)
+        a = b.put(arr.tobytes())
+        links.append((f"frame{k:02d}", dataset(b, arr, struct.pack("<BBQQ", 4, 1, a, arr.nbytes))))
+        data[f"frame{k:02d}"] = arr
+    g = dense_group(b, links, root_indirect)
+    li = struct.pack("<BBQQ", 0, 0, U, U)
+    root = b.put(ohdr([(hdf5.MSG_LINK_INFO, li, 0), (hdf5.MSG_LINK, link("frames", g), 0)]))
+    path = tmp_path / "dense.h5"
+    path.write_bytes(b.finish(root))
+    with hdf5.File(path) as f:
+        grp = f["frames"]
+        assert grp.keys() == sorted(data)
+        for k, v in data.items():
+            np.testing.assert_array_equal(f[f"frames/{k}"][()], v)
