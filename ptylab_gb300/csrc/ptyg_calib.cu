@@ -300,6 +300,8 @@ extern "C" int ptyg_calib_normalise(int n, int N, float* ft, const float* norm, 
 extern "C" int ptyg_calib_gaussian(int n, int N, int radius, const double* half_weights, const float* in, float* out,
                                    void* stream) {
   if (n < 0 || N < 1 || !in || !out) return invalid("bad arguments");
+  if (radius < 0 || radius > kMaxGaussRadius || !half_weights)
+    return ptyg::set_last_error(PTYG_ERR_UNSUPPORTED, "gaussian radius must lie in 0..63");
   if (n == 0) return PTYG_OK;
   cudaStream_t st = (cudaStream_t)stream;
   float* tmp = nullptr;

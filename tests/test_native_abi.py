@@ -136,3 +136,37 @@ def test_new_entry_points_reject_bad_arguments_before_touching_a_device(lib):
     assert lib.ptyg_stitch(None, dummy, 1, 32, 64, dummy, dummy, dummy, None) == _native.PTYG_ERR_INVALID
     assert lib.ptyg_stitch(dummy, dummy, 1, 64, 32, dummy, dummy, dummy, None) == _native.PTYG_ERR_INVALID
     assert lib.ptyg_nn_conv3_path(1) == 0
+
+
+def test_calibration_and_reference_entry_points_validate_first(lib):
+    """The FPM calibration calls and the interferometric readout refuse bad
+    arguments with the documented status before any device work."""
+    import ctypes as C
+
+    from ptylab_gb300 import _native
+
+    d = C.c_void_p(16)
+    host = (C.c_double * 4)(1.0, 0.5, 0.25, 0.125)
+    # frame sizes outside the transforms'; counts and pointers
+    assert lib.ptyg_calib_spectra(2, 48, d, d, d, d, d, d, d, None) == _native.PTYG_ERR_UNSUPPORTED
+    assert lib.ptyg_calib_spectra(0, 64, d, d, d, d, d, d, d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_spectra(2, 64, d, None, d, d, d, d, d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_normalise(-1, 64, d, d, C.c_float(1.0), None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_normalise(0, 64, d, d, C.c_float(1.0), None) == _native.PTYG_OK
+    assert lib.ptyg_calib_gaussian(2, 64, 64, host, d, d, None) == _native.PTYG_ERR_UNSUPPORTED
+    assert lib.ptyg_calib_gaussian(2, 64, 3, None, d, d, None) == _native.PTYG_ERR_UNSUPPORTED
+    assert lib.ptyg_calib_gaussian(0, 64, 3, host, d, d, None) == _native.PTYG_OK
+    # circle search: radii and angles at most 64, a search grid of at most 255
+    assert lib.ptyg_calib_arcs(64, d, 1, d, d, d, 0, host, 4, host, host, 3, d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_arcs(64, d, 1, d, d, d, 65, host, 4, host, host, 3, d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_arcs(64, d, 1, d, d, d, 4, host, 65, host, host, 3, d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_arcs(64, d, 1, d, d, d, 4, host, 4, host, host, 256, d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_arcs(64, d, 0, d, d, d, 4, host, 4, host, host, 3, d, None) == _native.PTYG_OK
+    assert lib.ptyg_calib_arcs(64, d, 1, d, d, d, 4, host, 4, host, None, 3, d, None) == _native.PTYG_ERR_INVALID
+    # candidate RMSE
+    assert lib.ptyg_calib_rms(96, d, d, 2, d, d, C.c_double(5.0), d, None) == _native.PTYG_ERR_UNSUPPORTED
+    assert lib.ptyg_calib_rms(64, d, d, -1, d, d, C.c_double(5.0), d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_rms(64, d, d, 2, d, d, C.c_double(-1.0), d, None) == _native.PTYG_ERR_INVALID
+    assert lib.ptyg_calib_rms(64, d, d, 0, d, d, C.c_double(5.0), d, None) == _native.PTYG_OK
+    # the interferometric field readout needs a plan
+    assert lib.ptyg_plan_get_reference(None, 0, d, None) == _native.PTYG_ERR_INVALID
