@@ -406,3 +406,16 @@ def test_data_preparation_matches_reference(golden, step):
         np.testing.assert_array_equal(got, want)
     with pytest.raises(TypeError):
         ed.cropCenter(4.0)
+
+
+def test_io_benchmark_runs(capsys, tmp_path):
+    """python -m ptylab_gb300.io.benchmark at a tiny size: both layouts, read
+    back equal to what was written."""
+    import json
+
+    from ptylab_gb300.io import benchmark
+
+    benchmark.main(["--frames", "6", "--Nd", "32", "--reps", "1", "--dir", str(tmp_path)])
+    lines = [json.loads(x) for x in capsys.readouterr().out.strip().splitlines()]
+    assert [x["layout"] for x in lines] == ["contiguous", "gzip"]
+    assert all(x["read"] > 0 and x["write"] > 0 for x in lines) and "fromfile" in lines[0]
