@@ -459,8 +459,8 @@ class IlluminationCalibration:
 
     # -------------------------------------------------------------- the two searches
     def findCalibratedRadius(self, ptychogram, FT_ptychogram, initialPositions):
-        """CalibrationFPM.py:421-536; ``FT_ptychogram`` is a device tensor of
-        the brightfield frames' Fourier images."""
+        """CalibrationFPM.py:421-536; ``FT_ptychogram``, the brightfield
+        frames' Fourier images, as a host array or a device tensor."""
         self.initialize_error_search_space()
         self.radiuSearchBounds = 5
         self.radiusSearchStep = 0.5
@@ -469,6 +469,9 @@ class IlluminationCalibration:
         tolerance = [self.radiusSearchStep * 1.1, self.radiusSearchStep * 0.9]
         self.apertRadiusPixel_init = self.apertRadiusPixel
         dev = self._device()
+        if isinstance(FT_ptychogram, np.ndarray):  # PtyLab's callers pass host arrays
+            FT_ptychogram = dev.upload(FT_ptychogram)
+        initialPositions = np.asarray(initialPositions)
         nimg = FT_ptychogram.shape[0]
         converged = False
         check_done = False
@@ -509,11 +512,16 @@ class IlluminationCalibration:
 
     def findPositionCalibrationMatrix(self, ptychogram, FT_ptychogram, initialPositions, spectra=None):
         """CalibrationFPM.py:538-665 with every LED searched at once:
-        ``ptychogram`` (windowed frames), ``FT_ptychogram`` and ``spectra``
-        (their inverse transforms) are device tensors of the brightfield
-        frames."""
+        ``ptychogram`` (windowed frames) and ``FT_ptychogram`` of the
+        brightfield frames as host arrays or device tensors; ``spectra``
+        (their inverse transforms) is computed when not given."""
         self.initialize_error_search_space()
         dev = self._device()
+        if isinstance(ptychogram, np.ndarray):  # PtyLab's callers pass host arrays
+            ptychogram = dev.upload(ptychogram)
+        if isinstance(FT_ptychogram, np.ndarray):
+            FT_ptychogram = dev.upload(FT_ptychogram)
+        initialPositions = np.asarray(initialPositions)
         nimg = FT_ptychogram.shape[0]
         calibrated = np.array(initialPositions, copy=True)
         failed = []

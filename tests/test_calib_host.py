@@ -201,3 +201,19 @@ def test_refused_sizes_and_plotting():
     ic.img_size = 96
     with pytest.raises(NotImplementedError):
         ic._fourier(np.zeros((2, 96, 96), np.float32))
+
+
+def test_public_steps_take_host_arrays():
+    """PtyLab's own callers pass NumPy arrays to the two search steps."""
+    g, settings = load_case("affine_small")
+    ic, rec, data, oracle = build(g, settings)
+    frames = g["ptychogram"].astype(np.float32)
+    FT = oracle.convertToFourierSpace(frames)  # windows frames in place
+    bf = g["brightfield"]
+    init = g["positions"] - int(g["No"]) // 2 + int(g["Np"]) // 2
+    m, fitted = ic.findPositionCalibrationMatrix(frames[bf], FT[bf], init[bf])
+    np.random.seed(1234)
+    oracle.run(g["ptychogram"].astype(np.float32), g["positions"])
+    np.testing.assert_array_equal(ic.calibrated_positions, oracle.calibrated_positions)
+    old, new = ic.findCalibratedRadius(frames[bf], FT[bf], init[bf])
+    assert old == pytest.approx(ic.apertRadiusPixel_init) and new > 0
