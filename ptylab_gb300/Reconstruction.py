@@ -301,6 +301,40 @@ class Reconstruction(object):
     def Ld(self):
         return self.Nd * self.dxd
 
+    # detector and object coordinates, detection NA and depth of field
+    # (Reconstruction.py:583-598, 652-672, 712-724)
+    @property
+    def xd(self):
+        return np.linspace(-self.Nd / 2, self.Nd / 2, int(self.Nd)) * self.dxd
+
+    @property
+    def Xd(self):
+        return np.meshgrid(self.xd, self.xd)[0]
+
+    @property
+    def Yd(self):
+        return np.meshgrid(self.xd, self.xd)[1]
+
+    @property
+    def xo(self):
+        return np.linspace(-self.No / 2, self.No / 2, int(self.No)) * self.dxo
+
+    @property
+    def Xo(self):
+        return np.meshgrid(self.xo, self.xo)[0]
+
+    @property
+    def Yo(self):
+        return np.meshgrid(self.xo, self.xo)[1]
+
+    @property
+    def NAd(self):
+        return self.Ld / (2 * self.zo)
+
+    @property
+    def DoF(self):
+        return self.wavelength / self.NAd**2
+
     @property
     def Np(self):
         return self.Nd

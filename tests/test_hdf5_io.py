@@ -419,3 +419,18 @@ def test_io_benchmark_runs(capsys, tmp_path):
     lines = [json.loads(x) for x in capsys.readouterr().out.strip().splitlines()]
     assert [x["layout"] for x in lines] == ["contiguous", "gzip"]
     assert all(x["read"] > 0 and x["write"] > 0 for x in lines) and "fromfile" in lines[0]
+
+
+def test_reconstruction_geometry_properties():
+    """Detector / object coordinates, detection NA and depth of field
+    (Reconstruction.py:583-598, 652-672, 712-724)."""
+    from ptylab_gb300 import Params
+
+    ed = ExperimentalData(str(INPUTS / "cpm_simulation.hdf5"))
+    rec = Reconstruction(ed, Params())
+    n, d = rec.Nd, rec.dxd
+    np.testing.assert_array_equal(rec.xd, np.linspace(-n / 2, n / 2, n) * d)
+    assert rec.Xd.shape == (n, n) and np.array_equal(rec.Xd[0], rec.xd) and np.array_equal(rec.Yd[:, 0], rec.xd)
+    np.testing.assert_array_equal(rec.xo, np.linspace(-rec.No / 2, rec.No / 2, rec.No) * rec.dxo)
+    assert rec.Xo.shape == (rec.No, rec.No)
+    assert rec.NAd == rec.Ld / (2 * rec.zo) and rec.DoF == rec.wavelength / rec.NAd**2
