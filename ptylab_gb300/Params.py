@@ -80,9 +80,32 @@ class Params(object):
         self.l2reg_probe_aleph = 0.01
         self.l2reg_object_aleph = 0.001
         self.TV_autofocus = False
+        # the autofocus's and OPR's settings, with PtyLab's defaults
+        # (Params.py:127-192): present so scripts that set or read them run;
+        # switching either feature on raises NotImplementedError
+        self.TV_autofocus_metric = "TV"
+        self.TV_autofocus_intensityonly = False
+        self.TV_autofocus_stepsize = 5
+        self.TV_autofocus_aleph = 0.01
+        self.TV_autofocus_roi = [0.4, 0.6]
+        self.TV_autofocus_range_dof = 11
+        self.TV_autofocus_friction = 0.7
+        self.TV_autofocus_what = "object"
+        self.TV_autofocus_run_every = 3
+        self.TV_autofocus_min_z = None
+        self.TV_autofocus_max_z = None
+        self.TV_autofocus_nplanes = 11
         self.map_position_to_z_change = False
         self.OPRP = False
         self.OPR_modes = np.array([0])
+        self.OPR_subspace = 4
+        self.OPR_alpha = 0.05
+        self.OPR_tv_freq = 5
+        self.OPR_tv = False
+        self.OPR_tsvd_type = "gram"
+        self.OPR_orthogonalize_modes = True
+        self.OPR_fast_orthogonalization = True
+        self.OPR_neighbor_constraint = False
         self.SHG_probe = False
 
     @property
