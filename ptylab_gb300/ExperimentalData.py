@@ -127,6 +127,13 @@ class ExperimentalData:
         self.energyAtPos = np.sum(abs(self.ptychogram), (-1, -2))
         self.maxProbePower = np.sqrt(np.max(np.sum(self.ptychogram, (-1, -2))))
 
+    def _move_data_to_cpu(self):
+        """ExperimentalData.py:264-266.  The engines upload what they need
+        into their own device buffers; the host arrays stay on the host."""
+
+    def _move_data_to_gpu(self):
+        """ExperimentalData.py:268-271: as ``_move_data_to_cpu``."""
+
     def relative_intensity(self, index):
         """Frame intensity relative to the brightest frames (ExperimentalData.py:273-288)."""
         if not hasattr(self, "_relative_intensity"):
