@@ -666,6 +666,59 @@ class BaseEngine(object):
                           "ptyg_plan_intensity_scaling")
             p.intensityScaling[...] = out
 
+    def update_data(self, experimentalData, reconstruction=None):
+        """BaseEngine.py:172-176."""
+        self.experimentalData = experimentalData
+        if reconstruction is not None:
+            self.reconstruction = reconstruction
+
+    def getBeamWidth(self):
+        """FWHM widths (y, x) of the probe's last-slice intensity, summed over
+        wavelengths and modes, from its second moments (BaseEngine.py:744-768);
+        also stored as reconstruction.beamWidthY / beamWidthX."""
+        rec = self.reconstruction
+        P = np.sum(np.abs(_host(rec.probe)[..., -1, :, :]) ** 2, axis=(0, 1, 2))
+        P = P / np.sum(P, axis=(-1, -2))
+        Xp, Yp = rec.Xp, rec.Yp
+        xm = np.sum(Xp * P, axis=(-1, -2))
+        ym = np.sum(Yp * P, axis=(-1, -2))
+        xv = np.sum((Xp - xm) ** 2 * P, axis=(-1, -2))
+        yv = np.sum((Yp - ym) ** 2 * P, axis=(-1, -2))
+        c = 2 * np.sqrt(2 * np.log(2))  # standard deviation -> FWHM of a Gaussian
+        rec.beamWidthX = c * np.sqrt(xv)
+        rec.beamWidthY = c * np.sqrt(yv)
+        return rec.beamWidthY, rec.beamWidthX
+
+    def getOverlap(self, ind1, ind2):
+        """Linear and area overlap of scan positions ind1 and ind2
+        (BaseEngine.py:770-818), stored as reconstruction.linearOverlap and
+        reconstruction.areaOverlap.  A host-side analysis of the probe for
+        monitors and scripts, off the reconstruction path: its one transform
+        is NumPy's."""
+        rec = self.reconstruction
+        pos = np.asarray(rec.positions)
+        sy = abs(pos[ind2, 0] - pos[ind1, 0]) * rec.dxp
+        sx = abs(pos[ind2, 1] - pos[ind1, 1]) * rec.dxp
+        self.getBeamWidth()
+        rec.linearOverlap = np.maximum(1 - np.sqrt(sx**2 + sy**2) / np.minimum(rec.beamWidthX, rec.beamWidthY), 0)
+        Np = int(rec.Np)
+        fx = np.arange(-Np // 2, Np // 2) * (1 / (Np * rec.dxp))
+        Fx, Fy = np.meshgrid(fx, fx)
+        ax = (-2, -1)  # centred unitary transform (utils.py:12-28)
+        A = np.abs(_host(rec.probe)[:, 0, 0, -1, ...])
+        Q = np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(A, axes=ax), norm="ortho"), axes=ax)
+        rec.areaOverlap = np.mean(
+            np.abs(np.sum(Q**2 * np.exp(-1.0j * 2 * np.pi * (Fx * sx + Fy * sy)), axis=(-1, -2)))
+            / np.sum(np.abs(Q) ** 2, axis=(-1, -2)),
+            axis=0,
+        )
+        return rec.linearOverlap, rec.areaOverlap
+
+    def convert2single(self):
+        """BaseEngine.py:683-697: the reference leaves the dtype matching
+        unimplemented; the GB300 engines are single precision throughout."""
+        raise NotImplementedError()
+
     def changeExperimentalData(self, experimentalData):
         if experimentalData is not None:
             self.experimentalData = experimentalData

@@ -1,5 +1,7 @@
 """Host-side logic of the drop-in against the reference fixtures and the oracle (no GPU)."""
 
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -202,3 +204,24 @@ def test_several_wavelengths_are_checked_before_device_work():
         setup("ePIE", "polychromeASP", spectral=False)._check_supported()
     setup("ePIE", "polychromeASP")._check_supported()
     setup("ePIE", "Fraunhofer")._check_supported()
+
+
+def test_beam_width_and_overlap_match_reference():
+    """getBeamWidth / getOverlap (BaseEngine.py:744-818) against the
+    reference's own methods on the same probe and positions."""
+    import types
+
+    from ptylab_gb300.Engines.BaseEngine import BaseEngine
+
+    g = np.load(Path(__file__).parent / "golden" / "analysis_golden.npz")
+    rec = types.SimpleNamespace(**{k[3:]: g[k] for k in g.files if k.startswith("in_")})
+    rec.Np, rec.dxp = int(rec.Np), float(rec.dxp)
+    eng = types.SimpleNamespace(reconstruction=rec)
+    by, bx = BaseEngine.getBeamWidth(eng)
+    np.testing.assert_allclose(by, g["beamWidthY"], rtol=1e-12)
+    np.testing.assert_allclose(bx, g["beamWidthX"], rtol=1e-12)
+    eng.getBeamWidth = lambda: BaseEngine.getBeamWidth(eng)
+    for a, b in ((0, 3), (2, 7), (5, 5)):
+        lin, area = BaseEngine.getOverlap(eng, a, b)
+        np.testing.assert_allclose(lin, g[f"linear_{a}_{b}"], rtol=1e-12)
+        np.testing.assert_allclose(area, g[f"area_{a}_{b}"], rtol=1e-6)
