@@ -922,10 +922,29 @@ class _Reader:
         """Read, unfilter and place chunks; filtered chunks are decoded on a
         thread pool (zlib and the byte shuffles release the GIL)."""
 
+        # shuffle applied first on writing is undone last on reading: when the
+        # chunk lies wholly inside the output and its destination is
+        # contiguous, undo it straight into the destination (one strided copy)
+        last_shuffle = bool(filters) and filters[0][0] == FILTER_SHUFFLE and dtype.itemsize > 1
+
         def one(item):
             child, csize, mask, offs = item
             raw = self.at(child, csize)
-            if filters:
+            if last_shuffle and not mask & 1:
+                raw = self._unfilter(raw, filters[1:], mask >> 1)
+                if len(raw) < nbytes:
+                    raise HDF5FormatError("chunk shorter than its shape")
+                dst = tuple(slice(o, o + c) for o, c in zip(offs, chunk))
+                dest = out[dst] if all(o + c <= s for o, c, s in zip(offs, chunk, out.shape)) else None
+                if dest is not None and dest.flags.c_contiguous:
+                    es = filters[0][3][0] if filters[0][3] else dtype.itemsize
+                    n = nbytes // es
+                    if es == dtype.itemsize and n * es == nbytes:
+                        planes = np.frombuffer(raw, np.uint8, count=nbytes).reshape(es, n)
+                        dest.view(np.uint8).reshape(n, es)[...] = planes.T
+                        return
+                raw = self._unfilter(raw, filters[:1], 0)
+            elif filters:
                 raw = self._unfilter(raw, filters, mask)
             if len(raw) < nbytes:
                 raise HDF5FormatError("chunk shorter than its shape")
