@@ -434,3 +434,20 @@ def test_reconstruction_geometry_properties():
     np.testing.assert_array_equal(rec.xo, np.linspace(-rec.No / 2, rec.No / 2, rec.No) * rec.dxo)
     assert rec.Xo.shape == (rec.No, rec.No)
     assert rec.NAd == rec.Ld / (2 * rec.zo) and rec.DoF == rec.wavelength / rec.NAd**2
+
+
+def test_matlab_73_file_loads_through_readHdf5(tmp_path):
+    """A MATLAB 7.3 .mat file is HDF5 (written by libhdf5 with a 512-byte
+    user block); loadInputData reads it as PtyLab's PyTables path does."""
+    import shutil
+
+    p = _libhdf5_mat_file()
+    if p is None:
+        pytest.skip("SciPy's MATLAB 7.3 test file is not installed")
+    mat = tmp_path / "measurement.mat"
+    shutil.copy(p, mat)
+    readHdf5.checkDataFields(mat, ["testdouble"])
+    got = readHdf5.loadInputData(mat, ["testdouble"], ["absent"])
+    np.testing.assert_array_equal(got["testdouble"], np.arange(9) * np.pi / 4)
+    assert got["absent"] is None
+    assert readHdf5.getOrientation(mat) is None
