@@ -107,8 +107,11 @@ PTYG_API int ptyg_propagate(int propagator, int direction, int fftshift, int Np,
  * resolves and fills that device's built-in arrays (a synchronous copy), so
  * make it before any stream capture.  All calls share the one scratch array:
  * calls that overlap on the GPU (different streams, or threads) race and must
- * be serialised by the caller.  Same arguments as ptyg_propagate, without
- * `scratch`. */
+ * be serialised by the caller.  The built-in arrays' device addresses are
+ * cached per device for the life of the process; after a cudaDeviceReset
+ * they are stale and this entry point must not be called again.  A device
+ * other than sm_103a fails with PTYG_ERR_DEVICE, as ptyg_device_init does.
+ * Same arguments as ptyg_propagate, without `scratch`. */
 PTYG_API int ptyg_propagate_noalloc(int propagator, int direction, int fftshift, int Np, int batch, const void* in,
                                     void* out, const void* table, void* stream);
 
@@ -135,9 +138,9 @@ PTYG_API int ptyg_propagate_sets(int propagator, int direction, int Np, int batc
 
 /* ------------------------------------------------------------------------
  * Engine plans: the drop-in for the position loop of ePIE.reconstruct_stepwise
- * (PtyLab/Engines/ePIE.py:78-112), mPIE.reconstruct (mPIE.py:276-333),
+ * (PtyLab/Engines/ePIE.py:78-112), mPIE.reconstruct (mPIE.py:110-195),
  * qNewton.reconstruct (qNewton.py:67-90), mqNewton.reconstruct
- * (mqNewton.py:81-140) and e3PIE.reconstruct (e3PIE.py:229-313), with
+ * (mqNewton.py:81-140) and e3PIE.reconstruct (e3PIE.py:71-190), with
  * BaseEngine.intensityProjection
  * (BaseEngine.py:870-1012) and getRMSD (BaseEngine.py:843-868).
  */
@@ -189,7 +192,7 @@ typedef struct ptyg_update_params {
   float reg_object, reg_probe;
   float friction, feedback;
   float probe_weight;
-  float slice_beta; /* e3PIE probe step for slices >= 1 (0.9 in e3PIE.py:280) */
+  float slice_beta; /* e3PIE probe step for slices >= 1 (0.9 in e3PIE.py:140) */
   int32_t momentum_method; /* enum ptyg_momentum */
   double beta1, beta2;
   float beta1_scale, beta2_scale;
@@ -199,7 +202,7 @@ typedef struct ptyg_update_params {
 /* Caller-owned device buffers of one scan.
  *   mPIE: object/probe buffers and momenta, and momentum_flags (one byte per
  *         order slot, nonzero -> momentum step after that position,
- *         mPIE.py:330-332).
+ *         mPIE.py:169-172).
  *   mqNewton: object_momentum and probe_momentum (the first moments),
  *         probe_buffer, and second_moment = {v_object, v_probe}: a float32
  *         device pair holding the value every element of objectMomentum_v /

@@ -369,8 +369,8 @@ class State:
 
 
 class OracleEngine:
-    """One engine run: the position loop of ePIE.py:68-118, mPIE.py:270-344,
-    qNewton.py:63-99 or e3PIE.py:225-325, with BaseEngine's projection,
+    """One engine run: the position loop of ePIE.py:68-118, mPIE.py:110-195,
+    qNewton.py:63-99 or e3PIE.py:71-190, with BaseEngine's projection,
     error metrics and the in-scope constraints."""
 
     def __init__(self, s: Settings, g: Geometry, state: State, ptychogram, positions, energyAtPos, Xp=None, Yp=None,

@@ -41,11 +41,11 @@ class e3PIE(BaseEngine):
         return np.ascontiguousarray(self._slice_tf().astype(np.complex64))
 
     def reconstruct(self):
-        """e3PIE.py:71-330: one kernel launch per iteration walks every position
+        """e3PIE.py:71-225: one kernel launch per iteration walks every position
         through the slices, the detector projection and back."""
         self._run_loop()
 
     def _finish(self):
         super()._finish()
-        # product of all object slices (e3PIE.py:316)
+        # product of all object slices (e3PIE.py:176)
         self.reconstruction.objectProd = np.prod(self.reconstruction.object, 3)

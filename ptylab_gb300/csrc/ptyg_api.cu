@@ -1,6 +1,7 @@
 // C ABI of libptyg.so (declared in include/ptyg.h).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -54,34 +55,45 @@ static int cuda_fail(cudaError_t e, const char* what) {
 static bool valid_np(int Np) { return Np == 32 || Np == 64 || Np == 128 || Np == 256; }
 
 // ------------------------------------------------------- per-device tables
-// W_N^m = exp(-2*pi*i*m/N), m = 0..N-1, built in double and rounded.
+// W_N^m = exp(-2*pi*i*m/N), m = 0..N-1, built in double and rounded.  One set
+// per device, in a fixed array (never resized, so readers need no lock); a set
+// is published through its `ready` flag only once all four tables exist.
 namespace {
+constexpr int kMaxDevices = 64;
 struct DeviceTables {
   float2* tw[4] = {nullptr, nullptr, nullptr, nullptr};  // N = 32, 64, 128, 256
+  std::atomic<bool> ready{false};
 };
 std::mutex g_tables_mu;
-std::vector<DeviceTables> g_tables;
+DeviceTables g_tables[kMaxDevices];
 
 int table_slot(int Np) { return Np == 32 ? 0 : Np == 64 ? 1 : Np == 128 ? 2 : 3; }
 
 int ensure_tables(int device) {
+  if (device < 0 || device >= kMaxDevices) return fail(PTYG_ERR_DEVICE, "device %d out of range", device);
   std::lock_guard<std::mutex> lk(g_tables_mu);
-  if ((int)g_tables.size() <= device) g_tables.resize(device + 1);
   DeviceTables& t = g_tables[device];
-  if (t.tw[0]) return PTYG_OK;
+  if (t.ready.load(std::memory_order_acquire)) return PTYG_OK;
   const double pi = 3.14159265358979323846;
-  for (int s = 0; s < 4; ++s) {
+  float2* built[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < 4 && e == cudaSuccess; ++s) {
     const int N = 32 << s;
     std::vector<float2> h(N);
     for (int m = 0; m < N; ++m) {
       const double ang = -2.0 * pi * (double)m / (double)N;
       h[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
-    float2* d = nullptr;
-    PTYG_CUDA(cudaMalloc(&d, N * sizeof(float2)), "twiddle table");
-    PTYG_CUDA(cudaMemcpy(d, h.data(), N * sizeof(float2), cudaMemcpyHostToDevice), "twiddle table");
-    t.tw[s] = d;
+    e = cudaMalloc(&built[s], N * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(built[s], h.data(), N * sizeof(float2), cudaMemcpyHostToDevice);
   }
+  if (e != cudaSuccess) {
+    for (float2* d : built)
+      if (d) cudaFree(d);
+    return cuda_fail(e, "twiddle table");
+  }
+  for (int s = 0; s < 4; ++s) t.tw[s] = built[s];
+  t.ready.store(true, std::memory_order_release);
   return PTYG_OK;
 }
 
@@ -91,6 +103,11 @@ int current_device(int* dev) {
   return PTYG_OK;
 }
 
+bool tables_ready(int device) {
+  return device >= 0 && device < kMaxDevices && g_tables[device].ready.load(std::memory_order_acquire);
+}
+
+// Only called after tables_ready(device) (ready_device or ptyg_device_init succeeded).
 const float2* twiddles(int device, int Np) { return g_tables[device].tw[table_slot(Np)]; }
 }  // namespace
 
@@ -115,7 +132,7 @@ extern "C" int ptyg_device_init(int device) {
 static int ready_device(int* dev) {
   int r = current_device(dev);
   if (r) return r;
-  if ((int)g_tables.size() <= *dev || !g_tables[*dev].tw[0]) {
+  if (!tables_ready(*dev)) {
     r = ptyg_device_init(*dev);
     if (r) return r;
   }

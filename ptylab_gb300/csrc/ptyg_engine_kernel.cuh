@@ -4,7 +4,7 @@
 // One thread-block cluster of C CTAs reconstructs one scan; a grid of G
 // clusters reconstructs G independent scans.  The cluster walks the positions
 // of one iteration in the order the host drew (PtyLab/Engines/BaseEngine.py:637-665)
-// and, for each position, runs the body of ePIE.py:84-105 / mPIE.py:280-332 /
+// and, for each position, runs the body of ePIE.py:84-105 / mPIE.py:119-172 /
 // qNewton.py:69-90 / mqNewton.py:95-126 as passes separated by cluster barriers.  CTA c owns rows
 // [c*L, (c+1)*L) of every row pass and Fourier-layout columns [c*L, (c+1)*L)
 // of every column pass (L = Np/C), so it always updates the same probe rows

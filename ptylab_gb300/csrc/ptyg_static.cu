@@ -47,13 +47,22 @@ int fail(int code, const char* fmt, ...) {
 
 int twiddle_offset(int Np) { return Np == 32 ? 0 : Np == 64 ? 32 : Np == 128 ? 96 : 224; }
 
-// Once per device, with that device current: resolve the device addresses of
-// the static arrays (host code may not use the symbols directly) and fill the
-// twiddle tables.  cudaMemcpyToSymbol is synchronous, so the first call on a
-// device must not be made while a stream is being captured.
+// Once per device, with that device current: check that it is an sm_103a GPU
+// (as ptyg_device_init does for every other entry point), resolve the device
+// addresses of the static arrays (host code may not use the symbols directly)
+// and fill the twiddle tables.  cudaMemcpyToSymbol is synchronous, so the
+// first call on a device must not be made while a stream is being captured.
+// The addresses are cached for the life of the process: after a
+// cudaDeviceReset they are stale, and this entry point must not be used again.
 int setup(int dev) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (g_scratch_ptr[dev]) return PTYG_OK;
+  int major = 0, minor = 0;
+  cudaError_t ea = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  if (ea == cudaSuccess) ea = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (ea != cudaSuccess) return fail(PTYG_ERR_DEVICE, "no CUDA device: %s", cudaGetErrorString(ea));
+  if (major != 10 || minor != 3)
+    return fail(PTYG_ERR_DEVICE, "device %d is sm_%d%d; libptyg is built for sm_103a only", dev, major, minor);
   void* scratch = nullptr;
   void* tw = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);

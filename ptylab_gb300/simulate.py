@@ -71,6 +71,31 @@ class ScanSpec:
     wavelength: float = 632.8e-9
     zo: float = 0.05
     dxd: float = 75e-6
+    # "fermat" (spiral) or "raster" (a square grid spanning the object, each
+    # position moved by a seeded uniform jitter of up to jitter_px pixels)
+    scan: str = "fermat"
+    jitter_px: float = 0.0
+    # multislice object: nslice weak-phase slices dz apart, the exit wave
+    # carried between them by the angular spectrum (e3PIE.py:99-124)
+    nslice: int = 1
+    dz: float = 0.0
+
+
+def _scan_pixels(spec: ScanSpec, rng, step):
+    if spec.scan == "raster":
+        n = int(round(np.sqrt(spec.num_positions)))
+        if n * n != spec.num_positions:
+            raise ValueError("a raster scan needs a square number of positions")
+        span = spec.No - spec.Np - 2 - 2 * spec.jitter_px
+        g = (np.arange(n) - (n - 1) / 2) * (span / max(n - 1, 1))
+        yy, xx = np.meshgrid(g, g, indexing="ij")
+        pos = np.stack([yy.ravel(), xx.ravel()], axis=1)
+        return pos + rng.uniform(-spec.jitter_px, spec.jitter_px, pos.shape)
+    pos = fermat_spiral(spec.num_positions, step)
+    span = spec.No - spec.Np - 2
+    if np.abs(pos).max() * 2 > span:
+        pos *= span / (2 * np.abs(pos).max())
+    return pos
 
 
 def simulate_cpm(spec: ScanSpec):
@@ -81,14 +106,19 @@ def simulate_cpm(spec: ScanSpec):
     dxp = spec.wavelength * spec.zo / (Np * spec.dxd)
     R = spec.probe_radius_fraction * Np
     step = spec.step_fraction * 2 * R
-    pos = fermat_spiral(spec.num_positions, step)
-    span = No - Np - 2
-    if np.abs(pos).max() * 2 > span:
-        pos *= span / (2 * np.abs(pos).max())
+    pos = _scan_pixels(spec, rng, step)
     encoder = pos * dxp
-    amp = spec.amp_min + (1 - spec.amp_min) * gaussian_random_field(rng, No, spec.sigma_px)
-    phase = spec.phase_max * gaussian_random_field(rng, No, spec.sigma_px)
-    obj = amp * np.exp(1j * phase)
+    if spec.nslice > 1:
+        # weak-phase slices, amplitude 1, phase in [0, phase_max]
+        obj = np.stack([np.exp(1j * spec.phase_max * gaussian_random_field(rng, No, spec.sigma_px))
+                        for _ in range(spec.nslice)])
+        from ._tables import multislice_tf
+
+        H = np.fft.ifftshift(multislice_tf(spec.dz, spec.wavelength, 1.0, Np, Np * dxp))
+    else:
+        amp = spec.amp_min + (1 - spec.amp_min) * gaussian_random_field(rng, No, spec.sigma_px)
+        phase = spec.phase_max * gaussian_random_field(rng, No, spec.sigma_px)
+        obj = amp * np.exp(1j * phase)
     yy, xx = np.mgrid[:Np, :Np] - Np / 2
     r = np.hypot(yy, xx)
     if spec.npsm == 1:
@@ -101,6 +131,12 @@ def simulate_cpm(spec: ScanSpec):
     rows_cols = np.round(encoder / dxp).astype(int) + No // 2 - Np // 2
     I = np.empty((spec.num_positions, Np, Np), np.float64)
     for j, (py, px) in enumerate(rows_cols):
+        if spec.nslice > 1:
+            w = obj[0, py : py + Np, px : px + Np] * probe
+            for sl in range(1, spec.nslice):
+                w = np.fft.ifft2(np.fft.fft2(w) * H) * obj[sl, py : py + Np, px : px + Np]
+            I[j] = np.sum(np.abs(fft2c(w)) ** 2, axis=0)
+            continue
         patch = obj[py : py + Np, px : px + Np]
         I[j] = np.sum(np.abs(fft2c(patch[None] * probe)) ** 2, axis=0)
     scale = spec.photons / I.max()
@@ -125,6 +161,10 @@ def cpm_problem(spec: ScanSpec, engine_seed: int = 20240607):
     p.positionOrder = "sequential"
     rec = Reconstruction(d, p, No=spec.No)
     rec.npsm = spec.npsm
+    if spec.nslice > 1:
+        rec.nslice = spec.nslice
+        rec.dz = spec.dz
+        rec.refrIndex = 1.0
     np.random.seed(engine_seed)
     rec.initializeObjectProbe()
     return d, p, rec, obj, probe
@@ -211,3 +251,64 @@ def fpm_problem(spec: FPMSpec, engine_seed: int = 20240607):
     np.random.seed(engine_seed)
     rec.initializeObjectProbe()
     return d, p, rec, obj, pupil
+
+
+# ---------------------------------------------------------------- configurations
+# The four benchmark workloads of the plain reconstruction loop, as engine
+# name, scan description and iteration count.
+#   C0  CPM ePIE, Fraunhofer, Np 64, No 256, 100 Fermat positions (~75 % overlap),
+#       circular pupil of radius Np/8 with 2 pi of defocus at the rim, phase in
+#       [0, pi], 1e5 photons; 20 iterations, beta 0.25, sequential order
+#   C1  CPM mPIE, 4 Hermite-Gauss probe modes (powers 1 : 0.5 : 0.25 : 0.125),
+#       Np 128, No 512, 400 Fermat positions (~70 % overlap), amplitude in
+#       [0.6, 1], phase in [0, 2 pi], 1e6 photons; alpha = beta = 0.25,
+#       friction 0.7, feedback 0.3, random order with momentum; 50 iterations
+#   C2  multislice (e3PIE): 4 weak-phase slices (<= 0.3 rad) 10 um apart,
+#       13.5 nm wavelength, 20 nm pixels, Np 256, No 768, 30 x 30 raster with
+#       +-2 px jitter; 30 iterations
+#   C3  FPM qNewton: 15 x 15 LEDs at 4 mm pitch, 80 mm away, 128 x 128 images
+#       (6.5 um pixels, 4x magnification), NA 0.1, 625 nm, spectrum 512 x 512,
+#       5e4 photons; 'NA' order, probeBoundary; 50 iterations
+CONFIG_ENGINES = {"C0": "ePIE", "C1": "mPIE", "C2": "e3PIE", "C3": "qNewton"}
+CONFIG_ITERATIONS = {"C0": 20, "C1": 50, "C2": 30, "C3": 50}
+
+
+def config_spec(name: str, seed: int | None = None):
+    """ScanSpec / FPMSpec of benchmark configuration `name` (C0 ... C3)."""
+    kw = {} if seed is None else {"seed": seed}
+    if name == "C0":
+        return ScanSpec(**kw)
+    if name == "C1":
+        return ScanSpec(Np=128, No=512, num_positions=400, npsm=4, step_fraction=0.3, probe_radius_fraction=1 / 4,
+                        photons=1e6, phase_max=2 * np.pi, amp_min=0.6, sigma_px=4.0, **kw)
+    if name == "C2":
+        return ScanSpec(Np=256, No=768, num_positions=900, scan="raster", jitter_px=2.0, probe_radius_fraction=0.2,
+                        wavelength=13.5e-9, zo=0.05, dxd=13.5e-9 * 0.05 / (256 * 20e-9), photons=1e5,
+                        phase_max=0.3, nslice=4, dz=10e-6, **kw)
+    if name == "C3":
+        return FPMSpec(**kw)
+    raise ValueError(f"unknown configuration {name!r}")
+
+
+def config_problem(name: str, seed: int | None = None, engine_seed: int = 20240607):
+    """(engine name, ExperimentalData, Params, Reconstruction) of configuration
+    `name` with seeded data and initial guesses, ready for
+    ``getattr(Engines, engine)(rec, d, p, monitor)``."""
+    spec = config_spec(name, seed)
+    if name == "C3":
+        d, p, rec, _, _ = fpm_problem(spec, engine_seed=engine_seed)
+    else:
+        d, p, rec, _, _ = cpm_problem(spec, engine_seed=engine_seed)
+    if name == "C1":
+        p.positionOrder = "random"
+    return CONFIG_ENGINES[name], d, p, rec
+
+
+def configure_engine(name: str, engine, iterations: int | None = None):
+    """The configuration's engine scalars (mPIE: alpha 0.25 as C1 states; the
+    other scalars are the engines' own defaults: beta 0.25 for ePIE / mPIE /
+    e3PIE, friction 0.7, feedback 0.3; qNewton beta 1, reg 1)."""
+    if name == "C1":
+        engine.alphaObject = engine.alphaProbe = 0.25
+    engine.numIterations = CONFIG_ITERATIONS[name] if iterations is None else iterations
+    return engine

@@ -5,7 +5,7 @@ Test infrastructure only: calls the REFERENCE's own methods on a small
 reconstruction (two probe modes, three wavelengths, positions of a Fermat
 scan) and records their outputs.
 
-    python tests/golden/make_analysis_golden.py --reference /root/reference
+    python tests/golden/make_analysis_golden.py --reference <path of a PtyLab.py checkout>
 
 Output: ``tests/golden/analysis_golden.npz``.
 """

@@ -12,7 +12,7 @@ brightfield frames, every ``calculateRMSE`` decision, the calibrated
 aperture radius and NA, the transform, the fitted positions and the updated
 encoder, plus the Fourier-domain images of two frames.
 
-    python tests/golden/make_calib_golden.py --reference /root/reference
+    python tests/golden/make_calib_golden.py --reference <path of a PtyLab.py checkout>
 
 Output: ``tests/golden/calib_<case>.npz``; each holds its own inputs.
 """

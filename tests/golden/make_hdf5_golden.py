@@ -16,7 +16,7 @@ flips, the result file's dataset names, types and values.
 
 Run from the repository root with the reference checked out:
 
-    python tests/golden/make_hdf5_golden.py --reference /root/reference
+    python tests/golden/make_hdf5_golden.py --reference <path of a PtyLab.py checkout>
 
 Outputs: ``tests/golden/hdf5/*.hdf5`` (inputs) and
 ``tests/golden/hdf5_golden.npz``.

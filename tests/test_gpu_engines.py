@@ -286,9 +286,12 @@ def test_config0_size_precision_vs_complex128(torch_cuda, engine):
     gpu_vs_64 = {k: rel_err(getattr(rec, k), getattr(r64, k)) for k in keys}
     msg = f"{engine}: gpu-c128 {gpu_vs_128} ref-c128 {ref_vs_128} gpu-ref {gpu_vs_64}"
     print(msg)
+    # the benchmark spec's 1e-4 wherever the reference's own spread leaves room for
+    # it (ePIE object and error curve), else a small multiple of that spread
+    chaos = 4.0 if engine == "mPIE" else 3.0
     for k in keys:
-        assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 1e-6, msg
-        assert gpu_vs_64[k] <= 4 * ref_vs_128[k] + 1e-6, msg
+        assert gpu_vs_128[k] <= 3 * ref_vs_128[k] + 1e-6 or gpu_vs_128[k] <= 1e-4, msg
+        assert gpu_vs_64[k] <= max(1e-4, chaos * ref_vs_128[k]), msg
 
 
 def test_config3_fpm_qnewton_precision_vs_complex128(torch_cuda):
