@@ -145,7 +145,9 @@ def algorithmic_counts(flags_per_step, nscans):
     """Per step (one launch): bytes and FP32 flops of the algorithm, not of the code.
     Per position: object patch read + write (16*Np^2 B), intensities (4*Np^2 B);
     the probe stays on chip.  Per momentum step: object and probe read (X, buffer,
-    momentum) and written (X, buffer, momentum): 48*(No^2 + npsm*Np^2) B.
+    momentum) and written (X, buffer, momentum): 48*(No^2 + npsm*Np^2) B -- three
+    arrays written, not two, because objectBuffer / probeBuffer are separate
+    caller-visible arrays that must hold the new object and probe (mPIE.py:196-224).
     Flops: 5*N*log2(N) per complex 2D transform of N = Np^2 points, two per mode,
     plus 60 flops per pixel per mode of elementwise work."""
     n2 = NP * NP
@@ -283,6 +285,14 @@ def run_gb300(args, rank, world, local_rank):
         lib.ptyg_plan_destroy(plan1)
         del keep1
         single = {"value": NPOS * min(args.steps, 50) / t1, "us_per_position": t1 / (min(args.steps, 50) * NPOS) * 1e6}
+        # against the roofline of the SMs one scan runs on (its cluster)
+        probe1 = C.c_void_p()
+        _native.check(lib.ptyg_plan_create(C.byref(geometry(1, 0)), C.byref(probe1)))
+        cl1 = C.c_int()
+        _native.check(lib.ptyg_plan_info(probe1, C.byref(cl1), C.byref(th), C.byref(sm), C.byref(maxc)))
+        lib.ptyg_plan_destroy(probe1)
+        single["cluster_ctas"] = cl1.value
+        single["cluster_fp32_frac"] = single["value"] * per_pos_flops / (cl1.value * 128 * 2 * sm_max * 1e6)
 
         # end to end through the public API, host NumPy in and out: the same
         # G scans as engines built the PtyLab way, reconstructed together
@@ -326,7 +336,7 @@ def run_gb300(args, rank, world, local_rank):
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64 (FP32 complex; FP64 error sums and momentum arithmetic)",
+            "vs_baseline": None, "dtype": "c64 (FP32 complex, the mPIE momentum step included, in the reference's complex64 rounding order; FP64 error sums)",
             "data": "synthetic: seeded Fermat scans, GRF objects, Hermite-Gauss probes, 1e6-photon Poisson",
             "config": {
                 "workload": WORKLOAD, "scans_per_gpu": G, "cluster_ctas_per_scan": cl.value,
@@ -354,6 +364,140 @@ def run_gb300(args, rank, world, local_rank):
         }
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args.cpu_iters)
+        if not args.no_configs:
+            cfgs = {"C1": {"engine": "mPIE", "value": value, "unit": UNIT, "ms_per_step": ms_per_step,
+                           "scans": G, "roofline": {"hbm_frac": achieved_gbs / hbm_peak,
+                                                    "fp32_frac": achieved_tf / fp32_peak,
+                                                    "frac": max(achieved_gbs / hbm_peak, achieved_tf / fp32_peak)},
+                           "single_scan": single, "note": "the headline line above"}}
+            for name in ("C0", "C2", "C3"):
+                cfgs[name] = measure_config(name, dev, lib, with_cpu=world == 1 and not args.no_cpu_baseline)
+            out["configs"] = cfgs
+    return out
+
+
+# ------------------------------------------------------------------ other configurations
+# The plain loop's other benchmark configurations (ptylab_gb300.simulate):
+# C0 ePIE Np 64, C2 multislice e3PIE Np 256 (4 slices, 900 positions), C3 FPM
+# qNewton Np 128.  Each is timed through the engine API: the set-up of
+# Engines.reconstruct_batch (data and state moved to HBM once), then K timed
+# iterations of every scan (host order draw and upload, one launch, error
+# record, constraints), with CUDA events on the engines' stream.
+CONFIG_STEPS = {"C0": (20, 3), "C2": (4, 3), "C3": (20, 3)}
+
+
+def config_counts(name, rec):
+    """Algorithmic FP32 flops and HBM bytes per position-iteration: 5 N log2 N
+    flops per complex 2D transform of N = Np^2 points plus 60 flops per pixel
+    per mode (per slice for multislice) of elementwise work; bytes = object
+    patch read and written (16 B per pixel per slice) and the intensities
+    (4 B per pixel).  Multislice runs 2 + 4 (S - 1) transforms per position."""
+    n2 = int(rec.Np) ** 2
+    lg = np.log2(n2)
+    K = int(rec.nosm) * int(rec.npsm) * int(getattr(rec, "nlambda", 1))
+    S = int(rec.nslice)
+    if S > 1:
+        flops = (2 + 4 * (S - 1)) * 5 * n2 * lg + 60 * n2 * S
+        bytes_ = S * 16 * n2 + 4 * n2
+    else:
+        flops = K * (2 * 5 * n2 * lg + 60 * n2)
+        bytes_ = 20 * n2
+    return float(flops), float(bytes_)
+
+
+def _config_cpu_sample(name, target_positions):
+    """The oracle (complex64 NumPy, one core) on the first positions of the
+    configuration's scan: positions*iterations/s."""
+    from oracle import ptyoracle as O
+    from ptylab_gb300 import simulate as S
+
+    eng, d, p, rec = S.config_problem(name)
+    kw = {"C3": dict(order="NA", operationMode="FPM", probeBoundary=True)}.get(name, {})
+    g = O.Geometry(Np=int(rec.Np), No=int(rec.No), dxp=float(rec.dxp), wavelength=float(rec.wavelength),
+                   zo=float(rec.zo), npsm=int(rec.npsm), nslice=int(rec.nslice), dz=float(getattr(rec, "dz", 0) or 0))
+    s = O.Settings(engine=eng, entrancePupilDiameter=float(d.entrancePupilDiameter or 0.0), **kw)
+    nf = d.ptychogram.shape[0]
+    n = min(nf, target_positions)
+    iters = max(1, target_positions // nf)
+    st = O.State(object=rec.object.copy(), probe=rec.probe.copy())
+    oe = O.OracleEngine(s, g, st, d.ptychogram[:n], np.asarray(rec.positions)[:n], d.energyAtPos[:n])
+    np.random.seed(1)
+    t0 = time.perf_counter()
+    oe.reconstruct(iters)
+    t = time.perf_counter() - t0
+    return {"value": n * iters / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{name}: oracle {eng}, {n} positions x {iters} iterations on one core"}
+
+
+def measure_config(name, dev, lib, with_cpu=True):
+    """Batched and single-scan throughput of one configuration, its roofline
+    fractions and the one-core NumPy sample."""
+    import torch
+
+    from ptylab_gb300 import DummyMonitor, Engines
+    from ptylab_gb300 import simulate as S
+    from ptylab_gb300.Engines.batch import begin_batch, finish_batch, iterate_batch
+
+    eng_name, d, p, rec = S.config_problem(name)
+    steps, warm = CONFIG_STEPS[name]
+    nf = d.ptychogram.shape[0]
+    stream = torch.cuda.current_stream(dev)
+
+    def engines(n):
+        out = []
+        for _ in range(n):
+            e = getattr(Engines, eng_name)(copy.deepcopy(rec), copy.deepcopy(d), copy.deepcopy(p), DummyMonitor())
+            out.append(S.configure_engine(name, e, warm + steps))
+        return out
+
+    def timed(n, throughput):
+        es = begin_batch(engines(n), throughput)
+        cl, th, sm, mx = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        lib.ptyg_plan_info(es[0]._plan, C.byref(cl), C.byref(th), C.byref(sm), C.byref(mx))
+        for loop in range(warm):
+            iterate_batch(es, loop)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for loop in range(warm, warm + steps):
+            iterate_batch(es, loop)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t = e0.elapsed_time(e1) / 1e3
+        finish_batch(es)
+        return t, cl.value, mx.value
+
+    # how many scans the throughput shape holds at once
+    _, _, G = timed(1, 1)
+    G = max(1, G)
+    t, cl, _ = timed(G, 1)
+    t1, cl1, _ = timed(1, 0)
+    flops, bytes_ = config_counts(name, rec)
+    hbm_peak, peak_kind, _ = measured_peaks()
+    props = torch.cuda.get_device_properties(dev)
+    clock = 2070.0
+    fp32_sm = 128 * 2 * clock * 1e6 / 1e12  # TFLOP/s per SM
+    value = G * nf * steps / t
+    single = nf * steps / t1
+    frac_f = value * flops / 1e12 / (props.multi_processor_count * fp32_sm)
+    frac_b = value * bytes_ / 1e9 / hbm_peak
+    out = {
+        "engine": eng_name, "value": value, "unit": UNIT, "ms_per_step": t / steps * 1e3, "steps": steps,
+        "warmup": warm, "scans": G, "cluster_ctas_per_scan": cl, "positions": nf,
+        "roofline": {"bound": "fp32" if frac_f >= frac_b else "hbm", "frac": max(frac_f, frac_b),
+                     "fp32_tflops": value * flops / 1e12, "fp32_frac": frac_f,
+                     "hbm_gbs": value * bytes_ / 1e9, "hbm_frac": frac_b, "hbm_peak": hbm_peak,
+                     "hbm_peak_kind": peak_kind, "fp32_peak": props.multi_processor_count * fp32_sm,
+                     "fp32_peak_kind": "nominal: SMs x 128 FP32 lanes x 2 x 2070 MHz",
+                     "flops_per_position": flops, "bytes_per_position": bytes_},
+        "single_scan": {"value": single, "us_per_position": t1 / (steps * nf) * 1e6, "cluster_ctas": cl1,
+                        "cluster_fp32_frac": single * flops / 1e12 / (cl1 * fp32_sm)},
+        "step": "one iteration of every scan through the engine API (order draw and upload, one launch, "
+                "error record, constraints); data and state resident in HBM",
+    }
+    if with_cpu:
+        target = {"C0": 2000, "C2": 60, "C3": 1125}[name]
+        out["cpu_baseline"] = _config_cpu_sample(name, target)
     return out
 
 
@@ -476,6 +620,95 @@ def run_calibration(args):
     }
 
 
+def run_network(args):
+    """The warm-start network's tensor-core kernels (BF16 operands, FP32
+    accumulation): with --layer NAME, that layer's 3x3 convolution and its
+    weight gradient on random operands; otherwise the whole forward pass and
+    the whole backward pass (data and weight gradients of every layer), eager
+    and as CUDA graphs.  FLOPs are 2 M N K per GEMM (M pixels, N output
+    channels, K = 9 x input channels; the backward pass counts a weight
+    gradient for every layer and a data gradient for every layer but the
+    first).  CUDA-event times after 3 warm-up repetitions."""
+    import numpy as np
+    import torch
+
+    from ptylab_gb300 import _native
+    from ptylab_gb300.warmstart.network import LEVELS, WarmStartNet, layer_specs
+
+    lib = _native.require(0)
+    B, S, reps = args.net_batch, args.net_size, args.net_reps
+    level = {"e1": 1, "e2": 2, "e3": 3, "ba": 4, "bb": 4, "d3": 3, "d2": 2, "d1": 1, "he": 1}
+
+    def timed(f):
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            f()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps / 1e3
+
+    out = {"metric": "warm-start network tensor-core throughput", "unit": "TFLOP/s", "higher_is_better": True,
+           "dtype": "bf16 operands, f32 accumulation", "data": "synthetic (random operands)",
+           "config": {"batch": B, "size": S, "levels": list(LEVELS), "reps": reps}}
+    if args.layer:
+        spec = {name: (cins, co) for name, cins, co, _ in layer_specs(LEVELS)}
+        if args.layer not in spec or args.layer in ("e1a", "head"):
+            raise SystemExit(f"--layer: one of {[n for n in spec if n not in ('e1a', 'head')]}")
+        cins, co = spec[args.layer]
+        c0, c1 = cins[0], (cins[1] if len(cins) > 1 else 0)
+        H = W = S >> (level[args.layer[:2]] - 1)
+        bf = torch.bfloat16
+        x0 = torch.randn(B * H * W, c0, device="cuda").to(bf)
+        x1 = torch.randn(B * H * W, max(c1, 8), device="cuda").to(bf)
+        w = torch.randn(co, 9 * (c0 + c1), device="cuda").to(bf)
+        y = torch.empty(B * H * W, co, device="cuda", dtype=bf)
+        bias = torch.zeros(co, device="cuda")
+        dy = torch.randn(B * H * W, co, device="cuda").to(bf)
+        splits = 8
+        part = torch.empty(splits, co, 9 * (c0 + c1), device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        x1p = x1.data_ptr() if c1 else None
+        conv = lambda: _native.check(lib.ptyg_nn_conv3(x0.data_ptr(), x1p, c0, c1, B, H, W, w.data_ptr(), co, None,  # noqa: E731
+                                                       y.data_ptr(), bias.data_ptr(), 1, st.data_ptr(), None))
+        wgrad = lambda: _native.check(lib.ptyg_nn_conv3_wgrad(dy.data_ptr(), co, x0.data_ptr(), x1p, c0, c1, B, H, W,  # noqa: E731
+                                                              splits, part.data_ptr(), st.data_ptr(), None))
+        flop = 2.0 * B * H * W * co * 9 * (c0 + c1)
+        res = {}
+        for name, f in (("conv3_forward", conv), ("weight_gradient", wgrad)):
+            t = timed(f)
+            res[name] = {"us": t * 1e6, "tflops": flop / t / 1e12, "M": B * H * W, "N": co, "K": 9 * (c0 + c1)}
+        if int(st.item()) != 0:
+            raise TimeoutError("a bounded tensor-core wait gave up")
+        out.update(workload=f"layer {args.layer}", value=res["conv3_forward"]["tflops"], layer=res)
+        return out
+    fwd = bwd = 0.0
+    for name, cins, co, _ in layer_specs(LEVELS):
+        side = S >> (level[name[:2]] - 1)
+        k = (1 if name == "head" else 9) * sum(cins)
+        f = 2.0 * B * side * side * co * k
+        fwd += f
+        bwd += f if name == "e1a" else 2 * f
+    rng = np.random.default_rng(0)
+    x = torch.as_tensor(rng.standard_normal((B, S, S)).astype(np.float32)).cuda()
+    dy = torch.as_tensor(rng.standard_normal((B, S, S, 2)).astype(np.float32)).cuda()
+    res = {}
+    for mode in ("eager", "graphs"):
+        net = WarmStartNet(seed=0)
+        if mode == "graphs":
+            net.enable_graphs()
+        for name, f, flop in (("forward", lambda: net.forward(x), fwd), ("backward", lambda: net.backward(dy), bwd)):
+            t = timed(f)
+            res[f"{name}_{mode}"] = {"ms": t * 1e3, "gflop": flop / 1e9, "tflops": flop / t / 1e12}
+        net.check_status()
+    out.update(workload="whole network, forward and backward passes", value=res["forward_graphs"]["tflops"],
+               passes=res)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -486,6 +719,7 @@ def main():
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per scan (0: the library's choice)")
     ap.add_argument("--cpu-iters", type=int, default=8, help="iterations of the one-core CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the C0 / C2 / C3 lines")
     ap.add_argument("--threads", type=int, default=0, help="CTA size of the batched launch (0 = the plan's choice)")
     ap.add_argument("--probe-smem", type=int, default=0,
                     help="batched launch: 0 = plan's choice, 1 = probe rows in L2, 2 = in shared memory")
@@ -494,9 +728,18 @@ def main():
     ap.add_argument("--calibration", action="store_true",
                     help="time the FPM illumination calibration instead of the reconstruction")
     ap.add_argument("--calib-reps", type=int, default=3)
+    ap.add_argument("--network", action="store_true",
+                    help="time the warm-start network's forward and backward passes instead")
+    ap.add_argument("--layer", default="", help="with --network: time one layer (e.g. d3a) instead")
+    ap.add_argument("--net-batch", type=int, default=16)
+    ap.add_argument("--net-size", type=int, default=128)
+    ap.add_argument("--net-reps", type=int, default=20)
     args = ap.parse_args()
     if args.calibration:
         print(json.dumps(run_calibration(args)), flush=True)
+        return
+    if args.network:
+        print(json.dumps(run_network(args)), flush=True)
         return
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

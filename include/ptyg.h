@@ -424,6 +424,18 @@ PTYG_API int ptyg_stitch(const void* patches, const int32_t* positions, int n, i
 PTYG_API int ptyg_nn_adam(float* p, const float* g, float* m, float* v, void* p16, int64_t n, float lr, float b1,
                           float b2, float eps, int step, float weight_decay, void* stream);
 
+/* Bounded-wait policy of the network kernels (ptyg_nn_gemm, _conv3,
+ * _conv3_wgrad, _dense_wgrad): every mbarrier wait polls at most `polls`
+ * times (default 2^26) before it gives up; the launch then sets its status
+ * word to 1, stops issuing work, waits (bounded) for what it issued, frees
+ * its tensor memory and returns, and the context stays usable.  With
+ * stall_launches > 0 the next that many launches first wait on a barrier
+ * nothing arrives at, before issuing any copy or MMA: fault injection for
+ * failure-detection tests, so a timeout can be produced without a fault.
+ * No counterpart in the reference (its failure handling is Python
+ * exceptions, BaseEngine.py:376-403). */
+PTYG_API int ptyg_nn_set_wait_policy(long long polls, int stall_launches);
+
 /* ---------------------------------------------------------------------
  * FPM illumination calibration (PtyLab/Reconstruction/CalibrationFPM.py).
  * PtyLab runs it in NumPy/SciPy (IlluminationCalibration, :33-919); these

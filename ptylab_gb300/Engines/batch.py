@@ -64,11 +64,11 @@ def _check_compatible(engines):
             raise ValueError("reconstruct_batch: numIterations differs")
 
 
-def reconstruct_batch(engines):
-    """Run ``engine.reconstruct()`` for every engine, all scans in one launch per iteration."""
+def begin_batch(engines, throughput=1):
+    """Set-up half of ``reconstruct_batch``: validation, host preparation,
+    device state, one launch plan with a cluster per scan.  Returns the list
+    of engines; run ``iterate_batch`` for every loop, then ``finish_batch``."""
     engines = list(engines)
-    if not engines:
-        return
     for e in engines:
         e._pre_prepare()
     _check_compatible(engines)
@@ -77,19 +77,40 @@ def reconstruct_batch(engines):
     for e in engines:
         e._device_state()
     e0 = engines[0]
-    e0._plan_and_bind(num_scans=len(engines), throughput=1)
+    e0._plan_and_bind(num_scans=len(engines), throughput=throughput)
     for i, e in enumerate(engines[1:], 1):
         e._plan_and_bind(plan=e0._plan, scan=i)
     for e in engines:
         e._loop_begin()
+    return engines
+
+
+def iterate_batch(engines, loop):
+    """One iteration of every scan: the host draws each order (and mPIE's
+    momentum flags), one kernel launch walks all scans' positions, then each
+    engine records its error and applies its constraints."""
+    e0 = engines[0]
     nf = e0.experimentalData.numFrames
-    n = e0.numIterations
-    for loop in range(n):
-        for e in engines:
-            e._loop_order(loop)
-        e0._run_positions(0, nf, record_detector_error=(loop == n - 1))  # every bound scan
-        for e in engines:
-            e._loop_end(loop)
+    for e in engines:
+        e._loop_order(loop)
+    e0._run_positions(0, nf, record_detector_error=(loop == e0.numIterations - 1))  # every bound scan
+    for e in engines:
+        e._loop_end(loop)
+
+
+def finish_batch(engines):
+    """Read every scan's results back into NumPy and release the plan."""
     for e in engines[1:]:
         e._finish()
-    e0._finish()  # the plan's owner last: it destroys the plan
+    engines[0]._finish()  # the plan's owner last: it destroys the plan
+
+
+def reconstruct_batch(engines):
+    """Run ``engine.reconstruct()`` for every engine, all scans in one launch per iteration."""
+    engines = list(engines)
+    if not engines:
+        return
+    engines = begin_batch(engines)
+    for loop in range(engines[0].numIterations):
+        iterate_batch(engines, loop)
+    finish_batch(engines)

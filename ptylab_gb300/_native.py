@@ -134,6 +134,7 @@ _SIGNATURES = {
         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
     ],
     "ptyg_nn_conv3_path": [C.c_int],
+    "ptyg_nn_set_wait_policy": [C.c_longlong, C.c_int],
     "ptyg_calib_spectra": [C.c_int, C.c_int] + [C.c_void_p] * 8,
     "ptyg_calib_normalise": [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p],
     "ptyg_calib_gaussian": [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 
 #include "ptyg.h"
@@ -31,6 +32,19 @@
 
 namespace ptyg {
 namespace nn {
+
+// Bounded-wait policy of every network launch (ptyg_nn_set_wait_policy): the
+// poll limit, and how many of the next launches start with the injected wait.
+static std::atomic<long long> g_wait_limit{1LL << 26};
+static std::atomic<int> g_stall_launches{0};
+
+void wait_policy(long long* limit, int* stall) {
+  *limit = g_wait_limit.load();
+  int n = g_stall_launches.load();
+  while (n > 0 && !g_stall_launches.compare_exchange_weak(n, n - 1)) {
+  }
+  *stall = n > 0 ? 1 : 0;
+}
 
 typedef __nv_bfloat16 bf16;
 
@@ -53,7 +67,6 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 }
 
 constexpr int BM = 128, BK = 64, STAGES = 4;
-constexpr long WAIT_LIMIT = 1L << 26;  // try_wait polls before an MMA wait is declared lost
 
 enum AMode { A_DENSE = 0, A_CONV3 = 1 };
 enum Epilogue { EPI_F32 = 0, EPI_BF16 = 1 };
@@ -73,11 +86,13 @@ struct GemmArgs {
   const float* bias; // + bias[n] (single K split only)
   int relu;          // EPI_BF16: max(0, .)
   int* status;       // set to 1 when a wait gives up
+  long long waitLimit;  // try_wait polls before a wait is declared lost
+  int stall;         // fault injection: first wait on a barrier nothing arrives at
 };
 
-NN_DEV bool mbar_wait(uint32_t bar, uint32_t phase) {
+NN_DEV bool mbar_wait(uint32_t bar, uint32_t phase, long long limit) {
   uint32_t done = 0;
-  for (long i = 0; i < WAIT_LIMIT && !done; ++i) {
+  for (long long i = 0; i < limit && !done; ++i) {
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
@@ -206,13 +221,18 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
   const uint32_t tmem = *tmem_slot;
   constexpr uint32_t idesc = idesc_bf16(BM, BN);
   bool ok = true;
+  // fault injection (failure-detection tests): wait on stage 0's barrier
+  // before any MMA is committed to it; nothing arrives, the bounded wait runs
+  // out and the launch reports it, with no copy or MMA of its own in flight
+  // but the prologue's cp.async groups, which are waited for below
+  if (g.stall) ok = __syncthreads_and(mbar_wait(smem_u32(mbar), 0u, g.waitLimit));
   for (int kb = 0; kb < nkb; ++kb) {
     const int s = kb % STAGES;
     // refill the stage the MMAs of kb - 1 read, once they are done
     const int kn = kb + STAGES - 1;
     if (kn < nkb) {
       const int sn = kn % STAGES;
-      if (kb >= 1 && !mbar_wait(smem_u32(mbar + sn), (uint32_t)(((kb - 1) / STAGES) & 1))) ok = false;
+      if (kb >= 1 && !mbar_wait(smem_u32(mbar + sn), (uint32_t)(((kb - 1) / STAGES) & 1), g.waitLimit)) ok = false;
       if (ok)
         load_stage<BN, AMODE>(g, ri, smem0 + sn * STAGE_BYTES, smem0 + sn * STAGE_BYTES + A_BYTES, kBegin + kn * BK,
                               kEnd, n0, tid);
@@ -248,7 +268,7 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(const GemmArgs g) {
   if (ok) {
     // the loop waited for commit j exactly when j + STAGES < nkb (before refilling its stage)
     for (int j = max(0, nkb - STAGES); j < nkb; ++j)
-      if (!mbar_wait(smem_u32(mbar + (j % STAGES)), (uint32_t)((j / STAGES) & 1))) ok = false;
+      if (!mbar_wait(smem_u32(mbar + (j % STAGES)), (uint32_t)((j / STAGES) & 1), g.waitLimit)) ok = false;
   }
   asm volatile("tcgen05.fence::after_thread_sync;\n");
   ok = __syncthreads_and(ok);
@@ -336,6 +356,8 @@ struct DwArgs {
   int pSplit;        // pixels per blockIdx.z (multiple of BK)
   float* C;          // [splits][Co][K]
   int* status;
+  long long waitLimit;  // try_wait polls before a wait is declared lost
+  int stall;         // fault injection: first wait on a barrier nothing arrives at
 };
 
 // The B-operand column a thread loads is the same for every pixel block
@@ -450,12 +472,17 @@ __global__ void __launch_bounds__(128, 1) dw_kernel(const DwArgs g) {
   constexpr uint32_t idesc = idesc_bf16(BM, BN) | (1u << 15) | (1u << 16);
   constexpr uint32_t LBO_A = (BM / 8) * 128, LBO_B = (BN / 8) * 128;
   bool ok = true;
+  // fault injection (failure-detection tests): wait on stage 0's barrier
+  // before any MMA is committed to it; nothing arrives, the bounded wait runs
+  // out and the launch reports it, with no copy or MMA of its own in flight
+  // but the prologue's cp.async groups, which are waited for below
+  if (g.stall) ok = __syncthreads_and(mbar_wait(smem_u32(mbar), 0u, g.waitLimit));
   for (int kb = 0; kb < nkb; ++kb) {
     const int s = kb % STAGES;
     const int kn = kb + STAGES - 1;
     if (kn < nkb) {
       const int sn = kn % STAGES;
-      if (kb >= 1 && !mbar_wait(smem_u32(mbar + sn), (uint32_t)(((kb - 1) / STAGES) & 1))) ok = false;
+      if (kb >= 1 && !mbar_wait(smem_u32(mbar + sn), (uint32_t)(((kb - 1) / STAGES) & 1), g.waitLimit)) ok = false;
       if (ok)
         dw_load_stage<BN, CONV>(g, col, smem0 + sn * STAGE_BYTES, smem0 + sn * STAGE_BYTES + A_BYTES,
                                 pBegin + kn * BK, pEnd, co0, tid);
@@ -487,7 +514,7 @@ __global__ void __launch_bounds__(128, 1) dw_kernel(const DwArgs g) {
   cp_wait<0>();
   if (ok) {
     for (int j = max(0, nkb - STAGES); j < nkb; ++j)
-      if (!mbar_wait(smem_u32(mbar + (j % STAGES)), (uint32_t)((j / STAGES) & 1))) ok = false;
+      if (!mbar_wait(smem_u32(mbar + (j % STAGES)), (uint32_t)((j / STAGES) & 1), g.waitLimit)) ok = false;
   }
   asm volatile("tcgen05.fence::after_thread_sync;\n");
   ok = __syncthreads_and(ok);
@@ -840,6 +867,7 @@ extern "C" int ptyg_nn_gemm(const void* A, const void* B, int M, int N, int K, i
   g.bias = bias;
   g.relu = relu;
   g.status = status;
+  ptyg::nn::wait_policy(&g.waitLimit, &g.stall);
   return nn_check(launch_gemm(g, A_DENSE, splits, (cudaStream_t)stream), "ptyg_nn_gemm");
 }
 
@@ -879,6 +907,7 @@ extern "C" int ptyg_nn_conv3(const void* X, const void* X1, int C0, int C1, int 
   g.bias = bias;
   g.relu = relu;
   g.status = status;
+  ptyg::nn::wait_policy(&g.waitLimit, &g.stall);
   return nn_check(launch_gemm(g, A_CONV3, 1, (cudaStream_t)stream), "ptyg_nn_conv3");
 }
 
@@ -1070,6 +1099,7 @@ extern "C" int ptyg_nn_conv3_wgrad(const void* dY, int Co, const void* X, const 
   splits = (g.P + g.pSplit - 1) / g.pSplit;
   g.C = C;
   g.status = (int*)status;
+  ptyg::nn::wait_policy(&g.waitLimit, &g.stall);
   return nn_check(launch_dw(g, true, splits, (cudaStream_t)stream), "ptyg_nn_conv3_wgrad");
 }
 
@@ -1089,5 +1119,14 @@ extern "C" int ptyg_nn_dense_wgrad(const void* dY, int Co, const void* X, int K,
   splits = (P + g.pSplit - 1) / g.pSplit;
   g.C = C;
   g.status = (int*)status;
+  ptyg::nn::wait_policy(&g.waitLimit, &g.stall);
   return nn_check(launch_dw(g, false, splits, (cudaStream_t)stream), "ptyg_nn_dense_wgrad");
+}
+
+extern "C" int ptyg_nn_set_wait_policy(long long polls, int stall_launches) {
+  if (polls < 1 || stall_launches < 0)
+    return ptyg::set_last_error(PTYG_ERR_INVALID, "ptyg_nn_set_wait_policy: polls >= 1, stall_launches >= 0");
+  ptyg::nn::g_wait_limit.store(polls);
+  ptyg::nn::g_stall_launches.store(stall_launches);
+  return PTYG_OK;
 }

@@ -39,13 +39,12 @@ typedef __nv_bfloat16 bf16;
 #define TMA_DEV __device__ __forceinline__
 
 constexpr int TBM = 128, TSTAGES = 4;
-constexpr long TWAIT_LIMIT = 1L << 26;
 
 TMA_DEV uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-TMA_DEV bool wait_parity(uint32_t bar, uint32_t phase) {
+TMA_DEV bool wait_parity(uint32_t bar, uint32_t phase, long long limit) {
   uint32_t done = 0;
-  for (long i = 0; i < TWAIT_LIMIT && !done; ++i) {
+  for (long long i = 0; i < limit && !done; ++i) {
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
@@ -133,9 +132,14 @@ __global__ void __launch_bounds__(128, 1)
   if (tid == 0) {
     // ---- producer
     int issued = 0;
-    for (int kb = 0; kb < g.nkb; ++kb) {
+    // fault injection (failure-detection tests): wait on stage 0's empty
+    // barrier before any copy is issued; nothing arrives there, the bounded
+    // wait runs out and nothing is issued (the MMA thread's first wait then
+    // runs out too)
+    if (g.stall && !wait_parity(empty(0), 0u, g.waitLimit)) ok = false;
+    for (int kb = 0; ok && kb < g.nkb; ++kb) {
       const int s = kb % TSTAGES;
-      if (kb >= TSTAGES && !wait_parity(empty(s), (uint32_t)((kb / TSTAGES - 1) & 1))) {
+      if (kb >= TSTAGES && !wait_parity(empty(s), (uint32_t)((kb / TSTAGES - 1) & 1), g.waitLimit)) {
         ok = false;
         break;
       }
@@ -153,14 +157,14 @@ __global__ void __launch_bounds__(128, 1)
     // every issued copy lands before the CTA may exit (on the normal path the
     // MMA thread has consumed them all; these waits then return at once)
     for (int kb = issued > TSTAGES ? issued - TSTAGES : 0; kb < issued; ++kb)
-      if (!wait_parity(full(kb % TSTAGES), (uint32_t)((kb / TSTAGES) & 1))) ok = false;
+      if (!wait_parity(full(kb % TSTAGES), (uint32_t)((kb / TSTAGES) & 1), g.waitLimit)) ok = false;
   } else if (tid == 32) {
     // ---- MMA issuer
     constexpr uint32_t id = idesc(TBM, BN);
     const uint32_t rowb = (uint32_t)(BK * 2);
     for (int kb = 0; kb < g.nkb; ++kb) {
       const int s = kb % TSTAGES;
-      if (!wait_parity(full(s), (uint32_t)((kb / TSTAGES) & 1))) {
+      if (!wait_parity(full(s), (uint32_t)((kb / TSTAGES) & 1), g.waitLimit)) {
         ok = false;
         break;
       }
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(128, 1)
     // completes once every MMA issued above has (also after a failed wait)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(done));
   }
-  if (!wait_parity(done, 0)) ok = false;
+  if (!wait_parity(done, 0, g.waitLimit)) ok = false;
   asm volatile("tcgen05.fence::after_thread_sync;\n");
   ok = __syncthreads_and(ok);
   if (!ok) {
@@ -345,6 +349,7 @@ cudaError_t conv3_tma(const void* X, const void* X1, int C0, int C1, int Bn, int
   g.bias = bias;
   g.relu = relu;
   g.status = status;
+  wait_policy(&g.waitLimit, &g.stall);
   const int tiles = Bn * g.tilesX * g.tilesY;
   switch (BN) {
     case 32: return launch_bn<32>(ma, ma1, mw, g, tiles, st);

@@ -20,7 +20,12 @@ struct ConvTmaArgs {
   const float* bias;   // + bias[n] (or null)
   int relu;            // bf16 output: max(0, .)
   int* status;         // set to 1 when a bounded wait gives up
+  long long waitLimit; // try_wait polls before a wait is declared lost
+  int stall;           // fault injection: the producer first waits on a barrier nothing arrives at
 };
+
+// The bounded-wait policy of the next launch (poll limit, injected stall).
+void wait_policy(long long* limit, int* stall);
 
 // Y = conv3x3(concat(X, X1), Wt) (+ bias, ReLU) with TMA operand loads;
 // cudaErrorNotSupported when the shapes do not fit the tiling (the caller

@@ -396,8 +396,12 @@ class WarmStartNet:
                        prm.p16.data_ptr(), prm.p.numel(), lr, b1, b2, eps, self.step, weight_decay)
 
     def check_status(self):
+        """Raise TimeoutError (PTYG_ERR_TIMEOUT's exception) when a bounded
+        tensor-core wait of an earlier launch gave up; the status word is
+        cleared so the network stays usable."""
         if int(self.status.item()) != 0:
-            raise RuntimeError("a tensor-core wait gave up in the warm-start network kernels")
+            self.status.zero_()
+            raise TimeoutError("a bounded tensor-core wait gave up in the warm-start network kernels")
 
 
 def _he_init(seed, specs):

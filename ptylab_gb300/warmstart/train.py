@@ -99,10 +99,13 @@ def _physics_loss(pred, probe, I_meas):
     return torch.sum((a_model - a_meas) ** 2) / torch.sum(a_meas**2)
 
 
-def train(net, data, steps, batch=16, lr=1e-3, lam_phys=0.5, seed=0, log=print, log_every=50):
+def train(net, data, steps, batch=16, lr=1e-3, lam_phys=0.5, seed=0, log=print, log_every=50, reducer=None):
     """Adam steps on batches of one scan each; returns the loss history.  The
     network's forward and backward passes run as CUDA graphs (bit-identical
-    to the eager passes; ``net.enable_graphs(False)`` turns them off)."""
+    to the eager passes; ``net.enable_graphs(False)`` turns them off).
+    ``reducer`` (dataparallel.network_reducer(net)) averages the gradients
+    over the ranks between the backward pass and the Adam step, for
+    data-parallel training where each rank passes its own shard of `data`."""
     torch = _torch()
     if net._graphs is None:
         net.enable_graphs()
@@ -129,6 +132,8 @@ def train(net, data, steps, batch=16, lr=1e-3, lam_phys=0.5, seed=0, log=print, 
             loss = loss + lam_phys * l_phys
         loss.backward()
         net.backward(out.grad)
+        if reducer is not None:
+            reducer()
         net.adam_step(lr=lr)
         hist.append((float(l_sup.detach()), float(l_phys.detach())))
         if log and (step + 1) % log_every == 0:
