@@ -82,6 +82,66 @@ PTYG_DEV float2 mul_w16(float2 a, int m) {
   return make_float2(fmaf(a.x, c, -a.y * sn), fmaf(a.x, sn, a.y * c));
 }
 
+// ------------------------------------------- packed FP32 pairs (f32x2)
+// Blackwell's packed single-precision instructions (add/sub/mul/fma.rn.f32x2)
+// apply one IEEE FP32 operation to both halves of a 64-bit register pair, so
+// two independent lines transformed side by side cost one instruction per
+// operation instead of two.  A float2 here is such a pair: .x belongs to the
+// first line, .y to the second.  Every operation rounds exactly as its scalar
+// counterpart, so the paired transform gives the scalar transform's bits.
+PTYG_DEV float2 padd(float2 a, float2 b) {
+  float2 r;
+  asm("{\n.reg .b64 ra, rb, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %5};\n"
+      "add.rn.f32x2 rd, ra, rb;\nmov.b64 {%0, %1}, rd;\n}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+PTYG_DEV float2 psub(float2 a, float2 b) {
+  float2 r;
+  asm("{\n.reg .b64 ra, rb, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %5};\n"
+      "sub.rn.f32x2 rd, ra, rb;\nmov.b64 {%0, %1}, rd;\n}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+PTYG_DEV float2 pmul(float2 a, float2 b) {
+  float2 r;
+  asm("{\n.reg .b64 ra, rb, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %5};\n"
+      "mul.rn.f32x2 rd, ra, rb;\nmov.b64 {%0, %1}, rd;\n}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+// a * b + c, fused (one rounding), per half
+PTYG_DEV float2 pfma(float2 a, float2 b, float2 c) {
+  float2 r;
+  asm("{\n.reg .b64 ra, rb, rc, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %5};\nmov.b64 rc, {%6, %7};\n"
+      "fma.rn.f32x2 rd, ra, rb, rc;\nmov.b64 {%0, %1}, rd;\n}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+PTYG_DEV float2 pdup(float v) { return make_float2(v, v); }
+// exact negation of both halves (-1 * x, signed zeros included)
+PTYG_DEV float2 pneg(float2 a) { return pmul(a, pdup(-1.f)); }
+
+// Two complex values, one per line, as a pair of real parts and a pair of
+// imaginary parts.
+struct CPair {
+  float2 re, im;
+};
+
+// a * w (cmul's rounding) for a twiddle w shared by both lines; wx, wy, nwy
+// are the pairs (w.x, w.x), (w.y, w.y), (-w.y, -w.y)
+PTYG_DEV CPair pcmul(CPair a, float2 wx, float2 wy, float2 nwy) {
+  return {pfma(a.re, wx, pmul(a.im, nwy)), pfma(a.re, wy, pmul(a.im, wx))};
+}
+// conj(w) * a (cmulc's rounding)
+PTYG_DEV CPair pcmulc(CPair a, float2 wx, float2 wy, float2 nwy) {
+  return {pfma(wx, a.re, pmul(wy, a.im)), pfma(wx, a.im, pmul(nwy, a.re))};
+}
+
 template <int E>
 struct Log2 {
   static constexpr int v = (E <= 1) ? 0 : 1 + Log2<E / 2>::v;
@@ -118,6 +178,60 @@ PTYG_DEV void dft_reg(float2 (&v)[E]) {
       }
     }
     float2 t[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) t[i] = v[i];
+#pragma unroll
+    for (int i = 0; i < E; ++i) v[i] = t[rev_bits<E>(i)];
+  }
+}
+
+// mul_w16 on a pair of lines (the same rounding and signs)
+template <bool INV>
+PTYG_DEV CPair pmul_w16(CPair a, int m) {
+  const float c1 = 0.92387953251128674f;  // cos(pi/8)
+  const float s1 = 0.38268343236508978f;  // sin(pi/8)
+  const float h = 0.70710678118654752f;   // sqrt(1/2)
+  float c, sn;
+  switch (m & 15) {
+    case 0: return a;
+    case 4: return INV ? CPair{pneg(a.im), a.re} : CPair{a.im, pneg(a.re)};
+    case 8: return CPair{pneg(a.re), pneg(a.im)};
+    case 12: return INV ? CPair{a.im, pneg(a.re)} : CPair{pneg(a.im), a.re};
+    case 2: c = h; sn = h; break;
+    case 6: c = -h; sn = h; break;
+    case 10: c = -h; sn = -h; break;
+    case 14: c = h; sn = -h; break;
+    case 1: c = c1; sn = s1; break;
+    case 3: c = s1; sn = c1; break;
+    case 5: c = -s1; sn = c1; break;
+    case 7: c = -c1; sn = s1; break;
+    case 9: c = -c1; sn = -s1; break;
+    case 11: c = -s1; sn = -c1; break;
+    case 13: c = s1; sn = -c1; break;
+    default: c = c1; sn = -s1; break;  // 15
+  }
+  if (!INV) sn = -sn;
+  return {pfma(a.re, pdup(c), pmul(a.im, pdup(-sn))), pfma(a.re, pdup(sn), pmul(a.im, pdup(c)))};
+}
+
+// dft_reg on a pair of lines
+template <int E, bool INV>
+PTYG_DEV void pdft_reg(CPair (&v)[E]) {
+  if constexpr (E > 1) {
+#pragma unroll
+    for (int span = E / 2; span >= 1; span >>= 1) {
+#pragma unroll
+      for (int start = 0; start < E; start += 2 * span) {
+#pragma unroll
+        for (int m = 0; m < span; ++m) {
+          const CPair a = v[start + m];
+          const CPair b = v[start + m + span];
+          v[start + m] = CPair{padd(a.re, b.re), padd(a.im, b.im)};
+          v[start + m + span] = pmul_w16<INV>(CPair{psub(a.re, b.re), psub(a.im, b.im)}, m * (16 / (2 * span)));
+        }
+      }
+    }
+    CPair t[E];
 #pragma unroll
     for (int i = 0; i < E; ++i) t[i] = v[i];
 #pragma unroll
@@ -213,6 +327,97 @@ struct WarpFFT {
     }
   }
 
+  // Two lines at once with packed FP32 pairs: the operations and roundings of
+  // fwdm / invm, one paired instruction per two scalar ones.  The per-lane
+  // twiddles tl multiply one register of each line, so they stay scalar.
+  PTYG_DEV void fwd2(float2 (&v)[2][E]) const {
+    CPair p[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) p[j] = CPair{make_float2(v[0][j].x, v[1][j].x), make_float2(v[0][j].y, v[1][j].y)};
+    pdft_reg<E, false>(p);
+#pragma unroll
+    for (int k = 1; k < E; ++k) {
+      const float2 a0 = cmul(make_float2(p[k].re.x, p[k].im.x), tl[k - 1]);
+      const float2 a1 = cmul(make_float2(p[k].re.y, p[k].im.y), tl[k - 1]);
+      p[k] = CPair{make_float2(a0.x, a1.x), make_float2(a0.y, a1.y)};
+    }
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      const int h = 16 >> s;
+      const float2 sg = pdup((lane & h) ? -1.f : 1.f);
+      const bool rot = (s == 3) && (lane & 2) && (lane & 1);
+      float2 wx, wy, nwy;
+      if (s < 3) {
+        wx = pdup(ts[s].x);
+        wy = pdup(ts[s].y);
+        nwy = pdup(-ts[s].y);
+      }
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+        float2 ore, oim;
+        ore.x = __shfl_xor_sync(0xffffffffu, p[r].re.x, h);
+        ore.y = __shfl_xor_sync(0xffffffffu, p[r].re.y, h);
+        oim.x = __shfl_xor_sync(0xffffffffu, p[r].im.x, h);
+        oim.y = __shfl_xor_sync(0xffffffffu, p[r].im.y, h);
+        // lower lane: mine + other ; upper lane: (other - mine) * w
+        CPair t{pfma(sg, p[r].re, ore), pfma(sg, p[r].im, oim)};
+        if (s < 3) t = pcmul(t, wx, wy, nwy);
+        else if (s == 3 && rot) t = CPair{t.im, pneg(t.re)};
+        p[r] = t;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      v[0][j] = make_float2(p[j].re.x, p[j].im.x);
+      v[1][j] = make_float2(p[j].re.y, p[j].im.y);
+    }
+  }
+
+  PTYG_DEV void inv2(float2 (&v)[2][E]) const {
+    CPair p[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) p[j] = CPair{make_float2(v[0][j].x, v[1][j].x), make_float2(v[0][j].y, v[1][j].y)};
+#pragma unroll
+    for (int s = 4; s >= 0; --s) {
+      const int h = 16 >> s;
+      const bool upper = (lane & h) != 0;
+      const float2 sg = pdup(upper ? -1.f : 1.f);
+      const bool rot = (s == 3) && upper && (lane & 1);
+      float2 wx, wy, nwy;
+      if (s < 3) {
+        wx = pdup(ts[s].x);
+        wy = pdup(ts[s].y);
+        nwy = pdup(-ts[s].y);
+      }
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+        // the upper lane pre-multiplies its own value by conj(w); then
+        // lower: mine + other ; upper: other - mine
+        CPair c = p[r];
+        if (s < 3) c = pcmulc(c, wx, wy, nwy);
+        else if (s == 3 && rot) c = CPair{pneg(c.im), c.re};
+        float2 ore, oim;
+        ore.x = __shfl_xor_sync(0xffffffffu, c.re.x, h);
+        ore.y = __shfl_xor_sync(0xffffffffu, c.re.y, h);
+        oim.x = __shfl_xor_sync(0xffffffffu, c.im.x, h);
+        oim.y = __shfl_xor_sync(0xffffffffu, c.im.y, h);
+        p[r] = CPair{pfma(sg, c.re, ore), pfma(sg, c.im, oim)};
+      }
+    }
+#pragma unroll
+    for (int k = 1; k < E; ++k) {
+      const float2 a0 = cmulc(tl[k - 1], make_float2(p[k].re.x, p[k].im.x));
+      const float2 a1 = cmulc(tl[k - 1], make_float2(p[k].re.y, p[k].im.y));
+      p[k] = CPair{make_float2(a0.x, a1.x), make_float2(a0.y, a1.y)};
+    }
+    pdft_reg<E, true>(p);
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      v[0][j] = make_float2(p[j].re.x, p[j].im.x);
+      v[1][j] = make_float2(p[j].re.y, p[j].im.y);
+    }
+  }
+
   PTYG_DEV void fwd(float2 (&v)[E]) const { fwdm<1>(reinterpret_cast<float2(&)[1][E]>(v)); }
   PTYG_DEV void inv(float2 (&v)[E]) const { invm<1>(reinterpret_cast<float2(&)[1][E]>(v)); }
 };
@@ -230,9 +435,9 @@ PTYG_DEV void fft_tasks(const WarpFFT<E>& F, int ntasks, LoadF&& load, StoreF&& 
     load(t, v[0]);
     load(t + nw, v[1]);
     if (INV)
-      F.template invm<2>(v);
+      F.inv2(v);
     else
-      F.template fwdm<2>(v);
+      F.fwd2(v);
     __syncwarp();
     store(t, v[0]);
     store(t + nw, v[1]);

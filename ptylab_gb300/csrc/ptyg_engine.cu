@@ -40,6 +40,11 @@ cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t s
   if (a.engine == ENG_MQNEWTON)
     return a.nlambda > 1 ? launch_engine_mq_poly(a, nscans, threads, smem, st) : launch_engine_mq(a, nscans, threads, smem, st);
   if (a.nlambda > 1 || a.iconstraint == IC_INTERFEROMETRIC) return launch_engine_poly(a, nscans, threads, smem, st);
+  // PtyLab's defaults (one object mode, Fraunhofer / Fresnel, standard
+  // projection): the instantiation with those switches folded
+  if (a.nosm == 1 && a.prop != PROP_ASP && a.iconstraint == IC_STANDARD && !a.denoise && !a.bgMode && !a.fmask &&
+      !a.imask)
+    return launch_engine_fast(a, nscans, threads, smem, st);
   return launch_engine_t<VAR_STD>(a, nscans, threads, smem, st);
 }
 

@@ -27,6 +27,20 @@ PTYG_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "m
 PTYG_DEV void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 PTYG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// The two halves of cluster_sync, for work that may overlap the barrier:
+// arrive (release: this CTA's earlier writes, local and remote, become
+// visible to the cluster), then wait (acquire) before reading what the other
+// CTAs wrote.  For C == 1 the wait is a CTA barrier.
+PTYG_DEV void cluster_arrive(int C) {
+  if (C > 1) asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+}
+PTYG_DEV void cluster_wait(int C) {
+  if (C > 1)
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+  else
+    __syncthreads();
+}
+
 PTYG_DEV void cluster_sync(int C) {
   if (C > 1) {
     asm volatile(

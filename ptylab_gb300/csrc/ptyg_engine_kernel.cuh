@@ -325,13 +325,19 @@ __host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int n
 // cluster has C = Np / L CTAs.  Both compile-time so index arithmetic is shifts.
 // VAR: VAR_MQ is the mqNewton instantiation (engine == ENG_MQNEWTON), VAR_POLY
 // ePIE / mPIE / qNewton over several wavelengths, VAR_STD ePIE / mPIE /
-// qNewton at one, VAR_MQ_POLY mqNewton over several wavelengths.
-enum { VAR_STD = 0, VAR_MQ = 1, VAR_POLY = 2, VAR_MQ_POLY = 3 };
+// qNewton at one, VAR_MQ_POLY mqNewton over several wavelengths.  VAR_FAST is
+// VAR_STD with the common case's switches made compile-time constants (one
+// wavelength, one object mode, Fraunhofer or Fresnel, the standard
+// projection without background, masks or denoising), so its index
+// arithmetic and mode loops fold away; the host picks it whenever they hold
+// (launch_engine).  It computes exactly what VAR_STD computes.
+enum { VAR_STD = 0, VAR_MQ = 1, VAR_POLY = 2, VAR_MQ_POLY = 3, VAR_FAST = 4 };
 template <int E, int L, int VAR>
 __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 512, 1)
     engine_kernel(const EngineArgs a) {
   constexpr bool MQ = VAR == VAR_MQ || VAR == VAR_MQ_POLY;
   constexpr bool POLY = VAR == VAR_POLY || VAR == VAR_MQ_POLY;
+  constexpr bool FAST = VAR == VAR_FAST;
   // (512 threads x 128 registers: one CTA of 16 warps, or two of 8 warps, per
   // SM; mqNewton: at most 256 threads, so its momentum pass keeps all of a
   // tile's loads in registers)
@@ -347,11 +353,11 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
   // wave k = (l * nosmW + o) * npsmW + p pairs object mode l * nosmW + o with
   // probe mode l * npsmW + p of the same wavelength l
   const int nl = POLY ? a.nlambda : 1;  // a compile-time 1 outside the several-wavelength instantiations
-  const int nosmW = a.nosm, npsmW = a.npsm;
+  const int nosmW = FAST ? 1 : a.nosm, npsmW = a.npsm;
   const int nosm = nl * nosmW, npsm = nl * npsmW, K = nl * nosmW * npsmW, No = a.No;
   const bool centred = a.centred != 0;
   const bool fresnel = a.prop == PROP_FRESNEL;
-  const bool asp = a.prop == PROP_ASP;
+  const bool asp = !FAST && a.prop == PROP_ASP;
   const int eng = a.engine;
   // mqNewton is its own instantiation (MQ): its momentum pass costs registers
   // the other engines' passes do not need
@@ -421,25 +427,26 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
     const float* dat = sm.dat;
 
     // ---------------- A: stage the patch rows, norms, exit waves, row FFT
-    for (int i = threadIdx.x; i < nosm * LN; i += blockDim.x) {
-      const int o = i / LN, rem = i - (i / LN) * LN;
-      const int l = rem / NP, x = rem - (rem / NP) * NP;
-      sm.obj[i] = ld_cg(s.object + o * No2 + (size_t)(row0 + line0 + l) * No + col0 + x);
-    }
-    __syncthreads();
     {
-      // max of sum_p|P|^2, sum_o|O|^2 (patch), sum_p|P|, and for qNewton the
-      // max of sum_o|O| over the object outside the patch, which this
-      // position leaves unchanged until its momentum step
+      // stage the patch and take, in the same pass over the CTA's pixels, the
+      // max of sum_p|P|^2, sum_o|O|^2 (patch), sum_p|P| (qNewton), and for
+      // qNewton the max of sum_o|O| over the object outside the patch, which
+      // this position leaves unchanged until its momentum step
       float mx[4] = {0.f, 0.f, 0.f, 0.f};
       for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+        const int l = i / NP, x = i - (i / NP) * NP;
+        const float2* src = s.object + (size_t)(row0 + line0 + l) * No + col0 + x;
         float sp2 = 0.f, sp1 = 0.f, so2 = 0.f;
+        for (int o = 0; o < nosm; ++o) {
+          const float2 v = ld_cg(src + o * No2);
+          sm.obj[o * LN + i] = v;
+          so2 += cabs2(v);
+        }
         for (int p = 0; p < npsm; ++p) {
           const float q = cabs2(sm.probe[p * pst + i]);
           sp2 += q;
-          sp1 += sqrtf(q);
+          if (qn) sp1 += sqrtf(q);
         }
-        for (int o = 0; o < nosm; ++o) so2 += cabs2(sm.obj[o * LN + i]);
         mx[0] = fmaxf(mx[0], sp2);
         mx[1] = fmaxf(mx[1], so2);
         mx[2] = fmaxf(mx[2], sp1);
@@ -473,7 +480,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         F, K * L,
         [&](int t, float2(&v)[E]) {
           const int k = t / L, l = t % L;
-          const int o = k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
+          const int o = nosm == 1 ? 0 : k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
           const int y = line0 + l;
           const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
 #pragma unroll
@@ -504,28 +511,30 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
     // instantiation only (which serves ePIE, mPIE and qNewton for any nlambda),
     // so the standard kernel's registers stay as they are
     const bool interf = VAR == VAR_POLY && a.iconstraint == IC_INTERFEROMETRIC;
+    const int icon = FAST ? (int)IC_STANDARD : a.iconstraint;
+    const bool denoise = !FAST && a.denoise;
     auto project = [&](auto Iest, float outScale, auto colsTag) -> double {
       constexpr bool cols = decltype(colsTag)::value;
       const bool det = a.writeDetErr && s.detErr;
       const size_t tb = (size_t)blk0 * NP;
-      float* bg = a.bgMode ? s.background + tb : nullptr;
-      const float* Wt = a.fmask ? a.W + tb : nullptr;
-      const float* Mt = a.imask ? a.imaskTab + tb : nullptr;
+      float* bg = (!FAST && a.bgMode) ? s.background + tb : nullptr;
+      const float* Wt = (!FAST && a.fmask) ? a.W + tb : nullptr;
+      const float* Mt = (!FAST && a.imask) ? a.imaskTab + tb : nullptr;
       float e = 0.f, noise = 0.f, aleph = 0.f;
       auto denoised = [&](float im) {
-        if (!a.denoise) return im;
+        if (!denoise) return im;
         const float am = fmaxf(sqrtf(im) - noise, 0.f);
         return am * am;
       };
       auto finish = [&](int i, float ie, float im, float d) {
         const float q = denoised(im) / (ie + 1e-10f);
         float frac;
-        if (a.iconstraint == IC_POISSON) {
+        if (icon == IC_POISSON) {
           frac = q;
-        } else if (a.iconstraint == IC_EXPONENTIAL) {
+        } else if (icon == IC_EXPONENTIAL) {
           const float w = expf(-0.05f * (d / (ie + 1e-10f)));
           frac = w * sqrtf(q) + (1.f - w);
-        } else if (a.iconstraint == IC_FLUCTUATION) {
+        } else if (icon == IC_FLUCTUATION) {
           frac = (1.f + aleph) * 0.5f * q;
         } else {  // standard and interferometric (BaseEngine.py:955-962)
           frac = sqrtf(q);
@@ -540,7 +549,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
           bg[i] = b;
         }
       };
-      const bool twoPass = !cols && (a.denoise || a.iconstraint == IC_FLUCTUATION);
+      const bool twoPass = !cols && (denoise || icon == IC_FLUCTUATION);
       double dn = 0.0;
       auto pixel = [&](int i, float ie) {
         if (bg) ie += bg[i];
@@ -550,7 +559,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         if (det) s.detErr[((size_t)frame * NP + blk0) * NP + i] = d;
         if (twoPass) {
           sm.fr[i] = ie;  // kept for the second pass (same thread)
-          if (a.denoise) dn += (double)(sqrtf(im) - sqrtf(fabsf(ie)));
+          if (denoise) dn += (double)(sqrtf(im) - sqrtf(fabsf(ie)));
         } else {
           finish(i, ie, im, d);
         }
@@ -562,12 +571,12 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         for (int i = threadIdx.x; i < LN; i += blockDim.x) pixel(i, Iest(i));
       }
       if (twoPass) {
-        if (a.denoise) {
+        if (denoise) {
           double v[1] = {dn};
           cluster_sum_n<1, C>(v, sm.part, sm.redD, crank);
           noise = fabsf((float)(v[0] / (double)(NP * NP)));
         }
-        if (a.iconstraint == IC_FLUCTUATION) {
+        if (icon == IC_FLUCTUATION) {
           double v[2] = {0.0, 0.0};
           for (int i = threadIdx.x; i < LN; i += blockDim.x) {
             const float ie = sm.fr[i], imd = denoised(dat[i]), w = Wt ? Wt[i] : 1.f;
@@ -587,7 +596,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
     };
 
     double err = 0.0;
-    if (!asp && nw == L && !(a.denoise || a.iconstraint == IC_FLUCTUATION || interf)) {
+    if (!asp && nw == L && !(denoise || icon == IC_FLUCTUATION || interf)) {
       // ---------------- B, fused: warp w owns column w of every mode, so it
       // transforms the column's K modes, sums their intensities in
       // registers, projects its own pixels and transforms back, with no
@@ -613,7 +622,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         float2 v[2][E];
         colLoad(k, v[0]);
         colLoad(k + 1, v[1]);
-        F.template fwdm<2>(v);
+        F.fwd2(v);
         __syncwarp();
         colStore(k, v[0]);
         colStore(k + 1, v[1]);
@@ -636,7 +645,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         float2 v[2][E];
         invLoad(k, v[0]);
         invLoad(k + 1, v[1]);
-        F.template invm<2>(v);
+        F.inv2(v);
         scatter_column<E, L>(sm.rows, v[0], k, sx0 + c);
         scatter_column<E, L>(sm.rows, v[1], k + 1, sx0 + c);
       }
@@ -745,16 +754,20 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
       cluster_sync(C);
       column_filter<E, L, POLY>(sm.tile, sm.rows, F, a.aspH, true, crank, K, nosmW * npsmW);
     }
+    // every read of dat (the projection) and of redD (its cluster sums) is
+    // behind this barrier: fetch the next position's intensities into dat
+    // while C and A run
+    __syncthreads();
+    prefetch_data<NP, L, false>(a, s, sm.dat, it + 1, blk0);
+    if (crank == 0 && threadIdx.x < RED_BANK) sm.slots[((it & 1) ^ 1) * RED_BANK + threadIdx.x] = 0u;
+    // this CTA's column results are in the row owners' buffers: arrive, and
+    // reduce the error partial while the other CTAs finish pass B
+    cluster_arrive(C);
     {
-      __syncthreads();  // sm.redD may still be read by the projection's cluster sums
       const double t = block_sum(err, sm.redD);
       if (threadIdx.x == 0) s.errPart[(size_t)frame * C + crank] = t;
     }
-    // every read of dat (the projection) is behind the barrier in block_sum:
-    // fetch the next position's intensities into it while C and A run
-    prefetch_data<NP, L, false>(a, s, sm.dat, it + 1, blk0);
-    if (crank == 0 && threadIdx.x < RED_BANK) sm.slots[((it & 1) ^ 1) * RED_BANK + threadIdx.x] = 0u;
-    cluster_sync(C);
+    cluster_wait(C);
 
     // ---------------- C: inverse row FFT and DELTA per mode
     fft_tasks<E, true>(
@@ -766,7 +779,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         },
         [&](int t, float2(&v)[E]) {
           const int k = t / L, l = t % L;
-          const int o = k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
+          const int o = nosm == 1 ? 0 : k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
           const int y = line0 + l;
           const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
           float2* row = sm.rows + t * NP;
@@ -801,6 +814,74 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
       const float pmax1 = slot_value(red, RED_PMAX1);
       const float invPmax2 = 1.f / pmax2, invOmax2 = 1.f / omax2, invPmax1 = 1.f / pmax1;
       const float stepP = a.betaP * a.weightP;
+      if constexpr (FAST) {
+        // one object mode, one wavelength, no mqNewton: each thread takes up
+        // to PPT pixels at once and runs the probe modes outermost, so the
+        // pixels' independent chains interleave; per pixel the arithmetic and
+        // its order are those of the general loop below
+        constexpr int PPT = LN >= 512 ? LN / 512 : 1;
+        auto gObjF = [&](float qp) {
+          if (eng == ENG_EPIE) return invPmax2;
+          if (eng == ENG_MPIE) {
+            float g = 1.f / (a.alphaO * pmax2 + (1.f - a.alphaO) * qp);
+            if (a.fpm) g *= sqrtf(qp) * invPmax2;
+            return g;
+          }
+          return sqrtf(qp) * invPmax1 / (qp + a.regO);
+        };
+        for (int base = 0; base < LN; base += PPT * (int)blockDim.x) {
+          int idx[PPT];
+          float2 O[PPT], accO[PPT];
+          float gP[PPT];
+#pragma unroll
+          for (int q = 0; q < PPT; ++q) {
+            idx[q] = base + (int)threadIdx.x + q * (int)blockDim.x;  // warp-uniform validity
+            O[q] = sm.obj[idx[q] < LN ? idx[q] : 0];
+            accO[q] = make_float2(0.f, 0.f);
+            const float qq = cabs2(O[q]);
+            if (eng == ENG_EPIE)
+              gP[q] = invOmax2;
+            else if (eng == ENG_MPIE)
+              gP[q] = 1.f / (a.alphaP * omax2 + (1.f - a.alphaP) * qq);
+            else
+              gP[q] = sqrtf(qq) / (qq + a.regP);
+          }
+          for (int p = 0; p < npsm; ++p) {
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+              if (idx[q] < LN) {
+                const int i = idx[q];
+                const float2 P = sm.probe[p * pst + i];
+                const float2 d = sm.rows[p * LN + i];
+                accO[q] = cadd(accO[q], cscale(cmulc(P, d), gObjF(cabs2(P))));
+                const float2 accP = cadd(make_float2(0.f, 0.f), cscale(cmulc(O[q], d), gP[q]));
+                if (qn)
+                  sm.U[p * LN + i] = accP;
+                else
+                  sm.probe[p * pst + i] = cadd(P, cscale(accP, stepP));
+              }
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < PPT; ++q) {
+            if (idx[q] < LN) {
+              const int i = idx[q];
+              const int l = i / NP, x = i - (i / NP) * NP;
+              const float2 On = cadd(O[q], cscale(accO[q], a.betaO));
+              st_cg(s.object + (size_t)(row0 + line0 + l) * No + col0 + x, On);
+              if (qn) {
+                const float onew = cabs(On);
+                omaxPatch = fmaxf(omaxPatch, onew);
+                const int tx = (col0 + x) / TILE;
+                const unsigned grp = __match_any_sync(0xffffffffu, tx);
+                const unsigned m = __reduce_max_sync(grp, __float_as_uint(onew));
+                if ((int)lane == __ffs(grp) - 1)
+                  atomicMax(reinterpret_cast<unsigned*>(s.tileMax) + ((row0 + line0 + l) / TILE) * a.tilesPerRow + tx, m);
+              }
+            }
+          }
+        }
+      } else
       for (int i = threadIdx.x; i < LN; i += blockDim.x) {
         float2 O[MAX_OBJECT_MODES], accO[MAX_OBJECT_MODES];
         float gP[MAX_OBJECT_MODES];

@@ -69,6 +69,7 @@ cudaError_t engine_max_clusters_mq(int Np, int cluster, int threads, size_t smem
 cudaError_t launch_engine_mq(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 cudaError_t engine_max_clusters_poly(int Np, int cluster, int threads, size_t smem, int* out);
 cudaError_t launch_engine_poly(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_engine_fast(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 cudaError_t engine_max_clusters_mq_poly(int Np, int cluster, int threads, size_t smem, int* out);
 cudaError_t launch_engine_mq_poly(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 
