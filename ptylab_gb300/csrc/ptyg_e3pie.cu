@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           F, K * L,
           [&](int t, float2(&v)[E]) {
 #pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + 32 * r + lane];
+            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + rsw<L>(t, 32 * r + lane)];
           },
           [&](int t, float2(&v)[E]) {
             const int p = t / L, l = t % L;
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           F, K * L,
           [&](int t, float2(&v)[E]) {
 #pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + 32 * r + lane];
+            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + rsw<L>(t, 32 * r + lane)];
           },
           [&](int t, float2(&v)[E]) {
 #pragma unroll
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           F, K * L,
           [&](int t, float2(&v)[E]) {
 #pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + 32 * r + lane];
+            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + rsw<L>(t, 32 * r + lane)];
           },
           [&](int t, float2(&v)[E]) {
             const int p = t / L, l = t % L;

@@ -200,7 +200,16 @@ PTYG_DEV void scatter_row(float2* tile, const float2 (&v)[E], int k, int y) {
 }
 
 // A column task's result (natural order along y) goes back to the row buffers
-// of the CTAs owning those rows, at Fourier-layout slot sx.
+// of the CTAs owning those rows, at Fourier-layout slot sx.  The lanes of one
+// store write one slot of up to 16 rows (NP * 8 bytes apart), so the slot is
+// swizzled by the row: row task t = k * L + l keeps slot s at t * NP + (s ^ l)
+// (rsw), which spreads those rows over distinct banks and keeps a row read
+// (lanes over s) a permutation within aligned groups of L slots.
+template <int L>
+PTYG_DEV int rsw(int t, int s) {
+  return s ^ (t & (L - 1));
+}
+
 template <int E, int L>
 PTYG_DEV void scatter_column(float2* rows, const float2 (&v)[E], int k, int sx) {
   constexpr int NP = 32 * E;
@@ -209,7 +218,7 @@ PTYG_DEV void scatter_column(float2* rows, const float2 (&v)[E], int k, int sx) 
   for (int j = 0; j < E; ++j) {
     const int y = lane + 32 * j;
     const int owner = y / L, ly = y - (y / L) * L;
-    *dsmem(&rows[(k * L + ly) * NP + sx], owner) = v[j];
+    *dsmem(&rows[(k * L + ly) * NP + (sx ^ ly)], owner) = v[j];
   }
 }
 

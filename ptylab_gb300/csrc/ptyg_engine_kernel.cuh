@@ -724,7 +724,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
           [&](int t, float2(&v)[E]) {
             const float2* row = sm.rows + t * NP;
 #pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = row[32 * r + lane];
+            for (int r = 0; r < E; ++r) v[r] = row[rsw<L>(t, 32 * r + lane)];
           },
           [&](int t, float2(&v)[E]) {
             float2* row = sm.rows + t * NP;
@@ -775,7 +775,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         [&](int t, float2(&v)[E]) {
           const float2* row = sm.rows + t * NP;
 #pragma unroll
-          for (int r = 0; r < E; ++r) v[r] = row[32 * r + lane];
+          for (int r = 0; r < E; ++r) v[r] = row[rsw<L>(t, 32 * r + lane)];
         },
         [&](int t, float2(&v)[E]) {
           const int k = t / L, l = t % L;
