@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/ptyg.h"
+#include "ptyg_common.cuh"
 #include "ptyg_engine.cuh"
 #include "ptyg_ops.cuh"
 
@@ -524,17 +525,10 @@ extern "C" int ptyg_plan_destroy(ptyg_plan* plan) {
 
 // Fourier-layout permutation of a centred table: out[sx][sy] = ifftshift(H)[ky][kx].
 static std::vector<float2> to_fourier_layout_host(const float2* centred, int Np) {
-  const int E = Np / 32;
-  auto bitrev5 = [](int l) {
-    int r = 0;
-    for (int b = 0; b < 5; ++b) r |= ((l >> b) & 1) << (4 - b);
-    return r;
-  };
-  auto k_of = [&](int s) { return (s >> 5) + E * bitrev5(s & 31); };
   std::vector<float2> out((size_t)Np * Np);
   for (int sx = 0; sx < Np; ++sx)
     for (int sy = 0; sy < Np; ++sy) {
-      const int ky = k_of(sy), kx = k_of(sx);
+      const int ky = ptyg::slot_to_freq_y(sy, Np), kx = ptyg::slot_to_freq_x(sx, Np);
       // ifftshift: element k of the shifted array is element (k + Np/2) % Np of the centred one
       const int cy = (ky + Np / 2) % Np, cx = (kx + Np / 2) % Np;
       out[(size_t)sx * Np + sy] = centred[(size_t)cy * Np + cx];

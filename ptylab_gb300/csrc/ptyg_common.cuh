@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #define PTYG_DEV __device__ __forceinline__
 
 namespace ptyg {
@@ -422,35 +424,201 @@ struct WarpFFT {
   PTYG_DEV void inv(float2 (&v)[E]) const { invm<1>(reinterpret_cast<float2(&)[1][E]>(v)); }
 };
 
-// Run `ntasks` independent line transforms over the warps of the CTA, two
-// per warp at a time: load(task, v) fills a line, store(task, v) consumes the
-// transformed line.  A __syncwarp separates the loads of a pair from its
-// stores, so a task may store in place of what it loaded.
+// 128-point lines, four per warp, with one shared-memory exchange.
+//
+// Lanes 16P .. 16P+15 (line pair P = lane / 16) hold lines 2P and 2P+1 as
+// the two halves of packed FP32 pairs (CPair), 8 points per thread:
+//   natural layout   : thread u = lane % 16, register a  <->  n = u + 16 a
+//   frequency layout : thread v = lane % 16, register d  <->  k = v + 16 d
+// so the frequency layout is plain frequency order, read and written by the
+// same 16-consecutive-index pattern as the natural one.  With n = u + 16 a and
+// k = b + 8 e + 16 d (b < 8, e < 2, d < 8):
+//   W128^(nk) = W8^(ab) W128^(ub) W16^(ie) W2^(he) W8^(id),  u = i + 8 h.
+// The forward transform is an 8-point DFT over a in registers, the twiddle
+// W128^(ub), an exchange through shared memory that gives thread v = b + 8 h
+// the values Y[i + 8h][b] (i < 8), a radix-2 butterfly between lanes v and
+// v ^ 8 (h -> e), the twiddle W16^(ie) on e = 1, and an 8-point DFT over i.
+// The inverse is its exact mirror with conjugate twiddles (unnormalised:
+// inverse(forward(x)) = 128 x).
+//
+// The exchange uses 128 16-byte entries per line pair (a CPair: both lines'
+// real parts, then both imaginary parts), e.g. the pair's own two line
+// buffers when the lines are transformed in place: Y[u][b] sits in entry
+// 16 b + (u ^ b), so that the writes (lanes over u) and the reads (lanes over
+// (b, h): entry 16 b + (v ^ i)) each touch 8 distinct 16-byte bank groups per
+// quarter-warp.
+struct Fft128 {
+  float2 tw[7];  // W128^(u * b), b = 1..7
+  unsigned lane;
+
+  // `table` is the 128-entry table W128^m (global or shared memory).
+  PTYG_DEV void init(const float2* table, unsigned ln) {
+    lane = ln;
+    const int u = (int)(ln & 15);
+#pragma unroll
+    for (int b = 1; b < 8; ++b) tw[b - 1] = table[(u * b) & 127];
+  }
+
+  template <bool INV>
+  PTYG_DEV void exchange(CPair (&p)[8], float4* xs) const {
+    const int u = (int)(lane & 15), b = u & 7;
+    float4* wr = INV ? xs + 16 * b : xs;  // write side: entry 16 j + (u ^ j) (fwd), 16 b + (u ^ j) (inv)
+    float4* rd = INV ? xs : xs + 16 * b;
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int e = (INV ? 0 : 16 * j) + (u ^ j);
+      wr[e] = make_float4(p[j].re.x, p[j].re.y, p[j].im.x, p[j].im.y);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int e = (INV ? 16 * j : 0) + (u ^ j);
+      const float4 z = rd[e];
+      p[j] = CPair{make_float2(z.x, z.y), make_float2(z.z, z.w)};
+    }
+    __syncwarp();
+  }
+
+  // radix-2 between lanes v and v ^ 8: lower mine + other, upper other - mine
+  PTYG_DEV void cross(CPair (&p)[8]) const {
+    const float2 sg = pdup((lane & 8) ? -1.f : 1.f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float2 ore, oim;
+      ore.x = __shfl_xor_sync(0xffffffffu, p[j].re.x, 8);
+      ore.y = __shfl_xor_sync(0xffffffffu, p[j].re.y, 8);
+      oim.x = __shfl_xor_sync(0xffffffffu, p[j].im.x, 8);
+      oim.y = __shfl_xor_sync(0xffffffffu, p[j].im.y, 8);
+      p[j] = CPair{pfma(sg, p[j].re, ore), pfma(sg, p[j].im, oim)};
+    }
+  }
+
+  PTYG_DEV void fwd(CPair (&p)[8], float4* xs) const {
+    pdft_reg<8, false>(p);
+#pragma unroll
+    for (int b = 1; b < 8; ++b) p[b] = pcmul(p[b], pdup(tw[b - 1].x), pdup(tw[b - 1].y), pdup(-tw[b - 1].y));
+    exchange<false>(p, xs);
+    cross(p);
+    if (lane & 8) {
+#pragma unroll
+      for (int i = 1; i < 8; ++i) p[i] = pmul_w16<false>(p[i], i);
+    }
+    pdft_reg<8, false>(p);
+  }
+
+  PTYG_DEV void inv(CPair (&p)[8], float4* xs) const {
+    pdft_reg<8, true>(p);
+    if (lane & 8) {
+#pragma unroll
+      for (int i = 1; i < 8; ++i) p[i] = pmul_w16<true>(p[i], i);
+    }
+    cross(p);
+    exchange<true>(p, xs);
+#pragma unroll
+    for (int b = 1; b < 8; ++b) p[b] = pcmulc(p[b], pdup(tw[b - 1].x), pdup(tw[b - 1].y), pdup(-tw[b - 1].y));
+    pdft_reg<8, true>(p);
+  }
+};
+
+// Fourier-plane slot order of the line transforms, per axis, for lines of Np
+// points.  Rows (x) at Np = 128 use Fft128: slot = frequency.  Columns (y),
+// and rows at other sizes, use WarpFFT: slot 32 r + l holds k = r + E bitrev5(l).
+__host__ __device__ inline int slot_bitrev5(int l) {
+  int r = 0;
+  for (int b = 0; b < 5; ++b) r |= ((l >> b) & 1) << (4 - b);
+  return r;
+}
+__host__ __device__ inline int slot_to_freq_y(int s, int Np) {
+  return (s >> 5) + (Np / 32) * slot_bitrev5(s & 31);
+}
+__host__ __device__ inline int freq_to_slot_y(int k, int Np) {
+  const int E = Np / 32;
+  return 32 * (k % E) + slot_bitrev5(k / E);
+}
+__host__ __device__ inline int slot_to_freq_x(int s, int Np) { return Np == 128 ? s : slot_to_freq_y(s, Np); }
+__host__ __device__ inline int freq_to_slot_x(int k, int Np) { return Np == 128 ? k : freq_to_slot_y(k, Np); }
+
+// Run `ntasks` independent line transforms over the warps of the CTA with
+// WarpFFT, two per warp at a time.  Element-wise callbacks: load(task, lo,
+// hi) returns element lo + hi of the line (natural index for the forward
+// transform, Fourier slot for the inverse), store(task, lo, hi, value) takes
+// element lo + hi of the result (slot, resp. natural index); lo = lane is the
+// thread's part of the index and hi = 32 j a compile-time multiple of 32, so
+// callers can keep addresses affine.  A __syncwarp separates the loads of a
+// pair from its stores, so a task may store in place of what it loaded.
 template <int E, bool INV, class LoadF, class StoreF>
 PTYG_DEV void fft_tasks(const WarpFFT<E>& F, int ntasks, LoadF&& load, StoreF&& store) {
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
   int t = warp;
   for (; t + nw < ntasks; t += 2 * nw) {
     float2 v[2][E];
-    load(t, v[0]);
-    load(t + nw, v[1]);
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      v[0][j] = load(t, lane, 32 * j);
+      v[1][j] = load(t + nw, lane, 32 * j);
+    }
     if (INV)
       F.inv2(v);
     else
       F.fwd2(v);
     __syncwarp();
-    store(t, v[0]);
-    store(t + nw, v[1]);
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      store(t, lane, 32 * j, v[0][j]);
+      store(t + nw, lane, 32 * j, v[1][j]);
+    }
   }
   if (t < ntasks) {
     float2 v[E];
-    load(t, v);
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = load(t, lane, 32 * j);
     if (INV)
       F.inv(v);
     else
       F.fwd(v);
     __syncwarp();
-    store(t, v);
+#pragma unroll
+    for (int j = 0; j < E; ++j) store(t, lane, 32 * j, v[j]);
+  }
+}
+
+// Row transforms: at Np = 128 with Fft128, four lines per warp (ntasks must
+// be a multiple of 4), lo = lane % 16 and hi = 16 a; `pairs(t)` (t even) is
+// the 128-entry exchange buffer of lines t and t + 1 (their own two row
+// buffers when transformed in place: every load of a line pair precedes its
+// first exchange write).  Other sizes run fft_tasks with WarpFFT.
+template <int E, bool INV, class LoadF, class StoreF, class PairF>
+PTYG_DEV void row_tasks(const float2* twiddle, int ntasks, LoadF&& load, StoreF&& store, PairF&& pairs) {
+  const int lane = threadIdx.x & 31;
+  if constexpr (E == 4) {
+    Fft128 F;
+    F.init(twiddle, (unsigned)lane);
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int P = lane >> 4, u = lane & 15;
+    for (int g = warp; 4 * g < ntasks; g += nw) {
+      const int t0 = 4 * g + 2 * P, t1 = t0 + 1;
+      CPair p[8];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const float2 x0 = load(t0, u, 16 * a), x1 = load(t1, u, 16 * a);
+        p[a] = CPair{make_float2(x0.x, x1.x), make_float2(x0.y, x1.y)};
+      }
+      if (INV)
+        F.inv(p, pairs(t0));
+      else
+        F.fwd(p, pairs(t0));
+#pragma unroll
+      for (int d = 0; d < 8; ++d) {
+        store(t0, u, 16 * d, make_float2(p[d].re.x, p[d].im.x));
+        store(t1, u, 16 * d, make_float2(p[d].re.y, p[d].im.y));
+      }
+    }
+  } else {
+    WarpFFT<E> F;
+    F.init(twiddle, (unsigned)lane);
+    fft_tasks<E, INV>(F, ntasks, load, store);
   }
 }
 

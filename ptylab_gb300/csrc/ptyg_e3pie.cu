@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
 
   if (threadIdx.x < 2 * RED_BANK) slots[threadIdx.x] = 0u;
   prefetch_data<NP, L>(a, s, dat, 0, blk0);
-  WarpFFT<E> F;
+  WarpFFT<E> F;  // the column transforms (rows: row_tasks)
   F.init(a.twiddle, lane);
   __syncthreads();
   cluster_sync(C);
@@ -103,20 +103,19 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
     }
 
     // ---------------- slice 0 exit waves, forward row FFT
-    fft_tasks<E, false>(
-        F, K * L,
-        [&](int t, float2(&v)[E]) {
-          const int p = t / L, l = t % L;
-          const int y = line0 + l;
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const int x = lane + 32 * j;
-            const float2 e = cmul(ld_cg(Ob(0) + (size_t)l * No + x), Pb(p, 0)[l * NP + x]);
-            Wb(0, p)[l * NP + x] = e;
-            v[j] = (S == 1) ? detector_in(e, y, x) : e;
-          }
+    // every row-buffer line is a transform's own buffer (in place) or free
+    auto row = [&](int t, int i) -> float2& { return rows[t * NP + i]; };
+    auto pairs = [&](int t) { return reinterpret_cast<float4*>(rows + t * NP); };
+    auto scatter = [&](int t, int lo, int hi, float2 v) { scatter_row<NP, L>(tile, t / L, line0 + t % L, lo, hi, v); };
+    row_tasks<E, false>(
+        a.twiddle, K * L,
+        [&](int t, int lo, int hi) {
+          const int p = t / L, l = t % L, x = lo + hi;
+          const float2 e = cmul(ld_cg(Ob(0) + (size_t)l * No + x), Pb(p, 0)[l * NP + x]);
+          Wb(0, p)[l * NP + x] = e;
+          return (S == 1) ? detector_in(e, line0 + l, x) : e;
         },
-        [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+        scatter, pairs);
     cp_async_wait_prev();  // this position's intensities
     cluster_sync(C);
 
@@ -125,21 +124,13 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       column_filter<E, L>(tile, rows, F, a.sliceH, false, crank, K, K);
       cluster_sync(C);
       // P_s rows (natural order) into the row buffer and the probe's slice sl
-      fft_tasks<E, true>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-#pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + rsw<L>(t, 32 * r + lane)];
+      row_tasks<E, true>(
+          a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, rsw<L>(t, lo) + hi); },
+          [&](int t, int lo, int hi, float2 v) {
+            row(t, lo + hi) = v;
+            Pb(t / L, sl)[(t % L) * NP + lo + hi] = v;
           },
-          [&](int t, float2(&v)[E]) {
-            const int p = t / L, l = t % L;
-#pragma unroll
-            for (int j = 0; j < E; ++j) {
-              const int x = lane + 32 * j;
-              rows[t * NP + x] = v[j];
-              Pb(p, sl)[l * NP + x] = v[j];
-            }
-          });
+          pairs);
       __syncthreads();
       {
         float m[1] = {0.f};
@@ -161,31 +152,18 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
         block_max_to_slots<1>(m, redF, red, idx);
       }
       __syncthreads();
-      fft_tasks<E, false>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-#pragma unroll
-            for (int j = 0; j < E; ++j) v[j] = rows[t * NP + lane + 32 * j];
-          },
-          [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+      row_tasks<E, false>(
+          a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, lo + hi); }, scatter, pairs);
       cluster_sync(C);
     }
 
     // ---------------- detector intensity projection (BaseEngine.py:870-1012)
     double err = 0.0;
     if (!asp) {
+      auto col = [&](int t, int i) -> float2& { return tile[tix<L>((t / L) * NP + i, t % L)]; };
       fft_tasks<E, false>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-            const int k = t / L, c = t % L;
-#pragma unroll
-            for (int j = 0; j < E; ++j) v[j] = tile[tix<L>(k * NP + lane + 32 * j, c)];
-          },
-          [&](int t, float2(&v)[E]) {
-            const int k = t / L, c = t % L;
-#pragma unroll
-            for (int r = 0; r < E; ++r) tile[tix<L>(k * NP + 32 * r + lane, c)] = v[r];
-          });
+          F, K * L, [&](int t, int lo, int hi) { return col(t, lo + hi); },
+          [&](int t, int lo, int hi, float2 v) { col(t, lo + hi) = v; });
       __syncthreads();
       {
         float e = 0.f;
@@ -205,27 +183,16 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       }
       __syncthreads();
       fft_tasks<E, true>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-            const int k = t / L, c = t % L;
-#pragma unroll
-            for (int r = 0; r < E; ++r)
-              v[r] = cscale(tile[tix<L>(k * NP + 32 * r + lane, c)], fr[c * NP + 32 * r + lane]);
-          },
-          [&](int t, float2(&v)[E]) { scatter_column<E, L>(rows, v, t / L, sx0 + t % L); });
+          F, K * L, [&](int t, int lo, int hi) { return cscale(col(t, lo + hi), fr[(t % L) * NP + lo + hi]); },
+          [&](int t, int lo, int hi, float2 v) { col(t, lo + hi) = v; });
+      __syncthreads();
+      flush_columns<NP, L>(tile, rows, K, sx0);
     } else {
       column_filter<E, L>(tile, rows, F, a.aspH, false, crank, K, K);
       cluster_sync(C);
-      fft_tasks<E, true>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-#pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + rsw<L>(t, 32 * r + lane)];
-          },
-          [&](int t, float2(&v)[E]) {
-#pragma unroll
-            for (int j = 0; j < E; ++j) rows[t * NP + lane + 32 * j] = v[j];
-          });
+      row_tasks<E, true>(
+          a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, rsw<L>(t, lo) + hi); },
+          [&](int t, int lo, int hi, float2 v) { row(t, lo + hi) = v; }, pairs);
       __syncthreads();
       {
         float e = 0.f;
@@ -242,17 +209,9 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
         err = (double)e;
       }
       __syncthreads();
-      fft_tasks<E, false>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-            const int l = t % L;
-#pragma unroll
-            for (int j = 0; j < E; ++j) {
-              const int x = lane + 32 * j;
-              v[j] = cscale(rows[t * NP + x], fr[l * NP + x]);
-            }
-          },
-          [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+      row_tasks<E, false>(
+          a.twiddle, K * L, [&](int t, int lo, int hi) { return cscale(row(t, lo + hi), fr[(t % L) * NP + lo + hi]); },
+          scatter, pairs);
       cluster_sync(C);
       column_filter<E, L>(tile, rows, F, a.aspH, true, crank, K, K);
     }
@@ -268,26 +227,19 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       // DELTA into the row buffer (natural order): the detector's back-propagated
       // last slice minus esw_{S-1}, or the back-propagated P_{sl+1} minus esw_sl
       const bool fromDetector = sl == S - 1;
-      fft_tasks<E, true>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-#pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = rows[t * NP + rsw<L>(t, 32 * r + lane)];
-          },
-          [&](int t, float2(&v)[E]) {
+      row_tasks<E, true>(
+          a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, rsw<L>(t, lo) + hi); },
+          [&](int t, int lo, int hi, float2 v) {
             const int p = t / L, l = t % L;
-            const int y = line0 + l;
-#pragma unroll
-            for (int j = 0; j < E; ++j) {
-              const int x = lane + 32 * j;
-              float2 u = v[j];
-              if (fromDetector && !asp) {
-                if (centred && ((y + x) & 1)) u = cscale(u, -1.f);
-                if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + x), u);
-              }
-              rows[t * NP + x] = csub(u, Wb(sl, p)[l * NP + x]);
+            const int y = line0 + l, x = lo + hi;
+            float2 u = v;
+            if (fromDetector && !asp) {
+              if (centred && ((y + x) & 1)) u = cscale(u, -1.f);
+              if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + x), u);
             }
-          });
+            row(t, x) = csub(u, Wb(sl, p)[l * NP + x]);
+          },
+          pairs);
       __syncthreads();
       // O_sl and P_sl steps (e3PIE.py:192-225) with the pre-update slices
       {
@@ -314,13 +266,8 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       if (sl > 0) {
         // back-propagate the updated P_sl by conj(H)
         __syncthreads();
-        fft_tasks<E, false>(
-            F, K * L,
-            [&](int t, float2(&v)[E]) {
-#pragma unroll
-              for (int j = 0; j < E; ++j) v[j] = rows[t * NP + lane + 32 * j];
-            },
-            [&](int t, float2(&v)[E]) { scatter_row<E, L>(tile, v, t / L, line0 + t % L); });
+        row_tasks<E, false>(
+            a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, lo + hi); }, scatter, pairs);
         cluster_sync(C);
         column_filter<E, L>(tile, rows, F, a.sliceH, true, crank, K, K);
         cluster_sync(C);

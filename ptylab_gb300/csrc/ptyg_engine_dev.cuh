@@ -185,80 +185,99 @@ PTYG_DEV int tix(int row, int c) {
   return row * L + (c ^ ((row / (16 / L)) & (L - 1)));
 }
 
-// A row task's transformed row (Fourier layout: register r, lane l is slot
-// 32r + l) goes to the column blocks of the CTAs owning those slots.
-template <int E, int L>
-PTYG_DEV void scatter_row(float2* tile, const float2 (&v)[E], int k, int y) {
-  constexpr int NP = 32 * E;
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int r = 0; r < E; ++r) {
-    const int sx = 32 * r + lane;
-    const int owner = sx / L, c = sx - (sx / L) * L;
-    *dsmem(&tile[tix<L>(k * NP + y, c)], owner) = v[r];
-  }
+// Store into the shared memory of cluster rank `rank` at the address `local`
+// has in this CTA (mapa on the 32-bit shared-window address).
+PTYG_DEV void st_cluster(const float2* local, int rank, float2 v) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+  unsigned r;
+  asm("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};\n" ::"r"(r), "f"(v.x), "f"(v.y));
+}
+PTYG_DEV void st_cluster4(const float4* local, int rank, float4 v) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+  unsigned r;
+  asm("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"r"(r), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
 }
 
-// A column task's result (natural order along y) goes back to the row buffers
-// of the CTAs owning those rows, at Fourier-layout slot sx.  The lanes of one
-// store write one slot of up to 16 rows (NP * 8 bytes apart), so the slot is
-// swizzled by the row: row task t = k * L + l keeps slot s at t * NP + (s ^ l)
-// (rsw), which spreads those rows over distinct banks and keeps a row read
-// (lanes over s) a permutation within aligned groups of L slots.
+// Element lo + hi (a Fourier slot; hi a multiple of L) of the transformed row
+// y of mode k goes to the column block of the CTA owning that slot.
+template <int NP, int L>
+PTYG_DEV void scatter_row(float2* tile, int k, int y, int lo, int hi, float2 v) {
+  st_cluster(&tile[tix<L>(k * NP + y, lo % L)], lo / L + hi / L, v);
+}
+
+// Row buffers (K * L rows of NP, Fourier layout along x) are written by the
+// column owners and read along rows, so the slot is swizzled by the row: row
+// task t = k * L + l keeps slot s at t * NP + (s ^ l) (rsw).  XOR with l < L
+// permutes slots within aligned groups of L, so a column block stays one
+// contiguous span of every row.
 template <int L>
 PTYG_DEV int rsw(int t, int s) {
   return s ^ (t & (L - 1));
 }
 
+// A column task stores its result (natural order along y) in its own column of
+// the CTA's tile, row k * NP + y; once every column task of the CTA is done
+// (a CTA barrier), flush_columns sends the tile to the row owners' row
+// buffers.  Each thread moves two neighbouring columns of one row (16 bytes),
+// and the L / 2 threads of a row write its whole column block, L * 8
+// contiguous bytes of the owner's buffer: one remote line per row instead of
+// one 8-byte remote store per column and row.
+template <int NP, int L>
+PTYG_DEV void flush_columns(const float2* tile, float2* rows, int K, int sx0) {
+  constexpr int PAIRS = L / 2;
+  const int n = K * NP * PAIRS;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int r = i / PAIRS, c = 2 * (i - (i / PAIRS) * PAIRS);  // tile row k * NP + y, even column c
+    const int k = r / NP, y = r - (r / NP) * NP;
+    const int sw = (r / (16 / L)) & (L - 1);  // the tix swizzle of row r
+    // columns c, c + 1 sit at (c ^ sw) and (c ^ sw) ^ 1: one aligned pair, swapped when sw is odd
+    const float4 f = *reinterpret_cast<const float4*>(tile + r * L + ((c ^ sw) & ~1));
+    const int owner = y / L, ly = y - (y / L) * L;
+    // in the owner's row, slots sx0 + c and sx0 + c + 1 sit at ((sx0 + c) ^ ly) and that ^ 1
+    const int pos = (k * L + ly) * NP + (((sx0 + c) ^ ly) & ~1);
+    const float4 o = ((sw ^ ly) & 1) ? make_float4(f.z, f.w, f.x, f.y) : f;
+    st_cluster4(reinterpret_cast<const float4*>(rows + pos), owner, o);
+  }
+}
+
+// The column task's store into its own tile column (natural order along y).
 template <int E, int L>
-PTYG_DEV void scatter_column(float2* rows, const float2 (&v)[E], int k, int sx) {
+PTYG_DEV void store_column(float2* tile, const float2 (&v)[E], int k, int c) {
   constexpr int NP = 32 * E;
   const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int j = 0; j < E; ++j) {
-    const int y = lane + 32 * j;
-    const int owner = y / L, ly = y - (y / L) * L;
-    *dsmem(&rows[(k * L + ly) * NP + (sx ^ ly)], owner) = v[j];
-  }
+  for (int j = 0; j < E; ++j) tile[tix<L>(k * NP + lane + 32 * j, c)] = v[j];
 }
 
 // Column pass that multiplies the spectrum by H (or conj H) / Np^2 between a
 // forward and an inverse column transform (ASP, Operators.py:155-230); the
-// result goes to the row owners' row buffers.
+// result goes to the row owners' row buffers (visible after a cluster barrier).
+// Column task t = k * L + c is transformed in place in the tile.
 template <int E, int L, bool SETS = false>
 PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, const float2* H, bool conjH, int crank,
                             int K, int kPerSet) {
   constexpr int NP = 32 * E;
-  const int lane = threadIdx.x & 31;
   const int sx0 = crank * L;
   const float inv2 = 1.f / (float)(NP * NP);
+  auto col = [&](int t, int i) -> float2& { return tile[tix<L>((t / L) * NP + i, t % L)]; };
   fft_tasks<E, false>(
-      F, K * L,
-      [&](int t, float2(&v)[E]) {
-        const int k = t / L, c = t % L;
-#pragma unroll
-        for (int j = 0; j < E; ++j) v[j] = tile[tix<L>(k * NP + lane + 32 * j, c)];
-      },
-      [&](int t, float2(&v)[E]) {
+      F, K * L, [&](int t, int lo, int hi) { return col(t, lo + hi); },
+      [&](int t, int lo, int hi, float2 v) {
         const int k = t / L, c = t % L;
         // SETS: one table per wavelength, modes k of wavelength k / kPerSet
         const float2* h = H + (SETS ? (size_t)(k / kPerSet) * NP * NP : 0) + (size_t)(sx0 + c) * NP;
-#pragma unroll
-        for (int r = 0; r < E; ++r) {
-          float2 hv = __ldg(h + r * 32 + lane);
-          if (conjH) hv.y = -hv.y;
-          tile[tix<L>(k * NP + 32 * r + lane, c)] = cscale(cmul(v[r], hv), inv2);
-        }
+        float2 hv = __ldg(h + lo + hi);
+        if (conjH) hv.y = -hv.y;
+        col(t, lo + hi) = cscale(cmul(v, hv), inv2);
       });
   __syncthreads();
   fft_tasks<E, true>(
-      F, K * L,
-      [&](int t, float2(&v)[E]) {
-        const int k = t / L, c = t % L;
-#pragma unroll
-        for (int r = 0; r < E; ++r) v[r] = tile[tix<L>(k * NP + 32 * r + lane, c)];
-      },
-      [&](int t, float2(&v)[E]) { scatter_column<E, L>(rows, v, t / L, sx0 + t % L); });
+      F, K * L, [&](int t, int lo, int hi) { return col(t, lo + hi); },
+      [&](int t, int lo, int hi, float2 v) { col(t, lo + hi) = v; });
+  __syncthreads();
+  flush_columns<NP, L>(tile, rows, K, sx0);
 }
 
 // Prefetch the measured intensities of order slot `it` (if it exists and is a

@@ -393,7 +393,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
   }
   if (threadIdx.x < 2 * RED_BANK) sm.slots[threadIdx.x] = 0u;
   prefetch_data<NP, L, false>(a, s, sm.dat, 0, blk0);
-  WarpFFT<E> F;
+  WarpFFT<E> F;  // the column transforms (rows: row_tasks)
   F.init(a.twiddle, lane);
   // mqNewton second moments: every CTA of the cluster carries the same values
   float vO = 0.f, vP = 0.f;
@@ -476,22 +476,19 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
       const int idx[4] = {RED_PMAX2, RED_OMAX2, RED_PMAX1, RED_OMAXW};
       block_max_to_slots<4>(mx, sm.redF, red, idx);
     }
-    fft_tasks<E, false>(
-        F, K * L,
-        [&](int t, float2(&v)[E]) {
+    // (the row buffers are free until pass B writes them: exchange buffers)
+    row_tasks<E, false>(
+        a.twiddle, K * L,
+        [&](int t, int lo, int hi) {
           const int k = t / L, l = t % L;
           const int o = nosm == 1 ? 0 : k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
           const int y = line0 + l;
-          const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const int x = lane + 32 * j;
-            float2 e = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[p * pst + l * NP + x]);
-            if (fresnel) e = cmul(e, __ldg(a.fresnelQ + y * NP + x));
-            v[j] = cscale(e, sg);
-          }
+          float2 e = cmul(sm.obj[(o * L + l) * NP + lo + hi], sm.probe[p * pst + l * NP + lo + hi]);
+          if (fresnel) e = cmul(e, __ldg(a.fresnelQ + y * NP + lo + hi));
+          return cscale(e, (centred && !asp && ((y + lo) & 1)) ? -1.f : 1.f);  // hi is even
         },
-        [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm.tile, v, t / L, line0 + t % L); });
+        [&](int t, int lo, int hi, float2 v) { scatter_row<NP, L>(sm.tile, t / L, line0 + t % L, lo, hi, v); },
+        [&](int t) { return reinterpret_cast<float4*>(sm.rows + t * NP); });
     cp_async_wait_all();  // this position's intensities (the one group in flight)
     cluster_sync(C);
 
@@ -634,7 +631,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         __syncwarp();
         colStore(k, v);
       }
-      err = project([&](int r) { return ie[r] * inv2; }, inv2, std::true_type{});
+      err = project([&](int r) { return __fmul_rn(ie[r], inv2); }, inv2, std::true_type{});
       __syncwarp();
       auto invLoad = [&](int kk, float2(&v)[E]) {
 #pragma unroll
@@ -646,29 +643,25 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         invLoad(k, v[0]);
         invLoad(k + 1, v[1]);
         F.inv2(v);
-        scatter_column<E, L>(sm.rows, v[0], k, sx0 + c);
-        scatter_column<E, L>(sm.rows, v[1], k + 1, sx0 + c);
+        __syncwarp();  // the column is stored in place of what the warp loaded
+        store_column<E, L>(sm.tile, v[0], k, c);
+        store_column<E, L>(sm.tile, v[1], k + 1, c);
       }
       if (k < K) {
         float2 v[E];
         invLoad(k, v);
         F.inv(v);
-        scatter_column<E, L>(sm.rows, v, k, sx0 + c);
+        __syncwarp();
+        store_column<E, L>(sm.tile, v, k, c);
       }
+      __syncthreads();
+      flush_columns<NP, L>(sm.tile, sm.rows, K, sx0);
     } else if (!asp) {
       // ---------------- B: Fourier-plane intensity projection (BaseEngine.py:870-1012)
+      auto col = [&](int t, int i) -> float2& { return sm.tile[tix<L>((t / L) * NP + i, t % L)]; };
       fft_tasks<E, false>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-            const int k = t / L, c = t % L;
-#pragma unroll
-            for (int j = 0; j < E; ++j) v[j] = sm.tile[tix<L>(k * NP + lane + 32 * j, c)];
-          },
-          [&](int t, float2(&v)[E]) {
-            const int k = t / L, c = t % L;
-#pragma unroll
-            for (int r = 0; r < E; ++r) sm.tile[tix<L>(k * NP + 32 * r + lane, c)] = v[r];
-          });
+          F, K * L, [&](int t, int lo, int hi) { return col(t, lo + hi); },
+          [&](int t, int lo, int hi, float2 v) { col(t, lo + hi) = v; });
       __syncthreads();
       // interferometric: the reference field of this CTA's pixels, plane k at
       // + k * NP * NP, held as N M R in the tile's scale and sign
@@ -685,7 +678,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
             } else {
               for (int k = 0; k < K; ++k) ie += cabs2(sm.tile[tix<L>(k * NP + sy, c)]);
             }
-            return ie * inv2;
+            return __fmul_rn(ie, inv2);  // explicit rounding: every column path rounds alike
           },
           inv2, std::false_type{});
       if (interf) {
@@ -707,30 +700,19 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
       }
       __syncthreads();
       fft_tasks<E, true>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-            const int k = t / L, c = t % L;
-#pragma unroll
-            for (int r = 0; r < E; ++r)
-              v[r] = cscale(sm.tile[tix<L>(k * NP + 32 * r + lane, c)], sm.fr[c * NP + 32 * r + lane]);
-          },
-          [&](int t, float2(&v)[E]) { scatter_column<E, L>(sm.rows, v, t / L, sx0 + t % L); });
+          F, K * L, [&](int t, int lo, int hi) { return cscale(col(t, lo + hi), sm.fr[(t % L) * NP + lo + hi]); },
+          [&](int t, int lo, int hi, float2 v) { col(t, lo + hi) = v; });
+      __syncthreads();
+      flush_columns<NP, L>(sm.tile, sm.rows, K, sx0);
     } else {
       // ---------------- ASP: x H, real-space projection, x conj(H)
       column_filter<E, L, POLY>(sm.tile, sm.rows, F, a.aspH, false, crank, K, nosmW * npsmW);
       cluster_sync(C);
-      fft_tasks<E, true>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-            const float2* row = sm.rows + t * NP;
-#pragma unroll
-            for (int r = 0; r < E; ++r) v[r] = row[rsw<L>(t, 32 * r + lane)];
-          },
-          [&](int t, float2(&v)[E]) {
-            float2* row = sm.rows + t * NP;
-#pragma unroll
-            for (int j = 0; j < E; ++j) row[lane + 32 * j] = v[j];
-          });
+      auto row = [&](int t, int i) -> float2& { return sm.rows[t * NP + i]; };
+      auto pairs = [&](int t) { return reinterpret_cast<float4*>(sm.rows + t * NP); };
+      row_tasks<E, true>(
+          a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, rsw<L>(t, lo) + hi); },
+          [&](int t, int lo, int hi, float2 v) { row(t, lo + hi) = v; }, pairs);
       __syncthreads();
       err = project(
           [&](int i) {
@@ -740,17 +722,9 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
           },
           1.f, std::false_type{});
       __syncthreads();
-      fft_tasks<E, false>(
-          F, K * L,
-          [&](int t, float2(&v)[E]) {
-            const int l = t % L;
-#pragma unroll
-            for (int j = 0; j < E; ++j) {
-              const int x = lane + 32 * j;
-              v[j] = cscale(sm.rows[t * NP + x], sm.fr[l * NP + x]);
-            }
-          },
-          [&](int t, float2(&v)[E]) { scatter_row<E, L>(sm.tile, v, t / L, line0 + t % L); });
+      row_tasks<E, false>(
+          a.twiddle, K * L, [&](int t, int lo, int hi) { return cscale(row(t, lo + hi), sm.fr[(t % L) * NP + lo + hi]); },
+          [&](int t, int lo, int hi, float2 v) { scatter_row<NP, L>(sm.tile, t / L, line0 + t % L, lo, hi, v); }, pairs);
       cluster_sync(C);
       column_filter<E, L, POLY>(sm.tile, sm.rows, F, a.aspH, true, crank, K, nosmW * npsmW);
     }
@@ -770,28 +744,19 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
     cluster_wait(C);
 
     // ---------------- C: inverse row FFT and DELTA per mode
-    fft_tasks<E, true>(
-        F, K * L,
-        [&](int t, float2(&v)[E]) {
-          const float2* row = sm.rows + t * NP;
-#pragma unroll
-          for (int r = 0; r < E; ++r) v[r] = row[rsw<L>(t, 32 * r + lane)];
-        },
-        [&](int t, float2(&v)[E]) {
+    row_tasks<E, true>(
+        a.twiddle, K * L, [&](int t, int lo, int hi) { return sm.rows[t * NP + rsw<L>(t, lo) + hi]; },
+        [&](int t, int lo, int hi, float2 v) {
           const int k = t / L, l = t % L;
           const int o = nosm == 1 ? 0 : k / npsmW, p = (nl == 1 ? 0 : (o / nosmW) * npsmW) + (k - o * npsmW);
           const int y = line0 + l;
-          const float sg = (centred && !asp && ((y + lane) & 1)) ? -1.f : 1.f;
-          float2* row = sm.rows + t * NP;
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const int x = lane + 32 * j;
-            float2 u = cscale(v[j], sg);
-            if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + x), u);
-            const float2 esw = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[p * pst + l * NP + x]);
-            row[x] = csub(u, esw);
-          }
-        });
+          const int x = lo + hi;
+          float2 u = cscale(v, (centred && !asp && ((y + lo) & 1)) ? -1.f : 1.f);  // hi is even
+          if (fresnel) u = cmulc(__ldg(a.fresnelQ + y * NP + x), u);
+          const float2 esw = cmul(sm.obj[(o * L + l) * NP + x], sm.probe[p * pst + l * NP + x]);
+          sm.rows[t * NP + x] = csub(u, esw);
+        },
+        [&](int t) { return reinterpret_cast<float4*>(sm.rows + t * NP); });
     __syncthreads();
 
     // ---------------- C: object and probe steps, pixel by pixel

@@ -202,17 +202,15 @@ cudaError_t prop_cols(int Np, const float2* in, float2* out, int batch, const Co
 }
 
 // ----------------------------------------------------------------- layouts
-PTYG_DEV int slot_to_index(int s, int E) { return (s >> 5) + E * (int)bitrev5((unsigned)(s & 31)); }
 
 // out[f][sx][sy] = in[f][ky(sy)][kx(sx)]  (natural -> Fourier layout, transposed)
 __global__ void to_fourier_layout_kernel(const float* __restrict__ in, float* __restrict__ out, int frames, int Np) {
   const size_t n = (size_t)frames * Np * Np;
-  const int E = Np / 32;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const size_t f = i / ((size_t)Np * Np);
     const int rem = (int)(i - f * Np * Np);
     const int sx = rem / Np, sy = rem % Np;
-    out[i] = in[(f * Np + slot_to_index(sy, E)) * Np + slot_to_index(sx, E)];
+    out[i] = in[(f * Np + slot_to_freq_y(sy, Np)) * Np + slot_to_freq_x(sx, Np)];
   }
 }
 
@@ -221,11 +219,10 @@ __global__ void to_fourier_layout_kernel(const float* __restrict__ in, float* __
 // transforms, 1 otherwise), so the field is kept as N M R.  Initial R = 1.
 __global__ void reference_init_kernel(float2* __restrict__ out, int planes, int Np, int centred) {
   const size_t n = (size_t)planes * Np * Np;
-  const int E = Np / 32;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int rem = (int)(i % ((size_t)Np * Np));
     const int sx = rem / Np, sy = rem % Np;
-    const int ky = slot_to_index(sy, E), kx = slot_to_index(sx, E);
+    const int ky = slot_to_freq_y(sy, Np), kx = slot_to_freq_x(sx, Np);
     const float m = (centred && ((ky + kx) & 1)) ? -1.f : 1.f;
     out[i] = make_float2(m * (float)Np, 0.f);
   }
@@ -235,14 +232,12 @@ __global__ void reference_init_kernel(float2* __restrict__ out, int planes, int 
 __global__ void reference_natural_kernel(const float2* __restrict__ in, float2* __restrict__ out, int planes, int Np,
                                          int centred) {
   const size_t n = (size_t)planes * Np * Np;
-  const int E = Np / 32;
   const float inv = 1.f / (float)Np;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const size_t f = i / ((size_t)Np * Np);
     const int rem = (int)(i - f * Np * Np);
     const int ky = rem / Np, kx = rem % Np;
-    const int sy = 32 * (ky % E) + (int)bitrev5((unsigned)(ky / E));
-    const int sx = 32 * (kx % E) + (int)bitrev5((unsigned)(kx / E));
+    const int sy = freq_to_slot_y(ky, Np), sx = freq_to_slot_x(kx, Np);
     const float m = (centred && ((ky + kx) & 1)) ? -inv : inv;
     const float2 v = in[(f * Np + sx) * Np + sy];
     out[i] = make_float2(v.x * m, v.y * m);
@@ -252,14 +247,11 @@ __global__ void reference_natural_kernel(const float2* __restrict__ in, float2* 
 // out[f][ky][kx] = in[f][sx(kx)][sy(ky)]  (inverse of the above)
 __global__ void from_fourier_layout_kernel(const float* __restrict__ in, float* __restrict__ out, int frames, int Np) {
   const size_t n = (size_t)frames * Np * Np;
-  const int E = Np / 32;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const size_t f = i / ((size_t)Np * Np);
     const int rem = (int)(i - f * Np * Np);
     const int ky = rem / Np, kx = rem % Np;
-    // index k = r + E*bitrev5(l)  <->  slot s = 32*r + l with r = k % E, l = bitrev5(k / E)
-    const int sy = 32 * (ky % E) + (int)bitrev5((unsigned)(ky / E));
-    const int sx = 32 * (kx % E) + (int)bitrev5((unsigned)(kx / E));
+    const int sy = freq_to_slot_y(ky, Np), sx = freq_to_slot_x(kx, Np);
     out[i] = in[(f * Np + sx) * Np + sy];
   }
 }
