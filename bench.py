@@ -372,6 +372,7 @@ def run_gb300(args, rank, world, local_rank):
                            "single_scan": single, "note": "the headline line above"}}
             for name in ("C0", "C2", "C3"):
                 cfgs[name] = measure_config(name, dev, lib, with_cpu=world == 1 and not args.no_cpu_baseline)
+            cfgs["C2_gradient"] = measure_c2_gradient(dev)
             out["configs"] = cfgs
     return out
 
@@ -499,6 +500,51 @@ def measure_config(name, dev, lib, with_cpu=True):
         target = {"C0": 2000, "C2": 60, "C3": 1125}[name]
         out["cpu_baseline"] = _config_cpu_sample(name, target)
     return out
+
+
+def measure_c2_gradient(dev, steps=4, warm=2):
+    """C2's gradient engine: Engines.e3qNewton (the quasi-Newton step on the
+    adjoint of the multislice model, 64 positions per step) on the C2 scan,
+    one scan on the whole GPU; K timed iterations after the set-up, CUDA
+    events on the engine's stream."""
+    import torch
+
+    from ptylab_gb300 import DummyMonitor, Engines
+    from ptylab_gb300 import simulate as S
+
+    _, d, p, rec = S.config_problem("C2")
+    eng = Engines.e3qNewton(rec, d, p, DummyMonitor())
+    eng.numIterations = warm + steps
+    nf = d.ptychogram.shape[0]
+    np.random.seed(2)
+    eng._begin()
+    for loop in range(warm):
+        eng._iterate(loop)
+    stream = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for loop in range(warm, warm + steps):
+        eng._iterate(loop)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    t = e0.elapsed_time(e1) / 1e3
+    eng._end()
+    flops, bytes_ = config_counts("C2", rec)
+    hbm_peak, peak_kind, _ = measured_peaks()
+    props = torch.cuda.get_device_properties(dev)
+    fp32_peak = props.multi_processor_count * 128 * 2 * 2070.0 * 1e6 / 1e12
+    value = nf * steps / t
+    return {
+        "engine": "e3qNewton", "value": value, "unit": UNIT, "ms_per_step": t / steps * 1e3, "steps": steps,
+        "warmup": warm, "scans": 1, "positions": nf, "positions_per_step": int(eng.batchSize),
+        "error_curve": [float(x) for x in np.asarray(rec.error)],
+        "roofline": {"bound": "fp32", "fp32_tflops": value * flops / 1e12, "fp32_frac": value * flops / 1e12 / fp32_peak,
+                     "hbm_frac": value * bytes_ / 1e9 / hbm_peak, "hbm_peak": hbm_peak, "hbm_peak_kind": peak_kind,
+                     "flops_per_position": flops, "bytes_per_position": bytes_},
+        "step": "one iteration: order draw and upload, then per 64 positions one gradient pass (forward, amplitude "
+                "residual, adjoint) and the quasi-Newton step of the 4 object slices and the probe",
+    }
 
 
 # ------------------------------------------------------------------ CPU legs

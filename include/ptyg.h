@@ -342,6 +342,33 @@ PTYG_API int ptyg_multislice_adjoint(const ptyg_multislice* geometry, const void
                                      void* grad_object, void* grad_probe, void* workspace, size_t workspace_bytes,
                                      void* stream);
 
+/* One gradient pass of the multislice model against measured intensities,
+ * for the quasi-Newton multislice engine (the reference has no gradient
+ * engine for multislice; its comparators are e3PIE's update,
+ * PtyLab/Engines/e3PIE.py:125-173, and qNewton's step, qNewton.py:108-140).
+ * For the frames order[0..num_frames) (all frames when order is NULL):
+ * forward model, amplitude loss L = sum (sqrt(I) - sqrt(measured))^2,
+ * dL/dI = 1 - sqrt(measured / (I + 1e-10)), and the adjoint, accumulating
+ * grad_object (nslice, No, No) and grad_probe (npsm, Np, Np) in the
+ * dL/dRe + i dL/dIm convention.  Optional outputs, accumulated too:
+ * illum_object (nslice, No, No) += sum over positions and modes of |incident
+ * field of slice s|^2; illum_probe (npsm, Np, Np) += sum over positions of
+ * |O_0[patch]|^2 (the same in every mode plane); err_at_pos[frame] += sum |measured - I| (FP64).
+ * measured is (frames, Np, Np) float32 in natural order, indexed by frame. */
+PTYG_API int ptyg_multislice_amplitude_gradient(const ptyg_multislice* geometry, const void* object, const void* probe,
+                                                const int32_t* positions, const void* slice_h, const int32_t* order,
+                                                const float* measured, void* grad_object, void* grad_probe,
+                                                float* illum_object, float* illum_probe, double* err_at_pos,
+                                                void* workspace, size_t workspace_bytes, void* stream);
+
+/* The quasi-Newton step of qNewton.py:108-140 on accumulated gradients, per
+ * plane of plane_size complex64 values (planes <= 64):
+ *   x -= beta / 2 * sqrt(w / max_plane(w)) / (w + reg) * grad,
+ * then grad and w are zeroed for the next accumulation.  scratch: `planes`
+ * device floats. */
+PTYG_API int ptyg_qn_step(void* x, void* grad, float* weight, int planes, int64_t plane_size, float beta, float reg,
+                          float* scratch, void* stream);
+
 /* ------------------------------------------------------------------------
  * Small per-iteration helpers of BaseEngine.applyConstraints
  * (BaseEngine.py:1440-1612) and orthogonalizeModes (utils.py:130-211).
