@@ -221,6 +221,35 @@ class BaseEngine(object):
         self._device_state()
         self._plan_and_bind()
 
+    def _host_state(self):
+        """What the device path takes from PtyLab's objects, read and checked
+        on the host: the state arrays (object, probe, and the engine's
+        buffers), the scan positions and the ptychogram, as NumPy arrays.  The
+        engines read nothing else from the objects on the way to the GPU but
+        the scalars of _geometry, _update_params and _host_tables."""
+        rec, d = self.reconstruction, self.experimentalData
+        Np, No = int(rec.Np), int(rec.No)
+        nosm, npsm, nslice = int(rec.nosm), int(rec.npsm), int(rec.nslice)
+        nl = int(getattr(rec, "nlambda", 1))
+        # (a state array that is already a torch tensor is passed through as it is)
+        out = {}
+        for name in self._state_fields():
+            v = getattr(rec, name)
+            out[name] = v if hasattr(v, "detach") else np.asarray(v).astype(np.complex64)
+        if tuple(out["object"].shape) != (nl, nosm, 1, nslice, No, No):
+            raise ValueError(f"object shape {tuple(out['object'].shape)} != {(nl, nosm, 1, nslice, No, No)}")
+        if tuple(out["probe"].shape) != (nl, 1, npsm, nslice, Np, Np):
+            raise ValueError(f"probe shape {tuple(out['probe'].shape)} != {(nl, 1, npsm, nslice, Np, Np)}")
+        nf = int(d.numFrames)
+        positions = np.asarray(rec.positions).astype(np.int64)
+        if positions.shape != (nf, 2):
+            raise ValueError(f"positions shape {positions.shape} != {(nf, 2)}")
+        if positions.min() < 0 or positions.max() > No - Np:
+            raise ValueError(f"scan positions fall outside the {No}x{No} object (patch {Np})")
+        out["positions"] = positions
+        out["ptychogram"] = np.asarray(_host(d.ptychogram)).astype(np.float32)
+        return out
+
     def _device_state(self):
         """The reconstruction state, data, positions and order buffers on the GPU."""
         torch = _torch()
@@ -231,25 +260,15 @@ class BaseEngine(object):
         device = torch.device("cuda", torch.cuda.current_device())
         lib = _native.require(device.index)
         rec, d, p = self.reconstruction, self.experimentalData, self.params
+        host = self._host_state()
         self._dev = {"device": device, "lib": lib}
         for name in self._state_fields():
-            setattr(rec, name, self._to_device(getattr(rec, name), torch.complex64))
-        Np, No = int(rec.Np), int(rec.No)
-        nosm, npsm, nslice = int(rec.nosm), int(rec.npsm), int(rec.nslice)
-        nl = int(getattr(rec, "nlambda", 1))
-        if tuple(rec.object.shape) != (nl, nosm, 1, nslice, No, No):
-            raise ValueError(f"object shape {tuple(rec.object.shape)} != {(nl, nosm, 1, nslice, No, No)}")
-        if tuple(rec.probe.shape) != (nl, 1, npsm, nslice, Np, Np):
-            raise ValueError(f"probe shape {tuple(rec.probe.shape)} != {(nl, 1, npsm, nslice, Np, Np)}")
+            setattr(rec, name, self._to_device(host[name], torch.complex64))
         nf = int(d.numFrames)
-        positions = np.asarray(rec.positions).astype(np.int64)
-        if positions.shape != (nf, 2):
-            raise ValueError(f"positions shape {positions.shape} != {(nf, 2)}")
-        if positions.min() < 0 or positions.max() > No - Np:
-            raise ValueError(f"scan positions fall outside the {No}x{No} object (patch {Np})")
+        positions = host["positions"]
         self._positions_host = positions
         self._dev["positions"] = torch.from_numpy(positions.astype(np.int32)).to(device)
-        self._dev["data"] = self._to_device(d.ptychogram, torch.float32)
+        self._dev["data"] = self._to_device(host["ptychogram"], torch.float32)
         self._dev["order"] = torch.zeros(nf, dtype=torch.int32, device=device)
         self._dev["flags"] = torch.zeros(nf, dtype=torch.uint8, device=device)
         # a ring of pinned staging buffers for the per-iteration order and
@@ -295,9 +314,10 @@ class BaseEngine(object):
         self._bind()
         self.params.gpuFlag = 1
 
-    def _set_tables(self):
+    def _host_tables(self):
+        """The propagator tables the plan takes (Fresnel chirp, ASP transfer
+        function(s), slice transfer function), computed on the host."""
         rec, p = self.reconstruction, self.params
-        lib = self._dev["lib"]
         Np = int(rec.Np)
         q = h = sh = None
         kind = p.propagatorType.lower()
@@ -311,7 +331,11 @@ class BaseEngine(object):
             # one transfer function per wavelength of spectralDensity (Operators.py:909-951)
             wl = tuple(float(w) for w in np.atleast_1d(rec.spectralDensity)[: int(rec.nlambda)])
             h = np.ascontiguousarray(_tables.polychrome_asp_tf(float(rec.zo), wl, Np, Np * float(rec.dxp)))
-        sh = self._slice_table()
+        return q, h, self._slice_table()
+
+    def _set_tables(self):
+        lib = self._dev["lib"]
+        q, h, sh = self._host_tables()
         self._tables_keepalive = (q, h, sh)
         ptr = lambda a: a.ctypes.data if a is not None else None  # noqa: E731
         _native.check(lib.ptyg_plan_set_tables(self._plan, ptr(q), ptr(h), ptr(sh)), "ptyg_plan_set_tables")
