@@ -162,7 +162,7 @@ def algorithmic_counts(flags_per_step, nscans):
 # DRAM bytes per position of the batched launch, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum of a 15-scan launch / 6000
 # positions; the summary is profiles/engine_kernel_mpie_c1.md)
-TRAFFIC_PER_POSITION = 402_945
+TRAFFIC_PER_POSITION = 406_993
 
 
 # ------------------------------------------------------------------ ranks
@@ -780,7 +780,23 @@ def main():
     ap.add_argument("--net-batch", type=int, default=16)
     ap.add_argument("--net-size", type=int, default=128)
     ap.add_argument("--net-reps", type=int, default=20)
+    ap.add_argument("--config", default="", choices=["", "C0", "C2", "C3", "C2_gradient"],
+                    help="time only this configuration's line (as in the headline line's configs)")
     args = ap.parse_args()
+    if args.config:
+        import torch
+
+        torch.cuda.set_device(0)
+        dev = torch.device("cuda", 0)
+        if args.config == "C2_gradient":
+            print(json.dumps(measure_c2_gradient(dev, steps=args.steps, warm=args.warmup)), flush=True)
+        else:
+            from ptylab_gb300 import _native
+
+            CONFIG_STEPS[args.config] = (args.steps, args.warmup)
+            out = measure_config(args.config, dev, _native.require(0), with_cpu=not args.no_cpu_baseline)
+            print(json.dumps(out), flush=True)
+        return
     if args.calibration:
         print(json.dumps(run_calibration(args)), flush=True)
         return

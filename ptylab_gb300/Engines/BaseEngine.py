@@ -291,6 +291,7 @@ class BaseEngine(object):
             num_frames=int(d.numFrames), num_scans=num_scans, engine=self._engine_code(),
             propagator=_native.PROPAGATORS[p.propagatorType.lower()], fftshift=int(bool(p.fftshiftSwitch)),
             fpm=int(d.operationMode == "FPM"), cluster=int(getattr(self, "cluster", 0) or 0), throughput=throughput,
+            threads=int(getattr(self, "threads", 0) or 0),
             nlambda=int(getattr(rec, "nlambda", 1)),
         )
 

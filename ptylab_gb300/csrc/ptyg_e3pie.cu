@@ -45,14 +45,15 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
   float2* tile = reinterpret_cast<float2*>(smem_f4);  // K * NP * L (swizzled, tix)
   float2* rows = tile + K * NP * L;                   // K * LN
   float* fr = reinterpret_cast<float*>(rows + K * LN);
-  float* dat = fr + LN;  // 2 * LN
-  unsigned* slots = reinterpret_cast<unsigned*>(dat + 2 * LN);
+  float* dat = fr + LN;  // LN: this position's intensities, then (once the projection has read
+                         // them) the next position's, in flight
+  unsigned* slots = reinterpret_cast<unsigned*>(dat + LN);
   double* redD = reinterpret_cast<double*>(slots + 2 * RED_BANK);
   float* redF = reinterpret_cast<float*>(redD + 32);
   unsigned* slots0 = dsmem(slots, 0);
 
   if (threadIdx.x < 2 * RED_BANK) slots[threadIdx.x] = 0u;
-  prefetch_data<NP, L>(a, s, dat, 0, blk0);
+  prefetch_data<NP, L, false>(a, s, dat, 0, blk0);
   WarpFFT<E> F;  // the column transforms (rows: row_tasks)
   F.init(a.twiddle, lane);
   __syncthreads();
@@ -61,16 +62,18 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
   const float inv2 = 1.f / (float)NP2;
 
   for (int it = 0; it < a.count; ++it) {
-    prefetch_data<NP, L>(a, s, dat, it + 1, blk0);
     const int frame = s.order[a.start + it];
     const int row0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame] : -1;
     const int col0 = (frame >= 0 && frame < a.numFrames) ? s.positions[2 * frame + 1] : -1;
     if (row0 < 0 || col0 < 0 || row0 > No - NP || col0 > No - NP) {
       if (crank == 0 && threadIdx.x == 0) atomicCAS(s.status, 0, 2);
+      cp_async_wait_all();  // the skipped position's block, then the next one's
+      __syncthreads();
+      prefetch_data<NP, L, false>(a, s, dat, it + 1, blk0);
       continue;  // uniform across the cluster
     }
     unsigned* red = slots0 + (it & 1) * RED_BANK;
-    const float* datc = dat + (it & 1) * LN;
+    const float* datc = dat;
     const size_t orow = (size_t)(row0 + line0) * No + col0;
     // this CTA's rows of object slice sl, probe mode p of slice sl, exit wave (sl, p)
     auto Ob = [&](int sl) { return s.object + sl * No2 + orow; };
@@ -116,7 +119,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           return (S == 1) ? detector_in(e, line0 + l, x) : e;
         },
         scatter, pairs);
-    cp_async_wait_prev();  // this position's intensities
+    cp_async_wait_all();  // this position's intensities (the one group in flight)
     cluster_sync(C);
 
     // ---------------- forward through the slices
@@ -215,6 +218,9 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       cluster_sync(C);
       column_filter<E, L>(tile, rows, F, a.aspH, true, crank, K, K);
     }
+    // every read of this position's intensities is behind a CTA barrier by
+    // now: fetch the next position's while the backward pass runs
+    prefetch_data<NP, L, false>(a, s, dat, it + 1, blk0);
     {
       const double t = block_sum(err, redD);
       if (threadIdx.x == 0) s.errPart[(size_t)frame * C + crank] = t;
@@ -287,7 +293,7 @@ size_t e3pie_smem_bytes(int Np, int C, int npsm) {
   const size_t LN = (size_t)L * Np;
   const size_t n = (size_t)npsm * Np * L + (size_t)npsm * LN;
   // redF holds 32 floats per reduced value: MAX_SLICES + 1 of them
-  return n * sizeof(float2) + 3 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
+  return n * sizeof(float2) + 2 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
          8 * 32 * sizeof(float) + 64;
 }
 
