@@ -403,10 +403,12 @@ static int engine_threads(const ptyg_geometry& g, int C) {
 
 // Cluster sizes to try, best first.  Latency: 8 rows per CTA (more CTAs,
 // shorter passes), then 16.  Throughput: 16 rows first (fewer CTAs per scan,
-// so more scans are resident at once).  A requested size goes first.
+// so more scans are resident at once), and at Np = 64 the whole patch in one
+// CTA before that.  A requested size goes first.
 static std::vector<int> cluster_candidates(const ptyg_geometry& g) {
   std::vector<int> c;
   if (g.cluster > 0) c.push_back(g.cluster);
+  if (g.throughput && g.Np == 64) c.push_back(1);
   const int order[2] = {g.throughput ? 16 : 8, g.throughput ? 8 : 16};
   for (int L : order) {
     const int cc = g.Np / L;

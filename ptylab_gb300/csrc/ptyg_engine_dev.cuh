@@ -176,13 +176,17 @@ PTYG_DEV float slot_value(const unsigned* slots, int i) {
 // Column block (tile) layout: row (k * NP + y) holds the CTA's L columns,
 // unpadded, column c stored at c ^ swz(row).  The swizzle spreads the 16
 // consecutive rows of a 64-bit half-warp access (a column task: lanes step
-// through y) over 16 distinct bank pairs: swz = row & 15 for L = 16 and
+// through y) over 16 distinct bank pairs: swz = row & 15 for L >= 16 and
 // (row >> 1) & 7 for L = 8 (where a row pair shares one 16-element span).
 // A row write (lanes step through c) stays one permuted contiguous span.
 template <int L>
+PTYG_DEV int tix_swz(int row) {
+  static_assert(L == 8 || L == 16 || L == 32 || L == 64, "tile swizzle defined for 8 to 64 columns");
+  return L == 8 ? (row >> 1) & 7 : row & 15;
+}
+template <int L>
 PTYG_DEV int tix(int row, int c) {
-  static_assert(L == 8 || L == 16, "tile swizzle defined for 8 or 16 columns");
-  return row * L + (c ^ ((row / (16 / L)) & (L - 1)));
+  return row * L + (c ^ tix_swz<L>(row));
 }
 
 // Store into the shared memory of cluster rank `rank` at the address `local`
@@ -200,21 +204,24 @@ PTYG_DEV void st_cluster4(const float4* local, int rank, float4 v) {
   asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"r"(r), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
 }
 
-// Element lo + hi (a Fourier slot; hi a multiple of L) of the transformed row
-// y of mode k goes to the column block of the CTA owning that slot.
+// Element lo + hi (a Fourier slot; lo the thread's part, hi a compile-time
+// offset) of the transformed row y of mode k goes to the column block of the
+// CTA owning that slot.
 template <int NP, int L>
 PTYG_DEV void scatter_row(float2* tile, int k, int y, int lo, int hi, float2 v) {
-  st_cluster(&tile[tix<L>(k * NP + y, lo % L)], lo / L + hi / L, v);
+  const unsigned s = (unsigned)(lo + hi);
+  st_cluster(&tile[tix<L>(k * NP + y, (int)(s % L))], (int)(s / L), v);
 }
 
 // Row buffers (K * L rows of NP, Fourier layout along x) are written by the
 // column owners and read along rows, so the slot is swizzled by the row: row
-// task t = k * L + l keeps slot s at t * NP + (s ^ l) (rsw).  XOR with l < L
-// permutes slots within aligned groups of L, so a column block stays one
-// contiguous span of every row.
+// task t = k * L + l keeps slot s at t * NP + (s ^ (l mod 16)) (rsw).  The XOR
+// touches bits 0..3 only, so it permutes slots within aligned groups of 16
+// (a column block of L >= 16 stays one contiguous span of every row) and
+// commutes with adding a multiple of 16: rsw(t, lo + hi) = rsw(t, lo) + hi.
 template <int L>
 PTYG_DEV int rsw(int t, int s) {
-  return s ^ (t & (L - 1));
+  return s ^ (t & ((L < 16 ? L : 16) - 1));
 }
 
 // A column task stores its result (natural order along y) in its own column of
@@ -231,13 +238,14 @@ PTYG_DEV void flush_columns(const float2* tile, float2* rows, int K, int sx0) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int r = i / PAIRS, c = 2 * (i - (i / PAIRS) * PAIRS);  // tile row k * NP + y, even column c
     const int k = r / NP, y = r - (r / NP) * NP;
-    const int sw = (r / (16 / L)) & (L - 1);  // the tix swizzle of row r
+    const int sw = tix_swz<L>(r);
     // columns c, c + 1 sit at (c ^ sw) and (c ^ sw) ^ 1: one aligned pair, swapped when sw is odd
     const float4 f = *reinterpret_cast<const float4*>(tile + r * L + ((c ^ sw) & ~1));
     const int owner = y / L, ly = y - (y / L) * L;
-    // in the owner's row, slots sx0 + c and sx0 + c + 1 sit at ((sx0 + c) ^ ly) and that ^ 1
-    const int pos = (k * L + ly) * NP + (((sx0 + c) ^ ly) & ~1);
-    const float4 o = ((sw ^ ly) & 1) ? make_float4(f.z, f.w, f.x, f.y) : f;
+    // in the owner's row, slots sx0 + c and sx0 + c + 1 sit at rsw(sx0 + c) and that ^ 1
+    const int t = k * L + ly;
+    const int pos = t * NP + (rsw<L>(t, sx0 + c) & ~1);
+    const float4 o = ((sw ^ t) & 1) ? make_float4(f.z, f.w, f.x, f.y) : f;
     st_cluster4(reinterpret_cast<const float4*>(rows + pos), owner, o);
   }
 }

@@ -784,7 +784,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         // to PPT pixels at once and runs the probe modes outermost, so the
         // pixels' independent chains interleave; per pixel the arithmetic and
         // its order are those of the general loop below
-        constexpr int PPT = LN >= 512 ? LN / 512 : 1;
+        constexpr int PPT = LN >= 2048 ? 4 : (LN >= 512 ? LN / 512 : 1);
         auto gObjF = [&](float qp) {
           if (eng == ENG_EPIE) return invPmax2;
           if (eng == ENG_MPIE) {
@@ -1209,8 +1209,10 @@ cudaError_t clusters_t(int threads, size_t smem, int* out) {
   return cudaOccupancyMaxActiveClusters(out, (void*)engine_kernel<E, L, VAR>, &cfg);
 }
 
-// Instantiated shapes: 8 or 16 rows per CTA, at most 16 CTAs per cluster.
-#define PTYG_ENGINE_SHAPES(X) X(1, 8) X(1, 16) X(2, 8) X(2, 16) X(4, 8) X(4, 16) X(8, 16)
+// Instantiated shapes: 8 or 16 rows per CTA, at most 16 CTAs per cluster;
+// and at Np = 64 the whole patch in one CTA (a cluster of one: its barriers
+// are CTA barriers and its transposes stay in its own shared memory).
+#define PTYG_ENGINE_SHAPES(X) X(1, 8) X(1, 16) X(2, 8) X(2, 16) X(2, 64) X(4, 8) X(4, 16) X(8, 16)
 
 
 // Launch / occupancy over the instantiated shapes for one variant; each

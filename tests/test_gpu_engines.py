@@ -181,8 +181,10 @@ def test_reconstruct_batch_equals_single_engines(torch_cuda, engine):
     RNG between the engines).  The batch runs the many-scan kernel shape
     (fewer, wider CTAs per scan); every sum that feeds the updates is formed
     in a tree fixed by the patch size, so object, probe and detector error
-    are bit-identical, and only the error metric (per-CTA partials summed on
-    the host) can differ in its last bits."""
+    are bit-identical, and only the error metric can differ in its last
+    bits: each thread sums its pixels' |I_meas - I_est| in FP32 before the
+    FP64 CTA and frame sums, and the batch shape gives a thread more pixels
+    (at Np = 64 the whole patch is one CTA: 16 pixels per thread)."""
     from ptylab_gb300 import DummyMonitor, Engines
     from ptylab_gb300.simulate import ScanSpec, cpm_problem
 
@@ -206,7 +208,7 @@ def test_reconstruct_batch_equals_single_engines(torch_cuda, engine):
         np.testing.assert_array_equal(rb.object, ra.object)
         np.testing.assert_array_equal(rb.probe, ra.probe)
         np.testing.assert_array_equal(rb.detectorError, ra.detectorError)
-        assert rel_err(np.asarray(rb.error), np.asarray(ra.error)) < 1e-9
+        assert rel_err(np.asarray(rb.error), np.asarray(ra.error)) < 1e-8
 
 
 def test_batched_scans_equal_single_runs(torch_cuda):
