@@ -38,10 +38,13 @@ def main():
     ap.add_argument("--weights", default=None, help="save the trained weights here (.npz)")
     ap.add_argument("--photons", type=float, default=None, help="photons per pattern of the evaluation scan")
     ap.add_argument("--train-photons", type=float, default=None, help="photons per pattern of the training scans")
+    ap.add_argument("--probe-first", default="0",
+                    help="comma-separated: warm runs whose first N iterations update the probe only")
+    ap.add_argument("--batch-scans", type=int, default=15, help="training scans reconstructed per launch")
     args = ap.parse_args()
     t0 = time.perf_counter()
     tspec = TR.TRAIN_SPEC if args.train_photons is None else replace(TR.TRAIN_SPEC, photons=args.train_photons)
-    data = TR.make_training_set(args.scans, spec=tspec, log=None)
+    data = TR.make_training_set(args.scans, spec=tspec, log=None, batch_scans=args.batch_scans)
     t_data = time.perf_counter() - t0
     net = WarmStartNet(seed=1)
     torch.cuda.synchronize()
@@ -52,7 +55,9 @@ def main():
     if args.weights:
         TR.save_weights(net, args.weights)
     spec = EV.C4 if args.photons is None else replace(EV.C4, photons=args.photons)
-    plain, warm, e0 = EV.compare(net, spec=spec, max_iters=args.max_iters)
+    pfs = tuple(int(v) for v in args.probe_first.split(","))
+    plain, warm, e0 = EV.compare(net, spec=spec, max_iters=args.max_iters, probe_first=pfs)
+    warms = warm if isinstance(warm, list) else [warm]
     out = {
         "evaluation": f"1024-position Fermat scan, Np=128, No=640, npsm=2, {spec.photons:g} photons (synthetic, seeded)",
         "training": {"scans": args.scans, "patterns": args.scans * 100, "steps": args.steps, "batch": args.batch,
@@ -61,9 +66,9 @@ def main():
                      "final_supervised_loss": float(sum(h[0] for h in hist[-100:]) / 100)},
         "warm_start_object_error": e0,
     }
-    for r in (plain, warm):
+    for r in (plain, *warms):
         out[r.label] = {"setup_seconds": r.setup_seconds, "iterations": len(r.errors), "final_error": r.errors[-1],
-                        **{f"seconds_to_{t:g}": r.time_to(t) for t in (1e-1, 3e-2, 1e-2)}}
+                        **{f"seconds_to_{t:g}": r.time_to(t) for t in (1e-1, 5e-2, 3e-2, 2e-2, 1e-2)}}
     print(json.dumps(out))
 
 

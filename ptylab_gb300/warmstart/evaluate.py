@@ -99,10 +99,12 @@ class Run:
         return None
 
 
-def mpie_iterations(eng, max_iters, truth, mask, threshold, label, setup_seconds=0.0):
+def mpie_iterations(eng, max_iters, truth, mask, threshold, label, setup_seconds=0.0, probe_first=0):
     """Run eng (an Engines.mPIE) one iteration at a time, as mPIE.reconstruct
     does, recording cumulative GPU time and the object error; stops at the
-    threshold or after max_iters."""
+    threshold or after max_iters.  probe_first: the first iterations update
+    the probe only (betaObject 0), so a probe guess can settle on an object
+    that is already close (the hand-over from a warm start)."""
     torch = _torch()
     rec = eng.reconstruction
     eng._prepareReconstruction()
@@ -116,7 +118,9 @@ def mpie_iterations(eng, max_iters, truth, mask, threshold, label, setup_seconds
     stream = torch.cuda.current_stream(dev)
     run = Run(label, [], [], setup_seconds)
     total = setup_seconds
+    beta_o = eng.betaObject
     for loop in range(max_iters):
+        eng.betaObject = 0.0 if loop < probe_first else beta_o
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         eng.setPositionOrder()
         draws = np.random.rand(nf) if hasattr(rec, "objectBuffer") else None
@@ -155,8 +159,10 @@ def _mpie(d, p, rec):
     return eng
 
 
-def compare(net, spec=C4, threshold=1e-2, max_iters=200, seed=5, batch=64):
-    """Plain mPIE and warm-started mPIE on the evaluation scan: (plain Run, warm Run, warm-start error)."""
+def compare(net, spec=C4, threshold=1e-2, max_iters=200, seed=5, batch=64, probe_first=(0,)):
+    """Plain mPIE and warm-started mPIE on the evaluation scan: (plain Run,
+    warm Run, warm-start error), with one warm Run per probe_first entry
+    (a list of Runs when probe_first has several)."""
     torch = _torch()
     from .stitch import predict_object
 
@@ -173,18 +179,19 @@ def compare(net, spec=C4, threshold=1e-2, max_iters=200, seed=5, batch=64):
     np.random.seed(seed)
     plain = mpie_iterations(_mpie(d, p, rec), max_iters, truth, mask, threshold, "plain mPIE")
 
-    d, p, rec, _, _ = c4_problem(spec)
-    rec.object, rec.probe = obj0.copy(), prb0.copy()
-    # warm-up of the inference (graph capture for this batch shape, first
-    # launches), not timed, like the plain run's warm-up above
-    predict_object(net, d.ptychogram, rec.positions, spec.No, spec.Np, batch=batch)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    warm_obj, setup = predict_object(net, d.ptychogram, rec.positions, spec.No, spec.Np, batch=batch)
-    rec.object = warm_obj.reshape(rec.object.shape).astype(np.complex64)
-    warm_err0 = normalized_error(warm_obj, truth, mask)
-    np.random.seed(seed)
-    warm = mpie_iterations(_mpie(d, p, rec), max_iters, truth, mask, threshold, "warm start + mPIE",
-                           setup_seconds=setup)
-    _ = t0
-    return plain, warm, warm_err0
+    warms = []
+    for pf in probe_first:
+        d, p, rec, _, _ = c4_problem(spec)
+        rec.object, rec.probe = obj0.copy(), prb0.copy()
+        # warm-up of the inference (graph capture for this batch shape, first
+        # launches), not timed, like the plain run's warm-up above
+        predict_object(net, d.ptychogram, rec.positions, spec.No, spec.Np, batch=batch)
+        torch.cuda.synchronize()
+        warm_obj, setup = predict_object(net, d.ptychogram, rec.positions, spec.No, spec.Np, batch=batch)
+        rec.object = warm_obj.reshape(rec.object.shape).astype(np.complex64)
+        warm_err0 = normalized_error(warm_obj, truth, mask)
+        np.random.seed(seed)
+        label = "warm start + mPIE" + (f" (probe only for {pf} iterations)" if pf else "")
+        warms.append(mpie_iterations(_mpie(d, p, rec), max_iters, truth, mask, threshold, label,
+                                     setup_seconds=setup, probe_first=pf))
+    return plain, (warms[0] if len(warms) == 1 else warms), warm_err0

@@ -38,35 +38,45 @@ def _torch():
     return torch
 
 
-def make_training_set(n_scans, seed0=1000, spec=TRAIN_SPEC, mpie_iters=150, log=print):
-    """Simulate n_scans scans and reconstruct each with the GPU mPIE: a list of
-    {x: float32 [n, Np, Np] network inputs, target: complex64 [n, Np, Np] mPIE
-    patches, truth: complex64 [n, Np, Np] true patches, probe: complex64
-    (npsm, Np, Np) reconstructed, I: float32 [n, Np, Np] measured}."""
-    from ..Engines import mPIE
+def make_training_set(n_scans, seed0=1000, spec=TRAIN_SPEC, mpie_iters=150, log=print, batch_scans=15):
+    """Simulate n_scans scans and reconstruct them with the GPU mPIE,
+    `batch_scans` at a time in one launch per iteration
+    (Engines.reconstruct_batch): a list of {x: float32 [n, Np, Np] network
+    inputs, target: complex64 [n, Np, Np] mPIE patches, truth: complex64
+    [n, Np, Np] true patches, probe: complex64 (npsm, Np, Np) reconstructed,
+    I: float32 [n, Np, Np] measured}."""
+    from ..Engines import mPIE, reconstruct_batch
     from ..Monitor import DummyMonitor
 
     out = []
     t0 = time.perf_counter()
-    for k in range(n_scans):
-        d, p, rec, obj, _ = cpm_problem(replace(spec, seed=seed0 + k), engine_seed=seed0 + k)
-        p.positionOrder = "random"
-        p.probePowerCorrectionSwitch = True
-        eng = mPIE(rec, d, p, DummyMonitor())
-        eng.alphaObject = eng.alphaProbe = 0.25
-        eng.betaObject = eng.betaProbe = 0.25
-        eng.numIterations = mpie_iters
-        np.random.seed(seed0 + k)
-        eng.reconstruct()
-        Np = spec.Np
-        o = np.asarray(rec.object)[0, 0, 0, 0]
-        pos = np.asarray(rec.positions)
-        tgt = np.stack([o[r : r + Np, c : c + Np] for r, c in pos]).astype(np.complex64)
-        tru = np.stack([obj[r : r + Np, c : c + Np] for r, c in pos]).astype(np.complex64)
-        out.append(dict(x=network_input(d.ptychogram), target=tgt, truth=tru, I=np.asarray(d.ptychogram, np.float32),
-                        probe=np.asarray(rec.probe)[0, 0, :, 0].astype(np.complex64)))
-        if log and (k + 1) % 10 == 0:
-            log(f"training scans: {k + 1}/{n_scans} ({time.perf_counter() - t0:.1f} s)")
+    Np = spec.Np
+    for k0 in range(0, n_scans, max(1, batch_scans)):
+        group = []
+        for k in range(k0, min(n_scans, k0 + max(1, batch_scans))):
+            d, p, rec, obj, _ = cpm_problem(replace(spec, seed=seed0 + k), engine_seed=seed0 + k)
+            p.positionOrder = "random"
+            p.probePowerCorrectionSwitch = True
+            eng = mPIE(rec, d, p, DummyMonitor())
+            eng.alphaObject = eng.alphaProbe = 0.25
+            eng.betaObject = eng.betaProbe = 0.25
+            eng.numIterations = mpie_iters
+            group.append((eng, d, rec, obj))
+        np.random.seed(seed0 + k0)
+        if len(group) == 1:
+            group[0][0].reconstruct()
+        else:
+            reconstruct_batch([g[0] for g in group])
+        for _, d, rec, obj in group:
+            o = np.asarray(rec.object)[0, 0, 0, 0]
+            pos = np.asarray(rec.positions)
+            tgt = np.stack([o[r : r + Np, c : c + Np] for r, c in pos]).astype(np.complex64)
+            tru = np.stack([obj[r : r + Np, c : c + Np] for r, c in pos]).astype(np.complex64)
+            out.append(dict(x=network_input(d.ptychogram), target=tgt, truth=tru,
+                            I=np.asarray(d.ptychogram, np.float32),
+                            probe=np.asarray(rec.probe)[0, 0, :, 0].astype(np.complex64)))
+        if log:
+            log(f"training scans: {len(out)}/{n_scans} ({time.perf_counter() - t0:.1f} s)")
     return out
 
 
