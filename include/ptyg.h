@@ -309,6 +309,12 @@ PTYG_API int ptyg_plan_frame_errors(ptyg_plan* plan, int scan, double* host_out,
  * next iteration while this one runs and read every iteration's sums once at
  * the end. */
 PTYG_API int ptyg_plan_frame_errors_device(ptyg_plan* plan, int scan, double* device_out, void* stream);
+/* The same for every bound scan in one launch: device_out[scan * num_frames +
+ * frame] (device float64, num_scans x num_frames), for batches of many scans
+ * whose per-scan calls would cost more host time than the iteration's launch.
+ * An addition for batched reconstruction; PtyLab reads its errors per engine
+ * (PtyLab/Engines/BaseEngine.py:819-841). */
+PTYG_API int ptyg_plan_frame_errors_all_device(ptyg_plan* plan, double* device_out, void* stream);
 
 /* The recorded |I_meas - I_est| maps (flags bit 0) in natural layout:
  * `out` is device float32 (num_frames, Np, Np). */

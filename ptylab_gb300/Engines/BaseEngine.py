@@ -66,6 +66,8 @@ class BaseEngine(object):
     engine_name = "BaseEngine"
     _err_n = 0  # iterations whose frame sums wait on the device (_record_errors)
     _err_dev = None
+    _batch = None  # the shared per-iteration state of reconstruct_batch (Engines/batch.py)
+    _batch_row = 0
 
     def __init__(self, reconstruction, experimentalData, params, monitor):
         self.betaObject = 0.25
@@ -421,6 +423,9 @@ class BaseEngine(object):
         return u
 
     def _upload_order(self, momentum=None):
+        if self._batch is not None:  # staged for the batch's one copy
+            self._batch.stage(self._batch_row, self.positionIndices, momentum)
+            return
         torch = _torch()
         slot = self._uploads % _UPLOAD_SLOTS
         if self._upload_events[slot] is not None:
@@ -517,6 +522,8 @@ class BaseEngine(object):
         _resolve_errors turns the rows into rec.errorAtPos and rec.error in
         iteration order once, so the host can queue the next iteration while
         this one runs."""
+        if self._batch is not None:  # the batch sums every scan's frames in one launch
+            return
         torch = _torch()
         nf = self.experimentalData.numFrames
         if self._err_dev is None or self._err_n == self._err_dev.shape[0]:
@@ -537,6 +544,8 @@ class BaseEngine(object):
         if not self._err_n:
             return
         rows = self._err_dev[: self._err_n].cpu().numpy()
+        if self._batch is not None:
+            self._err_dev = self._err_dev[self._err_n :]  # the batch's later rows
         self._err_n = 0
         for err in rows:
             self._append_errors(err)

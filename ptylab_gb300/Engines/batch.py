@@ -64,6 +64,81 @@ def _check_compatible(engines):
             raise ValueError("reconstruct_batch: numIterations differs")
 
 
+class _BatchState:
+    """What the scans of a batch share per iteration: one device buffer of all
+    scans' position orders and momentum flags (each scan's bound order is a
+    row), filled from a ring of pinned host rows by one copy each, and one
+    device row per iteration of all scans' per-frame error sums (each
+    engine's error rows are a view of it).  With many scans, per-scan copies
+    and launches would cost more host time than the iteration's kernel."""
+
+    SLOTS = 3
+
+    def __init__(self, engines):
+        import torch
+
+        e0 = engines[0]
+        dev = e0._dev["device"]
+        G, nf = len(engines), int(e0.experimentalData.numFrames)
+        self.device, self.G, self.nf = dev, G, nf
+        self.orders = torch.zeros((G, nf), dtype=torch.int32, device=dev)
+        self.flags = torch.zeros((G, nf), dtype=torch.uint8, device=dev)
+        self.ring = [(torch.zeros((G, nf), dtype=torch.int32).pin_memory(),
+                      torch.zeros((G, nf), dtype=torch.uint8).pin_memory()) for _ in range(self.SLOTS)]
+        self.events = [None] * self.SLOTS
+        self.uploads = 0
+        self.errs = torch.zeros((max(int(e0.numIterations), 1), G, nf), dtype=torch.float64, device=dev)
+        self.n_err = 0
+        self.staging = None
+        self.any_flags = False
+
+    def begin_upload(self):
+        slot = self.uploads % self.SLOTS
+        if self.events[slot] is not None:
+            self.events[slot].synchronize()
+        self.staging = self.ring[slot]
+        self.any_flags = False
+
+    def stage(self, g, order, momentum):
+        import torch
+
+        self.staging[0][g].copy_(torch.from_numpy(np.asarray(order, dtype=np.int32)))
+        if momentum is not None:
+            self.staging[1][g].copy_(torch.from_numpy(np.asarray(momentum, dtype=np.uint8)))
+            self.any_flags = True
+
+    def end_upload(self):
+        import torch
+
+        self.orders.copy_(self.staging[0], non_blocking=True)
+        if self.any_flags:
+            self.flags.copy_(self.staging[1], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.device))
+        self.events[self.uploads % self.SLOTS] = ev
+        self.uploads += 1
+
+    def record_errors(self, engines):
+        import torch
+
+        from .. import _native
+
+        e0 = engines[0]
+        if self.n_err == self.errs.shape[0]:
+            grown = torch.zeros((2 * self.errs.shape[0], self.G, self.nf), dtype=torch.float64, device=self.device)
+            grown[: self.n_err].copy_(self.errs)
+            # each engine's view moves to the grown buffer at the rows it has not read yet
+            for g, e in enumerate(engines):
+                e._err_dev = grown[self.n_err - e._err_n :, g, :]
+            self.errs = grown
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        _native.check(e0._dev["lib"].ptyg_plan_frame_errors_all_device(e0._plan, self.errs[self.n_err].data_ptr(), stream),
+                      "ptyg_plan_frame_errors_all_device")
+        self.n_err += 1
+        for e in engines:
+            e._err_n += 1
+
+
 def begin_batch(engines, throughput=1):
     """Set-up half of ``reconstruct_batch``: validation, host preparation,
     device state, one launch plan with a cluster per scan.  Returns the list
@@ -76,6 +151,12 @@ def begin_batch(engines, throughput=1):
         e._prepare_host()
     for e in engines:
         e._device_state()
+    state = _BatchState(engines)
+    for g, e in enumerate(engines):
+        # the scan's order and flags are rows of the shared buffers (bound below)
+        e._dev["order"], e._dev["flags"] = state.orders[g], state.flags[g]
+        e._batch, e._batch_row = state, g
+        e._err_dev, e._err_n = state.errs[:, g, :], 0
     e0 = engines[0]
     e0._plan_and_bind(num_scans=len(engines), throughput=throughput)
     for i, e in enumerate(engines[1:], 1):
@@ -87,13 +168,18 @@ def begin_batch(engines, throughput=1):
 
 def iterate_batch(engines, loop):
     """One iteration of every scan: the host draws each order (and mPIE's
-    momentum flags), one kernel launch walks all scans' positions, then each
-    engine records its error and applies its constraints."""
+    momentum flags) into the shared staging rows, one copy moves them, one
+    kernel launch walks all scans' positions, one launch sums every scan's
+    frame errors, then each engine applies its constraints."""
     e0 = engines[0]
+    state = e0._batch
     nf = e0.experimentalData.numFrames
+    state.begin_upload()
     for e in engines:
         e._loop_order(loop)
+    state.end_upload()
     e0._run_positions(0, nf, record_detector_error=(loop == e0.numIterations - 1))  # every bound scan
+    state.record_errors(engines)
     for e in engines:
         e._loop_end(loop)
 
@@ -103,6 +189,8 @@ def finish_batch(engines):
     for e in engines[1:]:
         e._finish()
     engines[0]._finish()  # the plan's owner last: it destroys the plan
+    for e in engines:
+        e._batch = None
 
 
 def reconstruct_batch(engines):

@@ -161,6 +161,7 @@ _SIGNATURES = {
     ],
     "ptyg_plan_frame_errors": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_frame_errors_device": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "ptyg_plan_frame_errors_all_device": [C.c_void_p, C.c_void_p, C.c_void_p],
     "ptyg_plan_detector_error": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "ptyg_plan_status": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p],
     "ptyg_plan_set_projection": [C.c_void_p, C.POINTER(Projection), C.c_void_p, C.c_void_p, C.c_void_p],

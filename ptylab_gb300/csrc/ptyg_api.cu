@@ -770,6 +770,30 @@ extern "C" int ptyg_plan_frame_errors_device(ptyg_plan* p, int scan, double* dev
   return PTYG_OK;
 }
 
+// out[scan][frame] = sum_c errPart_scan[frame][c] for every bound scan, in
+// the fixed order of sum_parts: one launch for a whole batch.
+__global__ void sum_parts_scans_kernel(const ScanDev* __restrict__ scans, double* __restrict__ out, int nscans,
+                                       int frames, int C) {
+  const size_t n = (size_t)nscans * frames;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(i / frames), f = (int)(i - (size_t)s * frames);
+    const double* part = scans[s].errPart + (size_t)f * C;
+    double t = 0.0;
+    for (int c = 0; c < C; ++c) t += part[c];
+    out[i] = t;
+  }
+}
+
+extern "C" int ptyg_plan_frame_errors_all_device(ptyg_plan* p, double* device_out, void* stream) {
+  if (!p || !device_out) return fail(PTYG_ERR_INVALID, "null argument");
+  const size_t n = (size_t)p->g.num_scans * p->g.num_frames;
+  const unsigned grid = (unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+  sum_parts_scans_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(p->dScans, device_out, p->g.num_scans,
+                                                                  p->g.num_frames, p->C);
+  PTYG_CUDA(cudaGetLastError(), "error sums");
+  return PTYG_OK;
+}
+
 extern "C" int ptyg_plan_detector_error(ptyg_plan* p, int scan, float* out, void* stream) {
   if (!p || !out) return fail(PTYG_ERR_INVALID, "null argument");
   if (scan < 0 || scan >= p->g.num_scans) return fail(PTYG_ERR_INVALID, "scan %d out of range", scan);
