@@ -539,7 +539,8 @@ def measure_c2_gradient(dev, steps=4, warm=2):
         "engine": "e3qNewton", "value": value, "unit": UNIT, "ms_per_step": t / steps * 1e3, "steps": steps,
         "warmup": warm, "scans": 1, "positions": nf, "positions_per_step": int(eng.batchSize),
         "error_curve": [float(x) for x in np.asarray(rec.error)],
-        "roofline": {"bound": "fp32", "fp32_tflops": value * flops / 1e12, "fp32_frac": value * flops / 1e12 / fp32_peak,
+        "roofline": {"bound": "fp32", "frac": value * flops / 1e12 / fp32_peak, "fp32_tflops": value * flops / 1e12,
+                     "fp32_frac": value * flops / 1e12 / fp32_peak,
                      "hbm_frac": value * bytes_ / 1e9 / hbm_peak, "hbm_peak": hbm_peak, "hbm_peak_kind": peak_kind,
                      "flops_per_position": flops, "bytes_per_position": bytes_},
         "step": "one iteration: order draw and upload, then per 64 positions one gradient pass (forward, amplitude "
