@@ -433,15 +433,8 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
       // qNewton the max of sum_o|O| over the object outside the patch, which
       // this position leaves unchanged until its momentum step
       float mx[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-        const int l = i / NP, x = i - (i / NP) * NP;
-        const float2* src = s.object + (size_t)(row0 + line0 + l) * No + col0 + x;
-        float sp2 = 0.f, sp1 = 0.f, so2 = 0.f;
-        for (int o = 0; o < nosm; ++o) {
-          const float2 v = ld_cg(src + o * No2);
-          sm.obj[o * LN + i] = v;
-          so2 += cabs2(v);
-        }
+      auto norms = [&](int i, float so2) {
+        float sp2 = 0.f, sp1 = 0.f;
         for (int p = 0; p < npsm; ++p) {
           const float q = cabs2(sm.probe[p * pst + i]);
           sp2 += q;
@@ -450,6 +443,41 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         mx[0] = fmaxf(mx[0], sp2);
         mx[1] = fmaxf(mx[1], so2);
         mx[2] = fmaxf(mx[2], sp1);
+      };
+      if constexpr (FAST) {
+        // one object mode: a thread's loads of up to four pixels are all in
+        // flight before the first is used
+        constexpr int U = 4;
+        for (int i0 = threadIdx.x; i0 < LN; i0 += U * (int)blockDim.x) {
+          float2 v[U];
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * (int)blockDim.x;
+            const int ic = i < LN ? i : i0;
+            const int l = ic / NP, x = ic - (ic / NP) * NP;
+            v[q] = ld_cg(s.object + (size_t)(row0 + line0 + l) * No + col0 + x);
+          }
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * (int)blockDim.x;
+            if (i < LN) {
+              sm.obj[i] = v[q];
+              norms(i, cabs2(v[q]));
+            }
+          }
+        }
+      } else {
+        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+          const int l = i / NP, x = i - (i / NP) * NP;
+          const float2* src = s.object + (size_t)(row0 + line0 + l) * No + col0 + x;
+          float so2 = 0.f;
+          for (int o = 0; o < nosm; ++o) {
+            const float2 v = ld_cg(src + o * No2);
+            sm.obj[o * LN + i] = v;
+            so2 += cabs2(v);
+          }
+          norms(i, so2);
+        }
       }
       if (qn) {
         // qNewton.py:130 takes the max over the whole object after the patch
