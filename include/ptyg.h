@@ -177,6 +177,13 @@ typedef struct ptyg_geometry {
   int32_t probe_in_smem; /* 0 = choose (shared memory when it fits), 1 = keep
                             the CTA's probe rows in global memory (L2),
                             2 = require them in shared memory */
+  int32_t asp_table_in_smem; /* ASP only: 0 = choose (the CTA's columns of the
+                                transfer function, one block per wavelength,
+                                copied into shared memory once per launch by
+                                the bulk-copy engine when they fit beside the
+                                probe rows), 1 = read them from global memory
+                                (L2) at every position, 2 = require them in
+                                shared memory */
 } ptyg_geometry;
 
 /* Engine scalars (ePIE.py:35-42, mPIE.py:233-245, qNewton.py:43-52,
@@ -256,7 +263,9 @@ PTYG_API int ptyg_plan_info(ptyg_plan* plan, int* cluster, int* threads, int* sm
 
 /* Intensity-projection switches (BaseEngine.intensityProjection,
  * PtyLab/Engines/BaseEngine.py:870-1012; adaptiveDenoising :1805-1822);
- * all zero = the standard projection.  Not for e3PIE plans. */
+ * all zero = the standard projection.  e3PIE plans take every switch but
+ * the interferometric constraint (its detector projection is BaseEngine's,
+ * PtyLab/Engines/e3PIE.py:118). */
 typedef struct ptyg_projection {
   int32_t intensity_constraint; /* enum ptyg_intensity_constraint */
   int32_t adaptive_denoising;   /* params.adaptiveDenoisingSwitch */
@@ -321,7 +330,9 @@ PTYG_API int ptyg_plan_frame_errors_all_device(ptyg_plan* plan, double* device_o
 PTYG_API int ptyg_plan_detector_error(ptyg_plan* plan, int scan, float* out, void* stream);
 
 /* Device status word of scan `scan` (0 = ok; 2 = a position fell outside
- * the object and was skipped). */
+ * the object and was skipped; 3 = the copy of the ASP transfer function into
+ * shared memory did not complete within its bounded wait, so the launch's
+ * results are not to be used). */
 PTYG_API int ptyg_plan_status(ptyg_plan* plan, int scan, int* host_status, void* stream);
 
 /* ------------------------------------------------------------------------

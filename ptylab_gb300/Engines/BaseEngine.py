@@ -104,8 +104,8 @@ class BaseEngine(object):
             raise ValueError("FourierMaskSwitch needs experimentalData.W")
         if getattr(p, "intensityMask", False) and getattr(rec, "intensity_mask", None) is None:
             raise ValueError("params.intensityMask needs reconstruction.intensity_mask")
-        if self._projection_switches_on() and self.engine_name == "e3PIE":
-            raise NotImplementedError("the GB300 e3PIE runs the standard intensity projection only")
+        if ic == "interferometric" and self.engine_name == "e3PIE":
+            raise NotImplementedError("the GB300 e3PIE runs every projection switch but the interferometric constraint")
         for name in _UNSUPPORTED:
             if getattr(p, name, False):
                 raise NotImplementedError(f"params.{name} is not supported by the GB300 engines")
@@ -295,6 +295,7 @@ class BaseEngine(object):
             fpm=int(d.operationMode == "FPM"), cluster=int(getattr(self, "cluster", 0) or 0), throughput=throughput,
             threads=int(getattr(self, "threads", 0) or 0),
             nlambda=int(getattr(rec, "nlambda", 1)),
+            asp_table_in_smem=int(getattr(self, "aspTableInSmem", 0) or 0),
         )
 
     def _plan_and_bind(self, plan=None, scan=0, num_scans=1, throughput=0):
@@ -654,6 +655,9 @@ class BaseEngine(object):
         torch = _torch()
         stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
         _native.check(self._dev["lib"].ptyg_plan_status(self._plan, self._scan, C.byref(st), stream), "ptyg_plan_status")
+        if st.value == 3:
+            raise RuntimeError("device status 3: the ASP transfer function's copy into shared memory did not "
+                               "complete within its bounded wait; this launch's results are not valid")
         if st.value != 0:
             raise RuntimeError(f"device status {st.value}: a scan position fell outside the object")
 

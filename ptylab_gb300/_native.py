@@ -60,6 +60,7 @@ class Geometry(C.Structure):
         ("nlambda", C.c_int32),
         ("threads", C.c_int32),
         ("probe_in_smem", C.c_int32),
+        ("asp_table_in_smem", C.c_int32),
     ]
 
 

@@ -349,6 +349,7 @@ struct ptyg_plan {
   int C = 1;
   int threads = 256;
   bool probeInSmem = true;
+  bool hInSmem = false;  // ASP: the CTA's transfer-function columns in shared memory
   size_t smem = 0;
   float2* fresnelQ = nullptr;
   float2* aspH = nullptr;
@@ -432,6 +433,8 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
     return fail(PTYG_ERR_INVALID, "threads=%d: a multiple of 32 in [128, %d]", g.threads,
                 g.engine == PTYG_MQNEWTON ? 256 : 512);
   if (g.probe_in_smem < 0 || g.probe_in_smem > 2) return fail(PTYG_ERR_INVALID, "probe_in_smem=%d", g.probe_in_smem);
+  if (g.asp_table_in_smem < 0 || g.asp_table_in_smem > 2)
+    return fail(PTYG_ERR_INVALID, "asp_table_in_smem=%d", g.asp_table_in_smem);
   if (!valid_np(g.Np)) return fail(PTYG_ERR_UNSUPPORTED, "Np=%d: supported sizes are 32, 64, 128, 256", g.Np);
   if (g.No < g.Np) return fail(PTYG_ERR_INVALID, "No=%d smaller than Np=%d", g.No, g.Np);
   if (g.nosm < 1 || g.npsm < 1 || g.nslice < 1 || g.num_frames < 1 || g.num_scans < 1)
@@ -459,31 +462,40 @@ extern "C" int ptyg_plan_create(const ptyg_geometry* geometry, ptyg_plan** plan)
   p->device = dev;
   int maxSmem = 0;
   cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  // the first instantiated cluster shape that fits in shared memory and can be co-scheduled
+  // the first instantiated cluster shape that fits in shared memory and can
+  // be co-scheduled; per shape the probe rows in shared memory first, then
+  // (ASP) the transfer function's columns
+  const bool e3 = g.engine == PTYG_E3PIE;
+  const bool aspTable = g.propagator == PTYG_ASP && !e3;
+  auto fits = [&](int c, bool psm, bool hsm) {
+    if ((g.probe_in_smem == 1 && psm) || (g.probe_in_smem == 2 && !psm)) return false;
+    if (aspTable && ((g.asp_table_in_smem == 1 && hsm) || (g.asp_table_in_smem == 2 && !hsm))) return false;
+    if (hsm && !aspTable) return false;
+    if (e3 && psm) return false;  // e3PIE keeps its probe slices in global memory
+    p->C = c;
+    p->probeInSmem = psm;
+    p->hInSmem = hsm;
+    p->threads = g.threads > 0 ? g.threads : engine_threads(g, c);
+    p->smem = e3 ? ptyg::e3pie_smem_bytes(g.Np, c, g.npsm)
+                 : ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.nlambda, g.engine, psm, hsm);
+    if ((int)p->smem > maxSmem) return false;
+    int nclusters = 0;
+    cudaError_t e = e3 ? ptyg::e3pie_max_clusters(g.Np, c, p->threads, p->smem, &nclusters)
+                       : ptyg::engine_max_clusters(g.Np, g.engine, g.nlambda, c, p->threads, p->smem, &nclusters);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return nclusters > 0;
+  };
   bool found = false;
   for (int c : cluster_candidates(g)) {
     if (!ptyg::engine_shape_supported(g.Np, c)) continue;
     for (bool psm : {true, false}) {
-      if ((g.probe_in_smem == 1 && psm) || (g.probe_in_smem == 2 && !psm)) continue;
-      p->C = c;
-      p->probeInSmem = psm;
-      p->threads = g.threads > 0 ? g.threads : engine_threads(g, c);
-      const bool e3 = g.engine == PTYG_E3PIE;
-      if (e3 && psm) continue;  // e3PIE keeps its probe slices in global memory
-      p->smem = e3 ? ptyg::e3pie_smem_bytes(g.Np, c, g.npsm)
-                   : ptyg::engine_smem_bytes(g.Np, c, g.nosm, g.npsm, g.nlambda, g.engine, psm);
-      if ((int)p->smem > maxSmem) continue;
-      int nclusters = 0;
-      cudaError_t e = e3 ? ptyg::e3pie_max_clusters(g.Np, c, p->threads, p->smem, &nclusters)
-                         : ptyg::engine_max_clusters(g.Np, g.engine, g.nlambda, c, p->threads, p->smem, &nclusters);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        continue;
+      for (bool hsm : {true, false}) {
+        if ((found = fits(c, psm, hsm))) break;
       }
-      if (nclusters > 0) {
-        found = true;
-        break;
-      }
+      if (found) break;
     }
     if (found) break;
   }
@@ -679,6 +691,7 @@ extern "C" int ptyg_plan_run(ptyg_plan* p, const ptyg_update_params* u, int star
   a.cluster = p->C;
   a.tilesPerRow = (g.No + ptyg::TILE - 1) / ptyg::TILE;
   a.probeInSmem = p->probeInSmem ? 1 : 0;
+  a.hInSmem = p->hInSmem ? 1 : 0;
   a.betaO = u->beta_object;
   a.betaP = u->beta_probe;
   a.alphaO = u->alpha_object;
@@ -854,10 +867,8 @@ extern "C" int ptyg_plan_set_projection(ptyg_plan* p, const ptyg_projection* pr,
     return fail(PTYG_ERR_UNSUPPORTED, "the interferometric constraint runs with Fraunhofer and Fresnel plans");
   if (q.intensity_constraint == PTYG_INTERFEROMETRIC && p->g.engine == PTYG_MQNEWTON)
     return fail(PTYG_ERR_UNSUPPORTED, "the interferometric constraint runs with ePIE, mPIE and qNewton plans");
-  const bool any = q.intensity_constraint || q.adaptive_denoising || q.background_mode || q.fourier_mask ||
-                   q.intensity_mask;
-  if (p->g.engine == PTYG_E3PIE && any)
-    return fail(PTYG_ERR_UNSUPPORTED, "e3PIE runs the standard projection only");
+  if (p->g.engine == PTYG_E3PIE && q.intensity_constraint == PTYG_INTERFEROMETRIC)
+    return fail(PTYG_ERR_UNSUPPORTED, "e3PIE runs every projection switch but the interferometric constraint");
   if (q.fourier_mask && !W) return fail(PTYG_ERR_INVALID, "FourierMaskSwitch needs W");
   if (q.intensity_mask && !intensity_mask) return fail(PTYG_ERR_INVALID, "intensityMask needs intensity_mask");
   cudaStream_t st = (cudaStream_t)stream;

@@ -7,7 +7,9 @@
 //
 //   forward   esw_0 = O_0 * P_0;  for s = 1..S-1:
 //             P_s = ifft2(fft2(esw_{s-1}) * H),  esw_s = P_s * O_s    (e3PIE.py:99-115)
-//   detector  intensity projection of the last slice's exit waves     (e3PIE.py:118)
+//   detector  intensity projection of the last slice's exit waves     (e3PIE.py:118),
+//             with every switch of the engines' projection but the
+//             interferometric constraint (project_intensities)
 //   backward  DELTA = eswUpdate - esw_{S-1}; for s = S-1..1:
 //             O_s += betaObject * sum_p conj(P_s) DELTA / max sum_p |P_s|^2
 //             P_s += 0.9 * conj(O_s) DELTA / max |O_s|^2
@@ -48,8 +50,9 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
   float* dat = fr + LN;  // LN: this position's intensities, then (once the projection has read
                          // them) the next position's, in flight
   unsigned* slots = reinterpret_cast<unsigned*>(dat + LN);
-  double* redD = reinterpret_cast<double*>(slots + 2 * RED_BANK);
-  float* redF = reinterpret_cast<float*>(redD + 32);
+  double* redD = reinterpret_cast<double*>(slots + 2 * RED_BANK);  // 64
+  double* part = redD + 64;                                          // 64: the projection's cluster sums
+  float* redF = reinterpret_cast<float*>(part + 64);
   unsigned* slots0 = dsmem(slots, 0);
 
   if (threadIdx.x < 2 * RED_BANK) slots[threadIdx.x] = 0u;
@@ -124,7 +127,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
 
     // ---------------- forward through the slices
     for (int sl = 1; sl < S; ++sl) {
-      column_filter<E, L>(tile, rows, F, a.sliceH, false, crank, K, K);
+      column_filter<E, L>(tile, rows, F, a.sliceH, (size_t)NP * NP, false, false, crank, K, K);
       cluster_sync(C);
       // P_s rows (natural order) into the row buffer and the probe's slice sl
       row_tasks<E, true>(
@@ -168,22 +171,15 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           F, K * L, [&](int t, int lo, int hi) { return col(t, lo + hi); },
           [&](int t, int lo, int hi, float2 v) { col(t, lo + hi) = v; });
       __syncthreads();
-      {
-        float e = 0.f;
-        const bool det = a.writeDetErr && s.detErr;
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-          const int c = i / NP, sy = i % NP;
-          float ie = 0.f;
-          for (int k = 0; k < K; ++k) ie += cabs2(tile[tix<L>(k * NP + sy, c)]);
-          ie *= inv2;
-          const float im = datc[i];
-          const float d = fabsf(im - ie);
-          e += d;
-          if (det) s.detErr[((size_t)frame * NP + sx0) * NP + i] = d;
-          fr[i] = sqrtf(im / (ie + 1e-10f)) * inv2;
-        }
-        err = (double)e;
-      }
+      err = project_intensities<NP, L, false, false, false>(
+          a, s, frame, blk0, crank, ProjectionIO{fr, datc, part, redD},
+          [&](int i) {
+            const int c = i / NP, sy = i % NP;
+            float ie = 0.f;
+            for (int k = 0; k < K; ++k) ie += cabs2(tile[tix<L>(k * NP + sy, c)]);
+            return ie * inv2;
+          },
+          inv2);
       __syncthreads();
       fft_tasks<E, true>(
           F, K * L, [&](int t, int lo, int hi) { return cscale(col(t, lo + hi), fr[(t % L) * NP + lo + hi]); },
@@ -191,32 +187,26 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       __syncthreads();
       flush_columns<NP, L>(tile, rows, K, sx0);
     } else {
-      column_filter<E, L>(tile, rows, F, a.aspH, false, crank, K, K);
+      column_filter<E, L>(tile, rows, F, a.aspH, (size_t)NP * NP, false, false, crank, K, K);
       cluster_sync(C);
       row_tasks<E, true>(
           a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, rsw<L>(t, lo) + hi); },
           [&](int t, int lo, int hi, float2 v) { row(t, lo + hi) = v; }, pairs);
       __syncthreads();
-      {
-        float e = 0.f;
-        const bool det = a.writeDetErr && s.detErr;
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-          float ie = 0.f;
-          for (int k = 0; k < K; ++k) ie += cabs2(rows[k * LN + i]);
-          const float im = datc[i];
-          const float d = fabsf(im - ie);
-          e += d;
-          if (det) s.detErr[((size_t)frame * NP + line0) * NP + i] = d;
-          fr[i] = sqrtf(im / (ie + 1e-10f));
-        }
-        err = (double)e;
-      }
+      err = project_intensities<NP, L, false, false, false>(
+          a, s, frame, blk0, crank, ProjectionIO{fr, datc, part, redD},
+          [&](int i) {
+            float ie = 0.f;
+            for (int k = 0; k < K; ++k) ie += cabs2(rows[k * LN + i]);
+            return ie;
+          },
+          1.f);
       __syncthreads();
       row_tasks<E, false>(
           a.twiddle, K * L, [&](int t, int lo, int hi) { return cscale(row(t, lo + hi), fr[(t % L) * NP + lo + hi]); },
           scatter, pairs);
       cluster_sync(C);
-      column_filter<E, L>(tile, rows, F, a.aspH, true, crank, K, K);
+      column_filter<E, L>(tile, rows, F, a.aspH, (size_t)NP * NP, false, true, crank, K, K);
     }
     // every read of this position's intensities is behind a CTA barrier by
     // now: fetch the next position's while the backward pass runs
@@ -275,7 +265,7 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
         row_tasks<E, false>(
             a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, lo + hi); }, scatter, pairs);
         cluster_sync(C);
-        column_filter<E, L>(tile, rows, F, a.sliceH, true, crank, K, K);
+        column_filter<E, L>(tile, rows, F, a.sliceH, (size_t)NP * NP, false, true, crank, K, K);
         cluster_sync(C);
       }
     }
@@ -292,8 +282,9 @@ size_t e3pie_smem_bytes(int Np, int C, int npsm) {
   const int L = Np / C;
   const size_t LN = (size_t)L * Np;
   const size_t n = (size_t)npsm * Np * L + (size_t)npsm * LN;
-  // redF holds 32 floats per reduced value: MAX_SLICES + 1 of them
-  return n * sizeof(float2) + 2 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 32 * sizeof(double) +
+  // redD and the projection's cluster-sum partials: 64 doubles each; redF
+  // holds 32 floats per reduced value: MAX_SLICES + 1 of them
+  return n * sizeof(float2) + 2 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 128 * sizeof(double) +
          8 * 32 * sizeof(float) + 64;
 }
 

@@ -6,16 +6,17 @@
 
 namespace ptyg {
 
-size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int nlambda, int engine, bool probe_in_smem) {
+size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int nlambda, int engine, bool probe_in_smem,
+                         bool asp_table_in_smem) {
   const int L = Np / C;
   const size_t LN = (size_t)L * Np;
   const bool qn = engine == ENG_QNEWTON || engine == ENG_MQNEWTON;
-  const size_t n =
-      smem_complex_elems(Np, L, nlambda * nosm * npsm, nlambda * nosm, nlambda * npsm, qn, probe_in_smem);
+  const size_t n = smem_complex_elems(Np, L, nlambda * nosm * npsm, nlambda * nosm, nlambda * npsm, qn, probe_in_smem,
+                                      asp_table_in_smem ? nlambda : 0);
   // + fr, dat (2 LN floats), slots, redD (4 x 32 doubles), redF (4 x 32
-  // floats), part (4 x 16 doubles), alignment slack
+  // floats), part (4 x 16 doubles), the copy's mbarrier, alignment slack
   return n * sizeof(float2) + 2 * LN * sizeof(float) + 2 * RED_BANK * sizeof(unsigned) + 4 * 32 * sizeof(double) +
-         4 * 32 * sizeof(float) + 4 * 16 * sizeof(double) + 64;
+         4 * 32 * sizeof(float) + 4 * 16 * sizeof(double) + sizeof(unsigned long long) + 64;
 }
 
 bool engine_shape_supported(int Np, int cluster) {

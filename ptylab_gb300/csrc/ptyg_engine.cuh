@@ -74,6 +74,7 @@ struct EngineArgs {
   int cluster;
   int tilesPerRow;         // ceil(No / TILE)
   int probeInSmem;         // keep the CTA's probe rows in shared memory
+  int hInSmem;             // ASP: copy the CTA's columns of aspH (each wavelength's) into shared memory
   float betaO, betaP, alphaO, alphaP, regO, regP, frictionM, feedbackM, weightP, bethSlice;
   // mqNewton: method, float32 beta1, 1-beta1, beta2, 1-beta2, 1-beta^itr, step sizes
   int momentum;

@@ -259,13 +259,49 @@ PTYG_DEV void store_column(float2* tile, const float2 (&v)[E], int k, int c) {
   for (int j = 0; j < E; ++j) tile[tix<L>(k * NP + lane + 32 * j, c)] = v[j];
 }
 
+// Copy nblk blocks of `bytes` bytes (block b from src + b * srcStride, 16-byte
+// aligned, bytes a multiple of 16) to consecutive shared memory at dst with
+// the bulk-copy engine (cp.async.bulk, completion on the mbarrier `bar`), and
+// wait in every thread of the CTA, polling at most BULK_WAIT_POLLS times.
+// Returns false when the wait gave up (the caller raises its status word).
+constexpr long long BULK_WAIT_POLLS = 1ll << 22;
+PTYG_DEV bool bulk_copy_wait(float2* dst, const float2* src, unsigned bytes, int nblk, size_t srcStride,
+                             unsigned long long* bar) {
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  const unsigned d0 = (unsigned)__cvta_generic_to_shared(dst);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(bytes * (unsigned)nblk)
+                 : "memory");
+    for (int k = 0; k < nblk; ++k)
+      asm volatile(
+          "{\n.reg .u64 g;\ncvta.to.global.u64 g, %1;\n"
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [g], %2, [%3];\n}\n" ::"r"(
+              d0 + (unsigned)k * bytes),
+          "l"(src + (size_t)k * srcStride), "r"(bytes), "r"(b)
+          : "memory");
+  }
+  __syncthreads();  // the barrier is initialised before anyone polls it
+  unsigned done = 0;
+  for (long long i = 0; i < BULK_WAIT_POLLS && !done; ++i)
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(b)
+        : "memory");
+  return done != 0;
+}
+
 // Column pass that multiplies the spectrum by H (or conj H) / Np^2 between a
 // forward and an inverse column transform (ASP, Operators.py:155-230); the
 // result goes to the row owners' row buffers (visible after a cluster barrier).
-// Column task t = k * L + c is transformed in place in the tile.
+// Column task t = k * L + c is transformed in place in the tile.  H: the
+// table in global memory (Fourier layout [sx][sy], tables Hset apart), or
+// with hsm the CTA's own columns of it in shared memory (column c at c * NP).
 template <int E, int L, bool SETS = false>
-PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, const float2* H, bool conjH, int crank,
-                            int K, int kPerSet) {
+PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, const float2* H, size_t Hset, bool hsm,
+                            bool conjH, int crank, int K, int kPerSet) {
   constexpr int NP = 32 * E;
   const int sx0 = crank * L;
   const float inv2 = 1.f / (float)(NP * NP);
@@ -275,8 +311,8 @@ PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, con
       [&](int t, int lo, int hi, float2 v) {
         const int k = t / L, c = t % L;
         // SETS: one table per wavelength, modes k of wavelength k / kPerSet
-        const float2* h = H + (SETS ? (size_t)(k / kPerSet) * NP * NP : 0) + (size_t)(sx0 + c) * NP;
-        float2 hv = __ldg(h + lo + hi);
+        const float2* h = H + (SETS ? (size_t)(k / kPerSet) * Hset : 0) + (size_t)((hsm ? 0 : sx0) + c) * NP;
+        float2 hv = hsm ? h[lo + hi] : __ldg(h + lo + hi);
         if (conjH) hv.y = -hv.y;
         col(t, lo + hi) = cscale(cmul(v, hv), inv2);
       });
@@ -286,6 +322,117 @@ PTYG_DEV void column_filter(float2* tile, float2* rows, const WarpFFT<E>& F, con
       [&](int t, int lo, int hi, float2 v) { col(t, lo + hi) = v; });
   __syncthreads();
   flush_columns<NP, L>(tile, rows, K, sx0);
+}
+
+// The intensity projection of a CTA's LN = L * NP detector pixels
+// (BaseEngine.py:881-1009): getRMSD on the estimate (plus the background),
+// adaptive denoising (:1805-1822, a frame mean: one cluster sum), the
+// standard / poission / exponential / fluctuation constraint (fluctuation:
+// two more frame sums), the intensity mask, the background update.  Iest(i)
+// is the estimate of pixel i; the factor goes to io.fr[i] times outScale.
+// Tables and the background are in the data layout, this CTA's block at
+// blk0 * NP.  Returns this thread's (FourierMask-weighted) error sum.
+// COLS: warp w handles the NP / 32 pixels of its own column w (pixel
+// w * NP + 32 r + lane gets Iest(r)), else every thread strides over the
+// CTA's LN pixels (pixel i gets Iest(i)); the column form serves only
+// single-pass projections.  FAST: the standard projection without
+// background, masks or denoising, folded at compile time.  INTERF: the
+// interferometric constraint compiled in (the raw factor goes to fr, applied
+// with the reference field after the projection: no intensity mask there,
+// BaseEngine.py:975-982).
+struct ProjectionIO {
+  float* fr;         // L * NP factors (between the passes of a two-pass projection: the estimates)
+  const float* dat;  // L * NP measured intensities
+  double* part;      // cluster-sum partials, rank 0's read by all (64 doubles)
+  double* redD;      // CTA scratch (64 doubles)
+};
+template <int NP, int L, bool FAST, bool INTERF, bool COLS, class IestF>
+PTYG_DEV double project_intensities(const EngineArgs& a, const ScanDev& s, int frame, int blk0, int crank,
+                                    const ProjectionIO& io, IestF&& Iest, float outScale) {
+  constexpr int C = NP / L, LN = L * NP, E = NP / 32;
+  const unsigned lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const bool interf = INTERF && a.iconstraint == IC_INTERFEROMETRIC;
+  const int icon = FAST ? (int)IC_STANDARD : a.iconstraint;
+  const bool denoise = !FAST && a.denoise;
+  float* fr = io.fr;
+  const float* dat = io.dat;
+  const bool det = a.writeDetErr && s.detErr;
+  const size_t tb = (size_t)blk0 * NP;
+  float* bg = (!FAST && a.bgMode) ? s.background + tb : nullptr;
+  const float* Wt = (!FAST && a.fmask) ? a.W + tb : nullptr;
+  const float* Mt = (!FAST && a.imask) ? a.imaskTab + tb : nullptr;
+  float e = 0.f, noise = 0.f, aleph = 0.f;
+  auto denoised = [&](float im) {
+    if (!denoise) return im;
+    const float am = fmaxf(sqrtf(im) - noise, 0.f);
+    return am * am;
+  };
+  auto finish = [&](int i, float ie, float im, float d) {
+    const float q = denoised(im) / (ie + 1e-10f);
+    float frac;
+    if (icon == IC_POISSON) {
+      frac = q;
+    } else if (icon == IC_EXPONENTIAL) {
+      const float w = expf(-0.05f * (d / (ie + 1e-10f)));
+      frac = w * sqrtf(q) + (1.f - w);
+    } else if (icon == IC_FLUCTUATION) {
+      frac = (1.f + aleph) * 0.5f * q;
+    } else {  // standard and interferometric (BaseEngine.py:955-962)
+      frac = sqrtf(q);
+    }
+    fr[i] = interf ? frac : (Mt ? frac * Mt[i] + (Mt[i] - 1.f) : frac) * outScale;
+    if (bg) {
+      const float u = 1.f + a.invFrames * (sqrtf(frac) - 1.f);
+      float b = bg[i] * (u * u);
+      if (Wt) b *= Wt[i];
+      bg[i] = b;
+    }
+  };
+  const bool twoPass = !COLS && (denoise || icon == IC_FLUCTUATION);
+  double dn = 0.0;
+  auto pixel = [&](int i, float ie) {
+    if (bg) ie += bg[i];
+    const float im = dat[i];
+    const float d = fabsf(im - ie);
+    e += Wt ? d * Wt[i] : d;
+    if (det) s.detErr[((size_t)frame * NP + blk0) * NP + i] = d;
+    if (twoPass) {
+      fr[i] = ie;  // kept for the second pass (same thread)
+      if (denoise) dn += (double)(sqrtf(im) - sqrtf(fabsf(ie)));
+    } else {
+      finish(i, ie, im, d);
+    }
+  };
+  if constexpr (COLS) {
+#pragma unroll
+    for (int r = 0; r < E; ++r) pixel(warp * NP + 32 * r + (int)lane, Iest(r));
+  } else {
+    for (int i = threadIdx.x; i < LN; i += blockDim.x) pixel(i, Iest(i));
+  }
+  if (twoPass) {
+    if (denoise) {
+      double v[1] = {dn};
+      cluster_sum_n<1, C>(v, io.part, io.redD, crank);
+      noise = fabsf((float)(v[0] / (double)(NP * NP)));
+    }
+    if (icon == IC_FLUCTUATION) {
+      double v[2] = {0.0, 0.0};
+      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+        const float ie = fr[i], imd = denoised(dat[i]), w = Wt ? Wt[i] : 1.f;
+        v[0] += (double)(imd * ie * w);
+        v[1] += (double)(imd * imd * w);
+      }
+      cluster_sum_n<2, C>(v, io.part + 32, io.redD, crank);
+      aleph = (float)(v[0] / v[1]);
+      if (crank == 0 && threadIdx.x == 0 && s.iscale) s.iscale[frame] = (double)aleph;
+    }
+    for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+      const float ie = fr[i], im = dat[i];
+      finish(i, ie, im, fabsf(im - ie));
+    }
+  }
+  return (double)e;
 }
 
 // Prefetch the measured intensities of order slot `it` (if it exists and is a

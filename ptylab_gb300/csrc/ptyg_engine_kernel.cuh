@@ -304,6 +304,7 @@ struct Smem {
   float2* tile;     // K * NP * L: the CTA's column block (written by every CTA; swizzled, tix)
   float2* rows;     // K * L * NP: the CTA's rows, Fourier layout along x
   float2* U;        // qNewton probe numerators, npsm * L * NP
+  float2* H;        // ASP (hInSmem): the CTA's L columns of the transfer function, one block per wavelength
   float* fr;        // L * NP projection factors
   float* dat;       // L * NP measured intensities: this position's, then (once the
                     // projection has read them) the next position's, in flight
@@ -311,13 +312,14 @@ struct Smem {
   double* redD;     // 4 * 32
   float* redF;      // 4 * 32
   double* part;     // 4 * 16: mqNewton gradient-norm partials [value][CTA] (rank 0)
+  unsigned long long* bar;  // the transfer function copy's mbarrier
 };
 
 __host__ __device__ inline size_t smem_complex_elems(int NP, int L, int K, int nosm, int npsm, bool qn,
-                                                     bool probe_in_smem) {
+                                                     bool probe_in_smem, int hBlocks) {
   const size_t LN = (size_t)L * NP;
   return (probe_in_smem ? (size_t)npsm * LN : 0) + (size_t)nosm * LN + (size_t)K * NP * L + (size_t)K * LN +
-         (qn ? npsm * LN : 0);
+         (qn ? npsm * LN : 0) + (size_t)hBlocks * LN;
 }
 
 // ------------------------------------------------------------------ kernel
@@ -377,13 +379,27 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
   sm.tile = sm.obj + nosm * LN;
   sm.rows = sm.tile + K * NP * L;
   sm.U = sm.rows + K * LN;
-  sm.fr = reinterpret_cast<float*>(sm.U + (qn ? npsm * LN : 0));
+  const bool hsm = asp && a.hInSmem;
+  sm.H = sm.U + (qn ? npsm * LN : 0);
+  sm.fr = reinterpret_cast<float*>(sm.H + (hsm ? nl * LN : 0));
   sm.dat = sm.fr + LN;
   sm.slots = reinterpret_cast<unsigned*>(sm.dat + LN);
   sm.redD = reinterpret_cast<double*>(sm.slots + 2 * RED_BANK);
   sm.redF = reinterpret_cast<float*>(sm.redD + 4 * 32);
   sm.part = reinterpret_cast<double*>(sm.redF + 4 * 32);
+  sm.bar = reinterpret_cast<unsigned long long*>(sm.part + 4 * 16);
   unsigned* slots0 = dsmem(sm.slots, 0);
+  // ASP: the CTA's columns sx0 .. sx0 + L of each wavelength's transfer
+  // function are contiguous in the Fourier layout [sx][sy]: one bulk copy
+  // per wavelength, read by the column filters of every position
+  const float2* Htab = hsm ? sm.H : a.aspH;
+  const size_t Hset = hsm ? (size_t)LN : (size_t)NP * NP;
+  if (hsm) {
+    if (!bulk_copy_wait(sm.H, a.aspH + (size_t)sx0 * NP, (unsigned)(LN * sizeof(float2)), nl, (size_t)NP * NP,
+                        sm.bar) &&
+        threadIdx.x == 0)
+      atomicCAS(s.status, 0, 3);
+  }
 
   if (psm) {
     for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
@@ -520,104 +536,18 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
     cp_async_wait_all();  // this position's intensities (the one group in flight)
     cluster_sync(C);
 
-    // The intensity projection of this CTA's LN detector pixels
-    // (BaseEngine.py:881-1009): getRMSD on the estimate (plus the background),
-    // adaptive denoising (:1805-1822, a frame mean: one cluster sum), the
-    // standard / poission / exponential / fluctuation constraint (fluctuation:
-    // two more frame sums), the intensity mask, the background update.  Iest(i)
-    // is the estimate of pixel i; the factor goes to sm.fr[i] times outScale.
-    // Tables and the background are in the data layout, this CTA's block at
-    // blk0 * NP.  Returns this thread's (FourierMask-weighted) error sum.
-    // cols (a compile-time tag): warp w handles the E pixels of its own
-    // column w (pixel w * NP + 32 r + lane gets Iest(r)), else every thread
-    // strides over the CTA's LN pixels (pixel i gets Iest(i)).  The column
-    // form serves the fused pass B and only single-pass projections.
-    // the interferometric constraint is compiled into the several-wavelength
-    // instantiation only (which serves ePIE, mPIE and qNewton for any nlambda),
-    // so the standard kernel's registers stay as they are
+    // The intensity projection of this CTA's pixels (project_intensities):
+    // cols (a compile-time tag) picks the warp-per-column form of the fused
+    // pass B.  The interferometric constraint is compiled into the
+    // several-wavelength instantiation only (which serves ePIE, mPIE and
+    // qNewton for any nlambda), so the standard kernel's registers stay as
+    // they are.
     const bool interf = VAR == VAR_POLY && a.iconstraint == IC_INTERFEROMETRIC;
     const int icon = FAST ? (int)IC_STANDARD : a.iconstraint;
     const bool denoise = !FAST && a.denoise;
     auto project = [&](auto Iest, float outScale, auto colsTag) -> double {
-      constexpr bool cols = decltype(colsTag)::value;
-      const bool det = a.writeDetErr && s.detErr;
-      const size_t tb = (size_t)blk0 * NP;
-      float* bg = (!FAST && a.bgMode) ? s.background + tb : nullptr;
-      const float* Wt = (!FAST && a.fmask) ? a.W + tb : nullptr;
-      const float* Mt = (!FAST && a.imask) ? a.imaskTab + tb : nullptr;
-      float e = 0.f, noise = 0.f, aleph = 0.f;
-      auto denoised = [&](float im) {
-        if (!denoise) return im;
-        const float am = fmaxf(sqrtf(im) - noise, 0.f);
-        return am * am;
-      };
-      auto finish = [&](int i, float ie, float im, float d) {
-        const float q = denoised(im) / (ie + 1e-10f);
-        float frac;
-        if (icon == IC_POISSON) {
-          frac = q;
-        } else if (icon == IC_EXPONENTIAL) {
-          const float w = expf(-0.05f * (d / (ie + 1e-10f)));
-          frac = w * sqrtf(q) + (1.f - w);
-        } else if (icon == IC_FLUCTUATION) {
-          frac = (1.f + aleph) * 0.5f * q;
-        } else {  // standard and interferometric (BaseEngine.py:955-962)
-          frac = sqrtf(q);
-        }
-        // interferometric: the raw factor, applied with the reference field
-        // after the projection (no intensity mask there, BaseEngine.py:975-982)
-        sm.fr[i] = interf ? frac : (Mt ? frac * Mt[i] + (Mt[i] - 1.f) : frac) * outScale;
-        if (bg) {
-          const float u = 1.f + a.invFrames * (sqrtf(frac) - 1.f);
-          float b = bg[i] * (u * u);
-          if (Wt) b *= Wt[i];
-          bg[i] = b;
-        }
-      };
-      const bool twoPass = !cols && (denoise || icon == IC_FLUCTUATION);
-      double dn = 0.0;
-      auto pixel = [&](int i, float ie) {
-        if (bg) ie += bg[i];
-        const float im = dat[i];
-        const float d = fabsf(im - ie);
-        e += Wt ? d * Wt[i] : d;
-        if (det) s.detErr[((size_t)frame * NP + blk0) * NP + i] = d;
-        if (twoPass) {
-          sm.fr[i] = ie;  // kept for the second pass (same thread)
-          if (denoise) dn += (double)(sqrtf(im) - sqrtf(fabsf(ie)));
-        } else {
-          finish(i, ie, im, d);
-        }
-      };
-      if constexpr (cols) {
-#pragma unroll
-        for (int r = 0; r < E; ++r) pixel(warp * NP + 32 * r + lane, Iest(r));
-      } else {
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) pixel(i, Iest(i));
-      }
-      if (twoPass) {
-        if (denoise) {
-          double v[1] = {dn};
-          cluster_sum_n<1, C>(v, sm.part, sm.redD, crank);
-          noise = fabsf((float)(v[0] / (double)(NP * NP)));
-        }
-        if (icon == IC_FLUCTUATION) {
-          double v[2] = {0.0, 0.0};
-          for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-            const float ie = sm.fr[i], imd = denoised(dat[i]), w = Wt ? Wt[i] : 1.f;
-            v[0] += (double)(imd * ie * w);
-            v[1] += (double)(imd * imd * w);
-          }
-          cluster_sum_n<2, C>(v, sm.part + 32, sm.redD, crank);
-          aleph = (float)(v[0] / v[1]);
-          if (crank == 0 && threadIdx.x == 0 && s.iscale) s.iscale[frame] = (double)aleph;
-        }
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-          const float ie = sm.fr[i], im = dat[i];
-          finish(i, ie, im, fabsf(im - ie));
-        }
-      }
-      return (double)e;
+      return project_intensities<NP, L, FAST, VAR == VAR_POLY, decltype(colsTag)::value>(
+          a, s, frame, blk0, crank, ProjectionIO{sm.fr, dat, sm.part, sm.redD}, Iest, outScale);
     };
 
     double err = 0.0;
@@ -734,7 +664,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
       flush_columns<NP, L>(sm.tile, sm.rows, K, sx0);
     } else {
       // ---------------- ASP: x H, real-space projection, x conj(H)
-      column_filter<E, L, POLY>(sm.tile, sm.rows, F, a.aspH, false, crank, K, nosmW * npsmW);
+      column_filter<E, L, POLY>(sm.tile, sm.rows, F, Htab, Hset, hsm, false, crank, K, nosmW * npsmW);
       cluster_sync(C);
       auto row = [&](int t, int i) -> float2& { return sm.rows[t * NP + i]; };
       auto pairs = [&](int t) { return reinterpret_cast<float4*>(sm.rows + t * NP); };
@@ -754,7 +684,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
           a.twiddle, K * L, [&](int t, int lo, int hi) { return cscale(row(t, lo + hi), sm.fr[(t % L) * NP + lo + hi]); },
           [&](int t, int lo, int hi, float2 v) { scatter_row<NP, L>(sm.tile, t / L, line0 + t % L, lo, hi, v); }, pairs);
       cluster_sync(C);
-      column_filter<E, L, POLY>(sm.tile, sm.rows, F, a.aspH, true, crank, K, nosmW * npsmW);
+      column_filter<E, L, POLY>(sm.tile, sm.rows, F, Htab, Hset, hsm, true, crank, K, nosmW * npsmW);
     }
     // every read of dat (the projection) and of redD (its cluster sums) is
     // behind this barrier: fetch the next position's intensities into dat

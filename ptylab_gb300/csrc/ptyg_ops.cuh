@@ -57,7 +57,8 @@ cudaError_t mix_modes(const float2* V, const float2* p, float2* out, int modes, 
 
 int set_last_error(int code, const char* msg);
 
-size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int nlambda, int engine, bool probe_in_smem);
+size_t engine_smem_bytes(int Np, int C, int nosm, int npsm, int nlambda, int engine, bool probe_in_smem,
+                         bool asp_table_in_smem);
 cudaError_t launch_engine(const EngineArgs& a, int nscans, int threads, size_t smem, cudaStream_t st);
 bool engine_modes_supported(int Np, int nosm, int npsm);
 bool engine_shape_supported(int Np, int cluster);

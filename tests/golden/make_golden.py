@@ -434,6 +434,23 @@ SCAN_CONFIGS = {
     "qnewton_savememory_background": dict(
         engine="qNewton", iters=3, W=True, params=dict(saveMemory=True, backgroundModeSwitch=True, FourierMaskSwitch=True)
     ),
+    # e3PIE's detector projection is BaseEngine's, every switch included (e3PIE.py:118)
+    "e3pie_exponential_fmask": dict(
+        engine="e3PIE", modes=(1, 1, 1, 3), iters=3, dz=2e-4, order="random", W=True, keep_detector_error=True,
+        params=dict(intensityConstraint="exponential", FourierMaskSwitch=True),
+    ),
+    "e3pie_background_denoise_modes": dict(
+        engine="e3PIE", modes=(1, 1, 2, 2), iters=3, dz=2e-4,
+        params=dict(backgroundModeSwitch=True, adaptiveDenoisingSwitch=True),
+    ),
+    "e3pie_fluctuation": dict(
+        engine="e3PIE", modes=(1, 1, 1, 2), iters=3, dz=2e-4, intensityScaling=True,
+        params=dict(intensityConstraint="fluctuation", probePowerCorrectionSwitch=True),
+    ),
+    "e3pie_asp_exponential_mask": dict(
+        engine="e3PIE", propagator="ASP", modes=(1, 1, 1, 2), iters=2, dz=2e-4, intensity_mask=True,
+        params=dict(intensityConstraint="exponential", intensityMask=True),
+    ),
 }
 
 FPM_CONFIGS = {

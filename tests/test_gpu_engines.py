@@ -28,7 +28,7 @@ def torch_cuda():
     return torch
 
 
-def run_fixture_gpu(fx, engine_name=None, iters=None):
+def run_fixture_gpu(fx, engine_name=None, iters=None, attrs=None):
     from ptylab_gb300 import DummyMonitor, Engines
 
     m, i, d, p, rec = containers(fx)
@@ -38,6 +38,8 @@ def run_fixture_gpu(fx, engine_name=None, iters=None):
     rec.probe = i["init_probe"].copy()
     eng = getattr(Engines, engine_name or str(m["engine"]))(rec, d, p, DummyMonitor())
     eng.numIterations = int(m["iters"]) if iters is None else iters
+    for k, v in (attrs or {}).items():
+        setattr(eng, k, v)
     if "momentum_method" in m and str(m["engine"]) == "mqNewton":
         eng.momentum_method = str(m["momentum_method"])
     np.random.seed(int(m["seed"]))
@@ -47,13 +49,26 @@ def run_fixture_gpu(fx, engine_name=None, iters=None):
 
 
 def reference_spread(fx):
-    """Relative error of the reference's complex64 result against a complex128
-    oracle run from the same inputs: the reference's own FP32 noise floor."""
+    """The reference's own FP32 noise floor on this case: how far its
+    complex64 result lies from a complex128 oracle run from the same inputs,
+    or from a complex64 oracle run whose initial probe differs by one part in
+    1e7 (a rounding-level change), whichever is larger.  The second term
+    matters only where the case amplifies rounding (a strongly mismatched
+    start, e.g. the unsquared constraints after probe-power correction);
+    elsewhere it is orders of magnitude below the first."""
     from oracle import ptyoracle as O
 
     st = O.run_fixture(fx, dtype=np.complex128)
+    moved = dict(fx)
+    p = fx["in_init_probe"]
+    moved["in_init_probe"] = (p * (1 + 1e-7 * np.random.default_rng(0).standard_normal(p.shape))).astype(p.dtype)
+    st2 = O.run_fixture(moved)
     keys = ("object", "probe", "error", "errorAtPos", "background", "intensityScaling", "reference")
-    return {k: rel_err(fx[f"out_{k}"], getattr(st, k)) for k in keys if f"out_{k}" in fx}
+    return {
+        k: max(rel_err(fx[f"out_{k}"], getattr(st, k)), rel_err(fx[f"out_{k}"], getattr(st2, k)))
+        for k in keys
+        if f"out_{k}" in fx
+    }
 
 
 @pytest.mark.parametrize("name", IN_SCOPE)
@@ -103,6 +118,22 @@ def test_engine_matches_reference_fixture(torch_cuda, name):
             if f"out_{key}" in fx and platform_reproduces_order(fx):
                 assert getattr(rec, key).shape == fx[f"out_{key}"].shape
                 assert rel_err(getattr(rec, key), fx[f"out_{key}"]) < max(1e-2, 3 * floor[part]), key
+
+
+@pytest.mark.parametrize("name", ["scan_epie_asp", "scan_epie_asp_denoise_background", "reg_epie_asp"])
+def test_asp_table_placement_agrees(torch_cuda, name):
+    """The ASP transfer function's CTA columns copied into shared memory once
+    per launch by the bulk-copy engine (asp_table_in_smem = 2, the default
+    where it fits) or read from global memory at every position (1): the same
+    reconstruction bit for bit, and both at the reference's result."""
+    fx = load_fixture(name)
+    rec_g, _ = run_fixture_gpu(fx, attrs={"aspTableInSmem": 1})
+    rec_s, _ = run_fixture_gpu(fx, attrs={"aspTableInSmem": 2})
+    for k in ("object", "probe", "error"):
+        np.testing.assert_array_equal(np.asarray(getattr(rec_g, k)), np.asarray(getattr(rec_s, k)))
+    if platform_reproduces_order(fx):
+        floor = reference_spread(fx)
+        assert rel_err(rec_s.object, fx["out_object"]) < max(TOL_FIXTURE, 3 * floor["object"])
 
 
 def test_engine_runs_are_deterministic(torch_cuda):

@@ -132,6 +132,10 @@ def test_new_entry_points_reject_bad_arguments_before_touching_a_device(lib):
     g = _native.Geometry(Np=64, No=128, nosm=1, npsm=1, nslice=1, num_frames=4, num_scans=1,
                          engine=_native.ENGINES["ePIE"], probe_in_smem=3)
     assert lib.ptyg_plan_create(C.byref(g), C.byref(plan)) == _native.PTYG_ERR_INVALID
+    g = _native.Geometry(Np=64, No=128, nosm=1, npsm=1, nslice=1, num_frames=4, num_scans=1,
+                         engine=_native.ENGINES["ePIE"], propagator=_native.PROPAGATORS["asp"], asp_table_in_smem=-1)
+    assert lib.ptyg_plan_create(C.byref(g), C.byref(plan)) == _native.PTYG_ERR_INVALID
+    assert b"asp_table_in_smem" in lib.ptyg_last_error()
     # the stitcher needs its buffers and No >= Np
     assert lib.ptyg_stitch(None, dummy, 1, 32, 64, dummy, dummy, dummy, None) == _native.PTYG_ERR_INVALID
     assert lib.ptyg_stitch(dummy, dummy, 1, 64, 32, dummy, dummy, dummy, None) == _native.PTYG_ERR_INVALID
