@@ -160,9 +160,9 @@ def algorithmic_counts(flags_per_step, nscans):
 
 
 # DRAM bytes per position of the batched launch, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum of a 15-scan launch / 6000
+# (dram__bytes.sum.per_second x gpu__time_duration of a 15-scan launch / 6000
 # positions; the summary is profiles/engine_kernel_mpie_c1.md)
-TRAFFIC_PER_POSITION = 406_993
+TRAFFIC_PER_POSITION = 410_520
 
 
 # ------------------------------------------------------------------ ranks

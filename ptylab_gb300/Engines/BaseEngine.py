@@ -566,16 +566,17 @@ class BaseEngine(object):
 
     def applyConstraints(self, loop):
         """In-scope subset of BaseEngine.applyConstraints (BaseEngine.py:1440-1500), in place on the device."""
-        torch = _torch()
         p, rec = self.params, self.reconstruction
-        lib = self._dev["lib"]
-        stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
         if p.orthogonalizationSwitch and np.mod(loop, p.orthogonalizationFrequency) == 0:
             self.orthogonalization()
         if p.probePowerCorrectionSwitch:
+            torch = _torch()
             norm = torch.sqrt(torch.sum(rec.probe * rec.probe.conj()))
             rec.probe.mul_(float(self.experimentalData.maxProbePower) / norm)
         if p.probeBoundary or p.absorbingProbeBoundary:
+            torch = _torch()
+            lib = self._dev["lib"]
+            stream = torch.cuda.current_stream(self._dev["device"]).cuda_stream
             w = self._window_device()
             if p.probeBoundary:
                 _native.check(
