@@ -89,23 +89,15 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       return (centred && ((y + x) & 1)) ? cscale(e, -1.f) : e;
     };
 
-    // ---------------- norms of the pre-update object slices and of P_0
-    {
-      float m[MAX_SLICES + 1];
-#pragma unroll
-      for (int q = 0; q <= MAX_SLICES; ++q) m[q] = 0.f;
-      for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-        const int l = i / NP, x = i % NP;
-#pragma unroll
-        for (int sl = 0; sl < MAX_SLICES; ++sl)
-          if (sl < S) m[sl] = fmaxf(m[sl], cabs2(ld_cg(Ob(sl) + (size_t)l * No + x)));
-        float sp = 0.f;
-        for (int p = 0; p < npsm; ++p) sp += cabs2(Pb(p, 0)[i]);
-        m[MAX_SLICES] = fmaxf(m[MAX_SLICES], sp);
-      }
-      const int idx[MAX_SLICES + 1] = {RED_SLICE_O,     RED_SLICE_O + 1, RED_SLICE_O + 2, RED_SLICE_O + 3,
-                                       RED_SLICE_O + 4, RED_SLICE_O + 5, RED_SLICE_P};
-      block_max_to_slots<MAX_SLICES + 1>(m, redF, red, idx);
+    // ---------------- the maxima the backward pass divides by: sum_p |P_s|^2
+    // and |O_s|^2 of the pre-update slices, each taken where the forward pass
+    // reads the slice anyway (slice 0 here and in its exit waves, slice s in
+    // its exit-wave loop), so no pass of its own reads the object slices
+    float mp0 = 0.f, mo0 = 0.f;
+    for (int i = threadIdx.x; i < LN; i += blockDim.x) {
+      float sp = 0.f;
+      for (int p = 0; p < npsm; ++p) sp += cabs2(Pb(p, 0)[i]);
+      mp0 = fmaxf(mp0, sp);
     }
 
     // ---------------- slice 0 exit waves, forward row FFT
@@ -117,11 +109,18 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
         a.twiddle, K * L,
         [&](int t, int lo, int hi) {
           const int p = t / L, l = t % L, x = lo + hi;
-          const float2 e = cmul(ld_cg(Ob(0) + (size_t)l * No + x), Pb(p, 0)[l * NP + x]);
+          const float2 o = ld_cg(Ob(0) + (size_t)l * No + x);
+          mo0 = fmaxf(mo0, cabs2(o));  // every pixel is some thread's, for every mode
+          const float2 e = cmul(o, Pb(p, 0)[l * NP + x]);
           Wb(0, p)[l * NP + x] = e;
           return (S == 1) ? detector_in(e, line0 + l, x) : e;
         },
         scatter, pairs);
+    {
+      float m[2] = {mp0, mo0};
+      const int idx[2] = {RED_SLICE_P, RED_SLICE_O};
+      block_max_to_slots<2>(m, redF, red, idx);
+    }
     cp_async_wait_all();  // this position's intensities (the one group in flight)
     cluster_sync(C);
 
@@ -139,11 +138,12 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           pairs);
       __syncthreads();
       {
-        float m[1] = {0.f};
+        float m[2] = {0.f, 0.f};
         const bool last = sl == S - 1;
         for (int i = threadIdx.x; i < LN; i += blockDim.x) {
           const int l = i / NP, x = i % NP;
           const float2 O = ld_cg(Ob(sl) + (size_t)l * No + x);
+          m[1] = fmaxf(m[1], cabs2(O));
           float sp = 0.f;
           for (int p = 0; p < npsm; ++p) {
             const float2 P = rows[p * LN + i];
@@ -154,8 +154,8 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
           }
           m[0] = fmaxf(m[0], sp);
         }
-        const int idx[1] = {RED_SLICE_P + sl};
-        block_max_to_slots<1>(m, redF, red, idx);
+        const int idx[2] = {RED_SLICE_P + sl, RED_SLICE_O + sl};
+        block_max_to_slots<2>(m, redF, red, idx);
       }
       __syncthreads();
       row_tasks<E, false>(
