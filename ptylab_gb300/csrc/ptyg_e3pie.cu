@@ -93,11 +93,27 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
     // and |O_s|^2 of the pre-update slices, each taken where the forward pass
     // reads the slice anyway (slice 0 here and in its exit waves, slice s in
     // its exit-wave loop), so no pass of its own reads the object slices
+    // (the pixel loops of this kernel keep U pixels' global loads in flight
+    // per thread before the first is used: the slices live in L2 or DRAM)
+    constexpr int U = 4;
     float mp0 = 0.f, mo0 = 0.f;
-    for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-      float sp = 0.f;
-      for (int p = 0; p < npsm; ++p) sp += cabs2(Pb(p, 0)[i]);
-      mp0 = fmaxf(mp0, sp);
+    for (int i0 = threadIdx.x; i0 < LN; i0 += U * (int)blockDim.x) {
+      float sp[U];
+#pragma unroll
+      for (int q = 0; q < U; ++q) sp[q] = 0.f;
+      for (int p = 0; p < npsm; ++p) {
+        float2 v[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+          const int i = i0 + q * (int)blockDim.x;
+          v[q] = Pb(p, 0)[i < LN ? i : i0];
+        }
+#pragma unroll
+        for (int q = 0; q < U; ++q) sp[q] += cabs2(v[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < U; ++q)
+        if (i0 + q * (int)blockDim.x < LN) mp0 = fmaxf(mp0, sp[q]);
     }
 
     // ---------------- slice 0 exit waves, forward row FFT
@@ -140,19 +156,31 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       {
         float m[2] = {0.f, 0.f};
         const bool last = sl == S - 1;
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-          const int l = i / NP, x = i % NP;
-          const float2 O = ld_cg(Ob(sl) + (size_t)l * No + x);
-          m[1] = fmaxf(m[1], cabs2(O));
-          float sp = 0.f;
-          for (int p = 0; p < npsm; ++p) {
-            const float2 P = rows[p * LN + i];
-            sp += cabs2(P);
-            const float2 e = cmul(P, O);
-            Wb(sl, p)[i] = e;
-            rows[p * LN + i] = last ? detector_in(e, line0 + l, x) : e;
+        for (int i0 = threadIdx.x; i0 < LN; i0 += U * (int)blockDim.x) {
+          float2 Ov[U];
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * (int)blockDim.x, ic = i < LN ? i : i0;
+            Ov[q] = ld_cg(Ob(sl) + (size_t)(ic / NP) * No + ic % NP);
           }
-          m[0] = fmaxf(m[0], sp);
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * (int)blockDim.x;
+            if (i < LN) {
+              const int l = i / NP, x = i % NP;
+              const float2 O = Ov[q];
+              m[1] = fmaxf(m[1], cabs2(O));
+              float sp = 0.f;
+              for (int p = 0; p < npsm; ++p) {
+                const float2 P = rows[p * LN + i];
+                sp += cabs2(P);
+                const float2 e = cmul(P, O);
+                Wb(sl, p)[i] = e;
+                rows[p * LN + i] = last ? detector_in(e, line0 + l, x) : e;
+              }
+              m[0] = fmaxf(m[0], sp);
+            }
+          }
         }
         const int idx[2] = {RED_SLICE_P + sl, RED_SLICE_O + sl};
         block_max_to_slots<2>(m, redF, red, idx);
@@ -242,21 +270,38 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
         const float invP = 1.f / slot_value(red, RED_SLICE_P + sl);
         const float invO = 1.f / slot_value(red, RED_SLICE_O + sl);
         const float stepP = (sl == 0) ? a.betaP : a.bethSlice;
-        for (int i = threadIdx.x; i < LN; i += blockDim.x) {
-          const int l = i / NP, x = i % NP;
-          float2* op = Ob(sl) + (size_t)l * No + x;
-          const float2 O = ld_cg(op);
-          float2 acc = make_float2(0.f, 0.f);
-          for (int p = 0; p < npsm; ++p) {
-            float2* pp = Pb(p, sl) + i;
-            const float2 P = *pp;
-            const float2 d = rows[p * LN + i];
-            acc = cadd(acc, cmulc(P, d));
-            const float2 Pn = cadd(P, cscale(cmulc(O, d), stepP * invO));
-            *pp = Pn;
-            rows[p * LN + i] = Pn;
+        for (int i0 = threadIdx.x; i0 < LN; i0 += U * (int)blockDim.x) {
+          float2 Ov[U], acc[U];
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * (int)blockDim.x, ic = i < LN ? i : i0;
+            Ov[q] = ld_cg(Ob(sl) + (size_t)(ic / NP) * No + ic % NP);
+            acc[q] = make_float2(0.f, 0.f);
           }
-          st_cg(op, cadd(O, cscale(acc, a.betaO * invP)));
+          for (int p = 0; p < npsm; ++p) {
+            float2 Pv[U];
+#pragma unroll
+            for (int q = 0; q < U; ++q) {
+              const int i = i0 + q * (int)blockDim.x;
+              Pv[q] = Pb(p, sl)[i < LN ? i : i0];
+            }
+#pragma unroll
+            for (int q = 0; q < U; ++q) {
+              const int i = i0 + q * (int)blockDim.x;
+              if (i < LN) {
+                const float2 d = rows[p * LN + i];
+                acc[q] = cadd(acc[q], cmulc(Pv[q], d));
+                const float2 Pn = cadd(Pv[q], cscale(cmulc(Ov[q], d), stepP * invO));
+                Pb(p, sl)[i] = Pn;
+                rows[p * LN + i] = Pn;
+              }
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * (int)blockDim.x;
+            if (i < LN) st_cg(Ob(sl) + (size_t)(i / NP) * No + i % NP, cadd(Ov[q], cscale(acc[q], a.betaO * invP)));
+          }
         }
       }
       if (sl > 0) {
