@@ -1053,7 +1053,7 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
         // 16-byte accesses (two pixels), MU of them per array in flight per
         // thread before any is used: the pass streams three arrays, so it
         // runs at what L2 delivers rather than one load latency per pixel
-        constexpr int MU = 2;
+        constexpr int MU = 4;
         const size_t n4 = nobj / 2;  // No even: whole float4s
         for (size_t i0 = (size_t)crank * blockDim.x + threadIdx.x; i0 < n4; i0 += MU * stride) {
           float4 X[MU], B[MU], M[MU];
@@ -1088,14 +1088,32 @@ __global__ void __launch_bounds__((VAR == VAR_MQ || VAR == VAR_MQ_POLY) ? 256 : 
           st_cg(s.objectBuffer + i, Xn);
         }
       }
-      for (int i = threadIdx.x; i < npsm * LN; i += blockDim.x) {
-        const int p = i / LN, rem = i - (i / LN) * LN;
-        const size_t gi = (size_t)p * NP * NP + (size_t)line0 * NP + rem;
-        float2 Xn, Mn;
-        step(sm.probe[p * pst + rem], s.probeBuffer[gi], s.probeMomentum[gi], Xn, Mn);
-        s.probeMomentum[gi] = Mn;
-        s.probeBuffer[gi] = Xn;
-        sm.probe[p * pst + rem] = Xn;
+      // the probe rows: PU elements' buffer and momentum loads in flight per
+      // thread before the first step
+      constexpr int PU = 4;
+      const int np = npsm * LN;
+      for (int i0 = threadIdx.x; i0 < np; i0 += PU * (int)blockDim.x) {
+        float2 B[PU], M[PU];
+#pragma unroll
+        for (int q = 0; q < PU; ++q) {
+          const int i = i0 + q * (int)blockDim.x, ic = i < np ? i : i0;
+          const size_t gi = (size_t)(ic / LN) * NP * NP + (size_t)line0 * NP + (ic - (ic / LN) * LN);
+          B[q] = s.probeBuffer[gi];
+          M[q] = s.probeMomentum[gi];
+        }
+#pragma unroll
+        for (int q = 0; q < PU; ++q) {
+          const int i = i0 + q * (int)blockDim.x;
+          if (i < np) {
+            const int p = i / LN, rem = i - (i / LN) * LN;
+            const size_t gi = (size_t)p * NP * NP + (size_t)line0 * NP + rem;
+            float2 Xn, Mn;
+            step(sm.probe[p * pst + rem], B[q], M[q], Xn, Mn);
+            s.probeMomentum[gi] = Mn;
+            s.probeBuffer[gi] = Xn;
+            sm.probe[p * pst + rem] = Xn;
+          }
+        }
       }
     }
     // qNewton's last cluster barrier (after pass C) already orders this
