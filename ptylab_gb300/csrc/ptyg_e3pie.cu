@@ -89,54 +89,61 @@ __global__ void __launch_bounds__(512, 1) e3pie_kernel(const EngineArgs a) {
       return (centred && ((y + x) & 1)) ? cscale(e, -1.f) : e;
     };
 
-    // ---------------- the maxima the backward pass divides by: sum_p |P_s|^2
-    // and |O_s|^2 of the pre-update slices, each taken where the forward pass
-    // reads the slice anyway (slice 0 here and in its exit waves, slice s in
-    // its exit-wave loop), so no pass of its own reads the object slices
-    // (the pixel loops of this kernel keep U pixels' global loads in flight
-    // per thread before the first is used: the slices live in L2 or DRAM)
+    // ---------------- slice 0 exit waves into the row buffers (and the
+    // exit-wave store), then the forward row FFT in place.  The maxima the
+    // backward pass divides by, sum_p |P_s|^2 and |O_s|^2 of the pre-update
+    // slices, are taken where the forward pass reads each slice anyway (slice
+    // 0 here, slice s in its exit-wave loop).  The pixel loops of this
+    // kernel keep U pixels' global loads in flight per thread before the
+    // first is used: the slices live in L2 or DRAM.
     constexpr int U = 4;
     float mp0 = 0.f, mo0 = 0.f;
     for (int i0 = threadIdx.x; i0 < LN; i0 += U * (int)blockDim.x) {
+      float2 Ov[U];
       float sp[U];
 #pragma unroll
-      for (int q = 0; q < U; ++q) sp[q] = 0.f;
+      for (int q = 0; q < U; ++q) {
+        const int i = i0 + q * (int)blockDim.x, ic = i < LN ? i : i0;
+        Ov[q] = ld_cg(Ob(0) + (size_t)(ic / NP) * No + ic % NP);
+        sp[q] = 0.f;
+      }
       for (int p = 0; p < npsm; ++p) {
-        float2 v[U];
+        float2 Pv[U];
 #pragma unroll
         for (int q = 0; q < U; ++q) {
           const int i = i0 + q * (int)blockDim.x;
-          v[q] = Pb(p, 0)[i < LN ? i : i0];
+          Pv[q] = Pb(p, 0)[i < LN ? i : i0];
         }
 #pragma unroll
-        for (int q = 0; q < U; ++q) sp[q] += cabs2(v[q]);
+        for (int q = 0; q < U; ++q) {
+          const int i = i0 + q * (int)blockDim.x;
+          if (i < LN) {
+            sp[q] += cabs2(Pv[q]);
+            const float2 e = cmul(Ov[q], Pv[q]);
+            Wb(0, p)[i] = e;
+            rows[p * LN + i] = (S == 1) ? detector_in(e, line0 + i / NP, i % NP) : e;
+          }
+        }
       }
 #pragma unroll
-      for (int q = 0; q < U; ++q)
-        if (i0 + q * (int)blockDim.x < LN) mp0 = fmaxf(mp0, sp[q]);
+      for (int q = 0; q < U; ++q) {
+        if (i0 + q * (int)blockDim.x < LN) {
+          mp0 = fmaxf(mp0, sp[q]);
+          mo0 = fmaxf(mo0, cabs2(Ov[q]));
+        }
+      }
     }
-
-    // ---------------- slice 0 exit waves, forward row FFT
+    {
+      float m[2] = {mp0, mo0};
+      const int idx[2] = {RED_SLICE_P, RED_SLICE_O};
+      block_max_to_slots<2>(m, redF, red, idx);  // (its CTA barrier also orders the row buffers)
+    }
     // every row-buffer line is a transform's own buffer (in place) or free
     auto row = [&](int t, int i) -> float2& { return rows[t * NP + i]; };
     auto pairs = [&](int t) { return reinterpret_cast<float4*>(rows + t * NP); };
     auto scatter = [&](int t, int lo, int hi, float2 v) { scatter_row<NP, L>(tile, t / L, line0 + t % L, lo, hi, v); };
     row_tasks<E, false>(
-        a.twiddle, K * L,
-        [&](int t, int lo, int hi) {
-          const int p = t / L, l = t % L, x = lo + hi;
-          const float2 o = ld_cg(Ob(0) + (size_t)l * No + x);
-          mo0 = fmaxf(mo0, cabs2(o));  // every pixel is some thread's, for every mode
-          const float2 e = cmul(o, Pb(p, 0)[l * NP + x]);
-          Wb(0, p)[l * NP + x] = e;
-          return (S == 1) ? detector_in(e, line0 + l, x) : e;
-        },
-        scatter, pairs);
-    {
-      float m[2] = {mp0, mo0};
-      const int idx[2] = {RED_SLICE_P, RED_SLICE_O};
-      block_max_to_slots<2>(m, redF, red, idx);
-    }
+        a.twiddle, K * L, [&](int t, int lo, int hi) { return row(t, lo + hi); }, scatter, pairs);
     cp_async_wait_all();  // this position's intensities (the one group in flight)
     cluster_sync(C);
 
