@@ -233,11 +233,13 @@ class BaseEngine(object):
         Np, No = int(rec.Np), int(rec.No)
         nosm, npsm, nslice = int(rec.nosm), int(rec.npsm), int(rec.nslice)
         nl = int(getattr(rec, "nlambda", 1))
-        # (a state array that is already a torch tensor is passed through as it is)
+        # (a state array that is already a torch tensor is passed through as it
+        # is; NumPy arrays of the right dtype are not copied: everything here
+        # is only read, on its way to the GPU)
         out = {}
         for name in self._state_fields():
             v = getattr(rec, name)
-            out[name] = v if hasattr(v, "detach") else np.asarray(v).astype(np.complex64)
+            out[name] = v if hasattr(v, "detach") else np.asarray(v).astype(np.complex64, copy=False)
         if tuple(out["object"].shape) != (nl, nosm, 1, nslice, No, No):
             raise ValueError(f"object shape {tuple(out['object'].shape)} != {(nl, nosm, 1, nslice, No, No)}")
         if tuple(out["probe"].shape) != (nl, 1, npsm, nslice, Np, Np):
@@ -249,7 +251,7 @@ class BaseEngine(object):
         if positions.min() < 0 or positions.max() > No - Np:
             raise ValueError(f"scan positions fall outside the {No}x{No} object (patch {Np})")
         out["positions"] = positions
-        out["ptychogram"] = np.asarray(_host(d.ptychogram)).astype(np.float32)
+        out["ptychogram"] = np.asarray(_host(d.ptychogram)).astype(np.float32, copy=False)
         return out
 
     def _device_state(self):
@@ -276,11 +278,9 @@ class BaseEngine(object):
         # a ring of pinned staging buffers for the per-iteration order and
         # momentum flags: the host fills slot n while the copies of earlier
         # iterations may still be queued; slot n's event (its last copy)
-        # is waited on before the slot is reused
-        self._upload_ring = [
-            (torch.zeros(nf, dtype=torch.int32).pin_memory(), torch.zeros(nf, dtype=torch.uint8).pin_memory())
-            for _ in range(_UPLOAD_SLOTS)
-        ]
+        # is waited on before the slot is reused.  Allocated at the first
+        # upload (a batch stages every scan's rows in its own ring instead)
+        self._upload_ring = None
         self._upload_events = [None] * _UPLOAD_SLOTS
         self._uploads = 0
         self._err_dev = None  # per-iteration frame sums awaiting readback
@@ -428,6 +428,12 @@ class BaseEngine(object):
             self._batch.stage(self._batch_row, self.positionIndices, momentum)
             return
         torch = _torch()
+        if self._upload_ring is None:
+            nf = int(self.experimentalData.numFrames)
+            self._upload_ring = [
+                (torch.zeros(nf, dtype=torch.int32).pin_memory(), torch.zeros(nf, dtype=torch.uint8).pin_memory())
+                for _ in range(_UPLOAD_SLOTS)
+            ]
         slot = self._uploads % _UPLOAD_SLOTS
         if self._upload_events[slot] is not None:
             self._upload_events[slot].synchronize()
