@@ -4,7 +4,7 @@ reference's algorithm, bit-exact to the reference on its own goldens).
 Each case runs the GB300 engine through PtyLab's surface and the oracle in
 complex64 (the reference's own precision) and complex128 from the same
 seeded data, initial guesses, position order and momentum draws.  The bar is
-the benchmark spec's relative L2 error (1e-4; 5e-4 for multislice and FPM) wherever
+the parity target's relative L2 error (1e-4; 5e-4 for multislice and FPM) wherever
 the reference's own complex64-vs-complex128 spread leaves room for it, and
 otherwise a small multiple of that spread: mPIE's momentum and qNewton's
 normalisations amplify rounding chaotically, so two FP32 implementations of

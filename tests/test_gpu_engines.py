@@ -319,7 +319,7 @@ def test_config0_size_precision_vs_complex128(torch_cuda, engine):
     gpu_vs_64 = {k: rel_err(getattr(rec, k), getattr(r64, k)) for k in keys}
     msg = f"{engine}: gpu-c128 {gpu_vs_128} ref-c128 {ref_vs_128} gpu-ref {gpu_vs_64}"
     print(msg)
-    # the benchmark spec's 1e-4 wherever the reference's own spread leaves room for
+    # the 1e-4 parity target wherever the reference's own spread leaves room for
     # it (ePIE object and error curve), else a small multiple of that spread
     chaos = 4.0 if engine == "mPIE" else 3.0
     for k in keys:
